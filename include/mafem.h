@@ -1,0 +1,164 @@
+/*
+ * mafem.h -- C ABI of libmafem.so, the GB300 (sm_103a) assemble-and-solve
+ * library for MembraneAleFem.jl's Newton step.
+ *
+ * The library replaces the two lines of the reference's `time_step!`
+ *     r_gl, K_gl = calc_r_K(mesh, xms, cps, time, Δt, p; args...)   # src/analysis/FiniteElement.jl:35
+ *     Δu = -K_gl \ r_gl                                              # src/analysis/FiniteElement.jl:38
+ * and, optionally, the whole Newton loop around them (FiniteElement.jl:11-63).
+ * Mesh construction, input preparation and the time loop stay with the caller
+ * (src/Input.jl, src/Analysis.jl), exactly as in the reference.
+ *
+ * Conventions
+ *  - Every array that crosses this boundary uses the reference's layout:
+ *    Julia column-major, 1-based node / unknown numbers, 0 = Dirichlet in ID.
+ *    xms is numnp x 3 and cps is numnp x ndf (column-major, Float64).
+ *  - Return codes: 0 = OK; > 0 = numerical outcome (the cases where the
+ *    reference @asserts); < 0 = usage, CUDA or memory error.  The message of
+ *    the last failure is available from mafem_last_error().
+ *  - A handle is used by one host thread at a time.  Handles are independent.
+ *  - No function allocates device memory after mafem_create(); every device
+ *    buffer of a handle is allocated there and freed by mafem_destroy().
+ */
+#ifndef MAFEM_H
+#define MAFEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define MAFEM_OK 0
+#define MAFEM_NEWTON_NOT_CONVERGED 1 /* FiniteElement.jl:61 @assert */
+#define MAFEM_ZERO_PIVOT 2           /* exactly singular tangent */
+#define MAFEM_NAN_DETECTED 3         /* non-finite residual or update */
+#define MAFEM_REFINE_STALLED 4       /* FP32 factor + FP64 refinement did not converge */
+#define MAFEM_ERR_ARG (-1)
+#define MAFEM_ERR_CUDA (-2)
+#define MAFEM_ERR_OOM (-3)
+#define MAFEM_ERR_UNSUPPORTED (-4)
+#define MAFEM_ERR_ADMISSION (-5)
+
+/* ---- enums: same numeric values as the reference (src/input/Enums.jl) --------- */
+enum mafem_motion { MAFEM_STATIC = 1, MAFEM_EUL = 2, MAFEM_LAG = 3, MAFEM_ALEV = 4, MAFEM_ALEVB = 5 };
+enum mafem_scenario { MAFEM_F_CAVI = 1, MAFEM_F_COUE = 2, MAFEM_F_POIS = 3, MAFEM_F_PULL = 4, MAFEM_F_BEND = 5 };
+enum mafem_boundary { MAFEM_BOTTOM = 1, MAFEM_RIGHT = 2, MAFEM_TOP = 3, MAFEM_LEFT = 4 };
+enum mafem_neumann { MAFEM_SHEAR = 1, MAFEM_STRETCH = 2, MAFEM_MOMENT = 3 };
+
+/* Linear-algebra form of a handle. */
+enum mafem_precision {
+  MAFEM_PLAIN_FP64 = 0, /* FP64 tangent, FP64 banded LU with partial pivoting */
+  MAFEM_FP32_REFINE = 1 /* FP64 residual; FP32 tangent and FP32 banded LU whose
+                           trailing updates are 3xTF32 tensor-core products;
+                           FP64 iterative refinement of every solve */
+};
+
+/* Params (src/input/Params.jl:36-55), field for field. */
+typedef struct mafem_params {
+  int32_t motion, scenario, num1el, num2el;
+  double length, kb, kg, zeta_v, pn;
+  int32_t poly, gp1d, nders, nen;
+  double alpha_db, alpha_m, eps_k, eps_nr;
+} mafem_params;
+
+/* The keyword arguments (`args...`) the hot path reads:
+ * pull_speed (src/input/Bc.jl:234,240), bend_tm and bend_mf
+ * (src/analysis/FiniteElement.jl:379, src/input/Bc.jl:389-390). */
+typedef struct mafem_args {
+  double pull_speed, bend_tm, bend_mf;
+} mafem_args;
+
+/* A view of the reference's `Mesh` struct (src/input/Mesh.jl:48-80): the fields
+ * the hot path reads, in the reference's own layout.  A Julia caller fills it
+ * from its `mesh`; mafem_mesh_view() fills it from a mesh
+ * built by mafem_mesh_build().  GP tables pack one GpBasisFnsζα
+ * (src/input/GpBasisFn.jl:96-112) as 55 doubles: w, N[9], ∂Nα (9x2
+ * column-major), ∂∂Nαβ (9x3 column-major, Voigt order 11, 22, 12). */
+typedef struct mafem_mesh_desc {
+  int64_t num1el, num2el, numel, num1np, num2np, numnp, ndf, nmdf;
+  int64_t dofs[8];        /* mesh.dofs[Dof.vx .. Dof.pm]: 1-based dof index, 0 if absent */
+  const int64_t* IX;      /* mesh.IX: 9 x numel, 1-based node numbers */
+  const int64_t* ID;      /* mesh.ID: ndf x numnp, 1-based unknown numbers, 0 = Dirichlet */
+  int64_t n_uel;          /* size(mesh.area_gp_fns.ufns, 1) */
+  const int64_t* uel_ids; /* mesh.area_gp_fns.uel_ids (numel, 1-based) */
+  const double* ufns;     /* mesh.area_gp_fns.ufns: [uel][gp 1..9] x 55 */
+  int64_t bdry_n_uel[4];            /* per Boundary (BOTTOM, RIGHT, TOP, LEFT) */
+  const int64_t* bdry_uel_ids[4];   /* mesh.bdry_gp_fns[b].uel_ids (num1el or num2el) */
+  const double* bdry_ufns[4];       /* mesh.bdry_gp_fns[b].ufns: [uel][gp 1..3] x 55 */
+  int64_t n_neu;                    /* length(mesh.inh_neu_bcs) (<= 8) */
+  const int64_t* neu_bdry;          /* Boundary of each entry */
+  const int64_t* neu_type;          /* Neumann type of each entry */
+  const double* neu_val;            /* value of each entry */
+  int64_t n_dir;                    /* length(mesh.inh_dir_bcs) */
+  const int64_t* dir_unknown;       /* Dof.Unknown of each entry (1..8) */
+  const int64_t* dir_node;          /* node (1-based) */
+  const double* dir_val;            /* value */
+} mafem_mesh_desc;
+
+typedef struct mafem_mesh mafem_mesh;     /* host mesh owned by the library */
+typedef struct mafem_handle mafem_handle; /* device-resident solver state */
+
+typedef struct mafem_step_stats {
+  int32_t newton_iters;       /* Newton iterations taken */
+  int32_t refine_iters;       /* total refinement sweeps (FP32 form) */
+  double eps[14];             /* ‖Δu‖₂ / nmdf per iteration (FiniteElement.jl:48) */
+  double res_norm[14];        /* ‖r‖₂ at the start of each iteration */
+  double ms_assemble, ms_factor, ms_solve, ms_total; /* device time */
+} mafem_step_stats;
+
+/* ---- host mesh (restates Mesh(p; args...) and prepare_input) ----------------- */
+
+/* Mesh(p; args...) -- src/input/Mesh.jl:79,94-302, src/input/Bc.jl. */
+int mafem_mesh_build(const mafem_params* p, const mafem_args* a, mafem_mesh** out);
+/* Fill `out` with pointers into `m` (valid until mafem_mesh_free). */
+int mafem_mesh_view(const mafem_mesh* m, mafem_mesh_desc* out);
+void mafem_mesh_free(mafem_mesh* m);
+/* prepare_input's default initial state (src/Input.jl:40-108, non-F_BEND
+ * scenarios): xms numnp x 3 and cps numnp x ndf, column-major. */
+int mafem_prepare_input(const mafem_mesh* m, const mafem_params* p, double* xms, double* cps);
+/* Half bandwidth of K in the reference's ID ordering. */
+int64_t mafem_mesh_half_bandwidth(const mafem_mesh_desc* d);
+
+/* ---- device handle ------------------------------------------------------------ */
+
+/* Allocate every device buffer for one patch and upload the mesh tables. */
+int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, const mafem_args* a,
+                 int32_t precision, mafem_handle** out);
+int mafem_destroy(mafem_handle* h);
+const char* mafem_last_error(const mafem_handle* h); /* h may be NULL */
+/* Bytes of device memory the handle holds (state + band factor + staging). */
+int64_t mafem_device_bytes(const mafem_handle* h);
+/* Same figure for a mesh before creating a handle (admission control). */
+int64_t mafem_footprint_bytes(const mafem_mesh_desc* d, int32_t precision);
+
+/* Copy state host -> device / device -> host (xms numnp x 3, cps numnp x ndf). */
+int mafem_upload_state(mafem_handle* h, const double* xms, const double* cps);
+int mafem_download_state(mafem_handle* h, double* xms, double* cps);
+
+/* calc_r_K (FiniteElement.jl:75-200) on the resident state.  r_out (nmdf) may be
+ * NULL.  If band_out is not NULL it receives K in LAPACK band layout: column j
+ * (0-based) at band_out + j*ldab_out, A(i,j) at row kl+ku+i-j with
+ * kl = ku = mafem_mesh_half_bandwidth(); the top kl rows are zero. */
+int mafem_calc_r_K(mafem_handle* h, double time, double dt, double* r_out, double* band_out,
+                   int64_t ldab_out);
+/* Δu = -K \ r for the K of the last mafem_calc_r_K and a host r (nmdf). */
+int mafem_solve(mafem_handle* h, const double* r, double* du_out);
+/* update_xms! (FiniteElement.jl:408-423) on the resident state: the predictor
+ * xms[:, j] += Δt * cps[:, m_motion_order[j]] (Analysis.jl:193). */
+int mafem_predict(mafem_handle* h, double dt);
+/* time_step! (FiniteElement.jl:11-63) on the resident state. */
+int mafem_time_step(mafem_handle* h, double time, double dt, mafem_step_stats* stats);
+/* time_step! with host state: upload xms/cps, Newton on the device, download
+ * the updated xms/cps into the same arrays -- the drop-in for the reference. */
+int mafem_time_step_host(mafem_handle* h, double* xms, double* cps, double time, double dt,
+                         mafem_step_stats* stats);
+/* run_analysis!'s time loop (src/Analysis.jl:183-216) on the resident state:
+ * predictor + time_step! for each Δt; times[k] = t0 + sum(dts[0..k]). */
+int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, mafem_step_stats* last);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MAFEM_H */

@@ -1,0 +1,692 @@
+// api.cu -- device handle, Newton driver and the C ABI of include/mafem.h.
+//
+// time_step! (src/analysis/FiniteElement.jl:11-63) runs on the device: per
+// Newton iteration the element kernel, the band/residual gathers, the banded
+// LU (FP64, or FP32 + FP64 refinement), the back substitution and the state
+// update are stream-ordered launches; the host reads back three doubles per
+// iteration (ε, ‖r‖, a NaN flag) to apply the reference's stopping rule
+// (`iter < 15`, `ε < εnr`).
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "mafem.h"
+#include "mafem_internal.h"
+
+namespace mafem {
+
+static std::mutex g_err_mu;
+static std::string g_err;
+void set_global_error(const std::string& s) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_err = s;
+}
+
+int64_t half_bandwidth(const mafem_mesh_desc& d) {
+  int64_t b = 0;
+  for (int64_t e = 0; e < d.numel; ++e) {
+    int64_t lo = INT64_MAX, hi = -1;
+    for (int a = 0; a < 9; ++a) {
+      int64_t node = d.IX[a + 9 * e] - 1;
+      for (int64_t k = 0; k < d.ndf; ++k) {
+        int64_t g = d.ID[k + d.ndf * node];
+        if (g > 0) {
+          lo = std::min(lo, g);
+          hi = std::max(hi, g);
+        }
+      }
+    }
+    if (hi >= 0) b = std::max(b, hi - lo);
+  }
+  return b;
+}
+
+// Panel width: the FP64 panel and its trailing-update CTA keep (nb + kl) x nb
+// values in shared memory.
+static int choose_nb(int kl, int precision) {
+  const size_t limit = 200 * 1024;
+  const size_t esz = precision == MAFEM_PLAIN_FP64 ? 8 : 4;
+  for (int nb : {32, 16, 8}) {
+    size_t R = (size_t)nb + kl;
+    size_t apply = R * nb * esz + 8 * R * esz + R * 4;
+    if (apply <= limit) return nb;
+  }
+  return 0;
+}
+
+}  // namespace mafem
+
+using namespace mafem;
+
+struct mafem_handle {
+  std::string err;
+  int precision = 0;
+  mafem_params p{};
+  mafem_args a{};
+  int ndf = 0, nq = 0, numel = 0, numnp = 0;
+  int64_t nmdf = 0;
+  DevPatch P{};
+  PhysParams pp{};
+  BandLayout L{};
+  int rmax = 0;
+  int64_t npan = 0;
+  int apply_threads = 256, apply_blocks = 152;
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+  double *d_rel = nullptr, *d_r = nullptr, *d_x = nullptr, *d_res = nullptr, *d_dx = nullptr;
+  double *d_part = nullptr, *d_out = nullptr;
+  void *d_Kel = nullptr, *d_band = nullptr, *d_band0 = nullptr;
+  int *d_ipiv = nullptr, *d_perm = nullptr, *d_info = nullptr;
+  double* h_out = nullptr;  // pinned: [0] eps [1] |r| [2] nan [3] refine |res| [4] info
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[6] = {};
+  bool factored = false;
+  int max_refine = 30;
+  double refine_tol = 1e-10;
+};
+
+#define CK(x)                                                               \
+  do {                                                                      \
+    cudaError_t e_ = (x);                                                   \
+    if (e_ != cudaSuccess) {                                                \
+      h->err = std::string(#x) + ": " + cudaGetErrorString(e_);             \
+      return MAFEM_ERR_CUDA;                                                \
+    }                                                                       \
+  } while (0)
+
+template <class X>
+static int dalloc(mafem_handle* h, X** p, size_t count) {
+  void* v = nullptr;
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(X);
+  cudaError_t e = cudaMalloc(&v, bytes);
+  if (e != cudaSuccess) {
+    h->err = std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? MAFEM_ERR_OOM : MAFEM_ERR_CUDA;
+  }
+  h->allocs.push_back(v);
+  h->bytes += (int64_t)bytes;
+  *p = reinterpret_cast<X*>(v);
+  return MAFEM_OK;
+}
+template <class X>
+static int dupload(mafem_handle* h, X** p, const std::vector<X>& v) {
+  int rc = dalloc(h, p, v.size());
+  if (rc) return rc;
+  CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice));
+  return MAFEM_OK;
+}
+
+// Gᵀ H⁻¹ G of the Dohrmann-Bochev projection (FiniteElement.jl:279-323) for one
+// unique element: G = Σ NDB Nᵀ w, H = Σ NDB NDBᵀ w, NDB = (ξ¹, ξ², 1).
+static void db_matrix(const double* uf /* 9 x 55 */, double out[81]) {
+  const double xi[3] = {-std::sqrt(3.0 / 5), 0.0, std::sqrt(3.0 / 5)};
+  double G[3][9] = {}, H[3][3] = {};
+  for (int gp = 0; gp < 9; ++gp) {
+    const double* f = uf + gp * 55;
+    const double w = f[0];
+    const double nd[3] = {xi[gp % 3], xi[gp / 3], 1.0};
+    for (int r = 0; r < 3; ++r) {
+      for (int a = 0; a < 9; ++a) G[r][a] += nd[r] * f[1 + a] * w;
+      for (int c = 0; c < 3; ++c) H[r][c] += nd[r] * nd[c] * w;
+    }
+  }
+  // 3x3 inverse by cofactors
+  double c00 = H[1][1] * H[2][2] - H[1][2] * H[2][1], c01 = H[1][2] * H[2][0] - H[1][0] * H[2][2],
+         c02 = H[1][0] * H[2][1] - H[1][1] * H[2][0];
+  double det = H[0][0] * c00 + H[0][1] * c01 + H[0][2] * c02;
+  double Hi[3][3] = {{c00 / det, (H[0][2] * H[2][1] - H[0][1] * H[2][2]) / det, (H[0][1] * H[1][2] - H[0][2] * H[1][1]) / det},
+                     {c01 / det, (H[0][0] * H[2][2] - H[0][2] * H[2][0]) / det, (H[0][2] * H[1][0] - H[0][0] * H[1][2]) / det},
+                     {c02 / det, (H[0][1] * H[2][0] - H[0][0] * H[2][1]) / det, (H[0][0] * H[1][1] - H[0][1] * H[1][0]) / det}};
+  double HG[3][9];
+  for (int r = 0; r < 3; ++r)
+    for (int a = 0; a < 9; ++a) HG[r][a] = Hi[r][0] * G[0][a] + Hi[r][1] * G[1][a] + Hi[r][2] * G[2][a];
+  for (int a = 0; a < 9; ++a)
+    for (int b = 0; b < 9; ++b) out[a * 9 + b] = G[0][a] * HG[0][b] + G[1][a] * HG[1][b] + G[2][a] * HG[2][b];
+}
+
+static int validate(const mafem_mesh_desc* d, const mafem_params* p, std::string& err) {
+  if (!d || !p) { err = "null argument"; return MAFEM_ERR_ARG; }
+  if (p->poly != 2 || p->nen != 9 || p->nders != 2 || p->gp1d != 3) {
+    err = "only poly = 2, nen = 9, nders = 2, gp1d = 3 are supported (Params.jl:93-95)";
+    return MAFEM_ERR_UNSUPPORTED;
+  }
+  if (d->ndf < 1 || d->ndf > 8 || d->numel != d->num1el * d->num2el || d->numnp != d->num1np * d->num2np ||
+      d->num1np != d->num1el + 2 || d->num2np != d->num2el + 2 || d->nmdf < 1) {
+    err = "inconsistent mesh sizes (flat patch expected: num?np = num?el + 2)";
+    return MAFEM_ERR_ARG;
+  }
+  if (!d->IX || !d->ID || !d->uel_ids || !d->ufns) { err = "missing mesh arrays"; return MAFEM_ERR_ARG; }
+  if (d->n_neu < 0 || d->n_neu > kMaxNeu) { err = "at most 8 Neumann entries are supported"; return MAFEM_ERR_ARG; }
+  for (int64_t k = 0; k < d->n_neu; ++k) {
+    if (d->neu_bdry[k] < 1 || d->neu_bdry[k] > 4) { err = "bad Neumann boundary"; return MAFEM_ERR_ARG; }
+    int t = (int)d->neu_type[k];
+    if (t != MAFEM_STRETCH && t != MAFEM_SHEAR && !(t == MAFEM_MOMENT && p->scenario == MAFEM_F_BEND)) {
+      err = "Neumann boundary condition not implemented (FiniteElement.jl:382)";
+      return MAFEM_ERR_UNSUPPORTED;
+    }
+  }
+  if (p->motion < MAFEM_STATIC || p->motion > MAFEM_ALEVB) { err = "unknown motion"; return MAFEM_ERR_ARG; }
+  return MAFEM_OK;
+}
+
+static int64_t footprint(const mafem_mesh_desc* d, int precision, int64_t kl) {
+  const int nb = choose_nb((int)kl, precision);
+  BandLayout L = make_band_layout(d->nmdf, (int)kl, (int)kl, nb ? nb : 8);
+  const int64_t esz = precision == MAFEM_PLAIN_FP64 ? 8 : 4;
+  const int64_t nq = 9 * d->ndf;
+  int64_t b = L.ldb * d->nmdf * esz * (precision == MAFEM_PLAIN_FP64 ? 1 : 2);  // band (+ unfactored copy)
+  b += d->numel * nq * nq * esz + d->numel * nq * 8;                             // element staging
+  b += d->numnp * (3 + d->ndf) * 8 + d->nmdf * 8 * 6;                           // state + vectors
+  b += ((d->nmdf + nb - 1) / std::max(nb, 1)) * ((int64_t)nb + kl) * 4;           // panel permutations
+  return b;
+}
+
+extern "C" int64_t mafem_mesh_half_bandwidth(const mafem_mesh_desc* d) { return d ? half_bandwidth(*d) : -1; }
+
+extern "C" int64_t mafem_footprint_bytes(const mafem_mesh_desc* d, int32_t precision) {
+  if (!d || !d->IX || !d->ID) return -1;
+  return footprint(d, precision, half_bandwidth(*d));
+}
+
+extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, const mafem_args* a,
+                            int32_t precision, mafem_handle** out) {
+  if (!out) return MAFEM_ERR_ARG;
+  *out = nullptr;
+  std::string err;
+  int rc = validate(d, p, err);
+  if (rc) {
+    set_global_error(err);
+    return rc;
+  }
+  if (precision != MAFEM_PLAIN_FP64 && precision != MAFEM_FP32_REFINE) {
+    set_global_error("unknown precision mode");
+    return MAFEM_ERR_ARG;
+  }
+  auto hp = std::make_unique<mafem_handle>();
+  mafem_handle* h = hp.get();
+  h->precision = precision;
+  h->p = *p;
+  if (a) h->a = *a;
+  h->ndf = (int)d->ndf;
+  h->nq = 9 * h->ndf;
+  h->numel = (int)d->numel;
+  h->numnp = (int)d->numnp;
+  h->nmdf = d->nmdf;
+  const int ndf = h->ndf, nq = h->nq, numel = h->numel, numnp = h->numnp;
+  const int64_t n = h->nmdf;
+
+  // physics parameters and dof maps
+  PhysParams& pp = h->pp;
+  std::memset(&pp, 0, sizeof pp);
+  pp.motion = p->motion;
+  pp.scenario = p->scenario;
+  pp.ndf = ndf;
+  pp.nq = nq;
+  pp.kb = p->kb; pp.kg = p->kg; pp.zv = p->zeta_v; pp.pn = p->pn; pp.adb = p->alpha_db; pp.am = p->alpha_m;
+  pp.bend_tm = h->a.bend_tm;
+  for (int u = 0; u < 8; ++u) pp.dof_of[u] = (int)d->dofs[u] - 1;
+  for (int k = 0; k < 8; ++k) pp.unk_of[k] = -1;
+  for (int u = 0; u < 8; ++u)
+    if (pp.dof_of[u] >= 0) pp.unk_of[pp.dof_of[u]] = u;
+  for (int j = 0; j < 3; ++j) {  // get_m_motion_order (Mesh.jl:529-542)
+    if (p->motion == MAFEM_STATIC) pp.mmo[j] = -1;
+    else if (p->motion == MAFEM_LAG) pp.mmo[j] = pp.dof_of[j];
+    else pp.mmo[j] = pp.dof_of[3 + j];
+  }
+  if (pp.dof_of[6] < 0) {
+    set_global_error("λ must be an unknown (FiniteElement.jl:235)");
+    return MAFEM_ERR_ARG;
+  }
+  pp.n_neu = (int)d->n_neu;
+  for (int k = 0; k < pp.n_neu; ++k) {
+    pp.neu_bdry[k] = (int)d->neu_bdry[k] - 1;
+    pp.neu_type[k] = (int)d->neu_type[k];
+    pp.neu_val[k] = d->neu_val[k];
+  }
+
+  // integer maps (0-based int32)
+  std::vector<int> ix((size_t)numel * 9), lm((size_t)numel * nq), uel(numel), bref((size_t)numel * 4, -1);
+  for (int e = 0; e < numel; ++e)
+    for (int b = 0; b < 9; ++b) ix[e * 9 + b] = (int)(d->IX[b + 9 * (int64_t)e] - 1);
+  for (int e = 0; e < numel; ++e)
+    for (int b = 0; b < 9; ++b)
+      for (int k = 0; k < ndf; ++k) lm[(size_t)e * nq + b * ndf + k] = (int)(d->ID[k + ndf * (int64_t)ix[e * 9 + b]] - 1);
+  for (int e = 0; e < numel; ++e) uel[e] = (int)(d->uel_ids[e] - 1);
+  std::vector<int> unk_node(n), unk_dof(n), node_unk((size_t)numnp * ndf, -1);
+  for (int nd = 0; nd < numnp; ++nd)
+    for (int k = 0; k < ndf; ++k) {
+      int64_t g = d->ID[k + ndf * (int64_t)nd];
+      if (g > 0) {
+        if (g > n) {
+          set_global_error("ID entry larger than nmdf");
+          return MAFEM_ERR_ARG;
+        }
+        unk_node[g - 1] = nd;
+        unk_dof[g - 1] = k;
+        node_unk[(size_t)nd * ndf + k] = (int)(g - 1);
+      }
+    }
+  // GP tables padded to kTab doubles per record
+  std::vector<double> tab((size_t)d->n_uel * 9 * kTab, 0.0), db((size_t)d->n_uel * 81);
+  for (int64_t u = 0; u < d->n_uel; ++u) {
+    for (int g = 0; g < 9; ++g)
+      std::memcpy(&tab[((size_t)u * 9 + g) * kTab], d->ufns + ((size_t)u * 9 + g) * 55, 55 * sizeof(double));
+    db_matrix(d->ufns + (size_t)u * 9 * 55, &db[(size_t)u * 81]);
+  }
+  // boundary tables and the per-element boundary row map (Mesh.jl:126-131,
+  // get_basis_fns(bdry, ...) Mesh.jl:390-403)
+  std::vector<double> btab;
+  int64_t boff[4];
+  {
+    int64_t rows = 0;
+    for (int b = 0; b < 4; ++b) {
+      boff[b] = rows;
+      rows += d->bdry_n_uel[b];
+    }
+    btab.assign((size_t)std::max<int64_t>(rows, 1) * 3 * kTab, 0.0);
+    for (int b = 0; b < 4; ++b)
+      for (int64_t u = 0; u < d->bdry_n_uel[b]; ++u)
+        for (int g = 0; g < 3; ++g)
+          std::memcpy(&btab[((size_t)(boff[b] + u) * 3 + g) * kTab], d->bdry_ufns[b] + ((size_t)u * 3 + g) * 55,
+                      55 * sizeof(double));
+    const int n1 = (int)d->num1el, n2 = (int)d->num2el;
+    for (int e2 = 0; e2 < n2; ++e2)
+      for (int e1 = 0; e1 < n1; ++e1) {
+        const int e = e1 + n1 * e2;
+        auto set = [&](int b, int bel) {
+          if (d->bdry_uel_ids[b] && d->bdry_n_uel[b] > 0) bref[e * 4 + b] = (int)(boff[b] + d->bdry_uel_ids[b][bel] - 1);
+        };
+        if (e2 == 0) set(0, e1);        // BOTTOM
+        if (e1 == n1 - 1) set(1, e2);   // RIGHT
+        if (e2 == n2 - 1) set(2, e1);   // TOP
+        if (e1 == 0) set(3, e2);        // LEFT
+      }
+  }
+  const int64_t kl = half_bandwidth(*d);
+  const int nb = choose_nb((int)kl, precision);
+  if (!nb) {
+    set_global_error("half bandwidth too large for the banded LU's shared-memory panel");
+    return MAFEM_ERR_UNSUPPORTED;
+  }
+  h->L = make_band_layout(n, (int)kl, (int)kl, nb);
+  h->npan = (n + nb - 1) / nb;
+  h->rmax = nb + (int)kl;
+
+  cudaError_t ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    set_global_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
+    return MAFEM_ERR_CUDA;
+  }
+  for (auto& e : h->ev) cudaEventCreate(&e);
+  int* d_ix;
+  int* d_lm;
+  int* d_uel;
+  int* d_bref;
+  int *d_un, *d_ud, *d_nu;
+  double *d_tab, *d_db, *d_btab;
+#define UP(ptr, vec)                          \
+  do {                                        \
+    int r_ = dupload(h, &ptr, vec);           \
+    if (r_) {                                 \
+      set_global_error(h->err);               \
+      mafem_destroy(hp.release());            \
+      return r_;                              \
+    }                                         \
+  } while (0)
+#define AL(ptr, cnt)                          \
+  do {                                        \
+    int r_ = dalloc(h, &ptr, cnt);            \
+    if (r_) {                                 \
+      set_global_error(h->err);               \
+      mafem_destroy(hp.release());            \
+      return r_;                              \
+    }                                         \
+  } while (0)
+  UP(d_ix, ix);
+  UP(d_lm, lm);
+  UP(d_uel, uel);
+  UP(d_bref, bref);
+  UP(d_un, unk_node);
+  UP(d_ud, unk_dof);
+  UP(d_nu, node_unk);
+  UP(d_tab, tab);
+  UP(d_db, db);
+  UP(d_btab, btab);
+  double *d_xms, *d_cps;
+  AL(d_xms, (size_t)numnp * 3);
+  AL(d_cps, (size_t)numnp * ndf);
+  AL(h->d_rel, (size_t)numel * nq);
+  AL(h->d_r, n);
+  AL(h->d_x, n);
+  AL(h->d_res, n);
+  AL(h->d_dx, n);
+  AL(h->d_part, 2048);
+  AL(h->d_out, 16);
+  AL(h->d_ipiv, n);
+  AL(h->d_perm, (size_t)h->npan * h->rmax);
+  AL(h->d_info, 4);
+  const size_t band_elems = (size_t)h->L.ldb * n;
+  if (precision == MAFEM_PLAIN_FP64) {
+    double *kel, *band;
+    AL(kel, (size_t)numel * nq * nq);
+    AL(band, band_elems);
+    h->d_Kel = kel;
+    h->d_band = band;
+  } else {
+    float *kel, *band, *band0;
+    AL(kel, (size_t)numel * nq * nq);
+    AL(band, band_elems);
+    AL(band0, band_elems);
+    h->d_Kel = kel;
+    h->d_band = band;
+    h->d_band0 = band0;
+  }
+  ce = cudaMallocHost(&h->h_out, 16 * sizeof(double));
+  if (ce != cudaSuccess) {
+    set_global_error("cudaMallocHost failed");
+    mafem_destroy(hp.release());
+    return MAFEM_ERR_OOM;
+  }
+  DevPatch& P = h->P;
+  P.numel = numel; P.numnp = numnp; P.num1el = (int)d->num1el; P.num2el = (int)d->num2el;
+  P.num1np = (int)d->num1np; P.num2np = (int)d->num2np; P.nmdf = n;
+  P.kl = (int)kl; P.ku = (int)kl;
+  P.ix = d_ix; P.lm = d_lm; P.uel = d_uel; P.tab = d_tab; P.db = d_db; P.bref = d_bref; P.btab = d_btab;
+  P.unk_node = d_un; P.unk_dof = d_ud; P.node_unk = d_nu;
+  P.xms = d_xms; P.cps = d_cps;
+  cudaError_t e1, e2;
+  if (precision == MAFEM_PLAIN_FP64) {
+    e1 = band_lu_setup<double>(h->L, h->apply_threads);
+    e2 = band_solve_setup<double, double>(h->L);
+  } else {
+    e1 = band_lu_setup<float>(h->L, h->apply_threads);
+    e2 = band_solve_setup<float, double>(h->L);
+  }
+  if (e1 != cudaSuccess || e2 != cudaSuccess) {
+    set_global_error(std::string("kernel attribute setup: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    mafem_destroy(hp.release());
+    return MAFEM_ERR_CUDA;
+  }
+  *out = hp.release();
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_destroy(mafem_handle* h) {
+  if (!h) return MAFEM_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->h_out) cudaFreeHost(h->h_out);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return MAFEM_OK;
+}
+
+extern "C" const char* mafem_last_error(const mafem_handle* h) {
+  if (h) return h->err.c_str();
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  return g_err.c_str();
+}
+
+extern "C" int64_t mafem_device_bytes(const mafem_handle* h) { return h ? h->bytes : -1; }
+
+extern "C" int mafem_upload_state(mafem_handle* h, const double* xms, const double* cps) {
+  if (!h || !xms || !cps) return MAFEM_ERR_ARG;
+  CK(cudaMemcpyAsync(h->P.xms, xms, sizeof(double) * 3 * h->numnp, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(h->P.cps, cps, sizeof(double) * h->ndf * h->numnp, cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_download_state(mafem_handle* h, double* xms, double* cps) {
+  if (!h) return MAFEM_ERR_ARG;
+  if (xms) CK(cudaMemcpyAsync(xms, h->P.xms, sizeof(double) * 3 * h->numnp, cudaMemcpyDeviceToHost, h->st));
+  if (cps) CK(cudaMemcpyAsync(cps, h->P.cps, sizeof(double) * h->ndf * h->numnp, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return MAFEM_OK;
+}
+
+// element kernel + gathers: r -> d_r, K -> d_band
+static int assemble(mafem_handle* h, double time, double dt) {
+  cudaError_t e;
+  if (h->precision == MAFEM_PLAIN_FP64) {
+    e = launch_elem<double>(h->P, h->pp, time, dt, h->d_rel, (double*)h->d_Kel, h->st);
+    if (e != cudaSuccess) {
+      h->err = std::string("element kernel: ") + cudaGetErrorString(e);
+      return MAFEM_ERR_CUDA;
+    }
+    launch_band_gather<double>(h->P, h->ndf, h->nq, h->L, (const double*)h->d_Kel, (double*)h->d_band, h->st);
+  } else {
+    e = launch_elem<float>(h->P, h->pp, time, dt, h->d_rel, (float*)h->d_Kel, h->st);
+    if (e != cudaSuccess) {
+      h->err = std::string("element kernel: ") + cudaGetErrorString(e);
+      return MAFEM_ERR_CUDA;
+    }
+    launch_band_gather<float>(h->P, h->ndf, h->nq, h->L, (const float*)h->d_Kel, (float*)h->d_band, h->st);
+  }
+  launch_resid_gather(h->P, h->ndf, h->nq, h->d_rel, h->d_r, h->st);
+  CK(cudaGetLastError());
+  h->factored = false;
+  return MAFEM_OK;
+}
+
+// Solve K x = rhs (rhs in d_x on entry for the plain form; x in d_x on exit).
+// Factors the band if needed.  Returns the number of refinement sweeps in *sweeps.
+static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps) {
+  const int64_t n = h->nmdf;
+  *sweeps = 0;
+  if (h->precision == MAFEM_PLAIN_FP64) {
+    CK(cudaMemcpyAsync(h->d_x, rhs_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    if (!h->factored) {
+      CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
+      band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, h->d_x,
+                             h->apply_threads, h->apply_blocks, h->st);
+      h->factored = true;
+    } else {
+      band_forward<double, double>((const double*)h->d_band, h->L, h->d_perm, h->rmax, h->d_x, h->st);
+    }
+    cudaEventRecord(h->ev[2], h->st);
+    band_backward<double, double>((const double*)h->d_band, h->L, h->d_x, h->st);
+    CK(cudaGetLastError());
+    return MAFEM_OK;
+  }
+  // FP32 factor of the FP32 tangent, FP64 iterative refinement
+  if (!h->factored) {
+    CK(cudaMemcpyAsync(h->d_band0, h->d_band, (size_t)h->L.ldb * n * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
+    band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
+                          h->apply_threads, h->apply_blocks, h->st);
+    h->factored = true;
+  }
+  cudaEventRecord(h->ev[2], h->st);
+  CK(cudaMemsetAsync(h->d_x, 0, n * sizeof(double), h->st));
+  CK(cudaMemcpyAsync(h->d_res, rhs_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  // ‖rhs‖
+  launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part, h->d_out + 4,
+                              h->st);
+  CK(cudaMemcpyAsync(h->h_out + 4, h->d_out + 4, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const double r0 = h->h_out[4];
+  if (!(r0 > 0.0)) return MAFEM_OK;
+  double prev = r0;
+  for (int k = 0; k < h->max_refine; ++k) {
+    CK(cudaMemcpyAsync(h->d_dx, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
+    band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
+    launch_axpy(n, h->d_dx, h->d_x, h->st);
+    launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part,
+                                h->d_out + 3, h->st);
+    CK(cudaMemcpyAsync(h->h_out + 3, h->d_out + 3, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    *sweeps = k + 1;
+    const double rn = h->h_out[3];
+    if (!std::isfinite(rn)) {
+      h->err = "non-finite refinement residual";
+      return MAFEM_NAN_DETECTED;
+    }
+    if (rn <= h->refine_tol * r0) return MAFEM_OK;
+    if (rn > 0.5 * prev && k >= 3) {
+      h->err = "iterative refinement stalled at relative residual " + std::to_string(rn / r0);
+      return MAFEM_REFINE_STALLED;
+    }
+    prev = rn;
+  }
+  h->err = "iterative refinement did not reach its tolerance";
+  return MAFEM_REFINE_STALLED;
+}
+
+extern "C" int mafem_calc_r_K(mafem_handle* h, double time, double dt, double* r_out, double* band_out,
+                              int64_t ldab_out) {
+  if (!h) return MAFEM_ERR_ARG;
+  const BandLayout& L = h->L;
+  if (band_out && ldab_out < 2LL * L.kl + L.ku + 1) {
+    h->err = "ldab_out must be >= 2*kl + ku + 1";
+    return MAFEM_ERR_ARG;
+  }
+  int rc = assemble(h, time, dt);
+  if (rc) return rc;
+  if (r_out) CK(cudaMemcpyAsync(r_out, h->d_r, h->nmdf * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (band_out) {
+    const size_t rows = 2 * (size_t)L.kl + L.ku + 1;
+    if (h->precision == MAFEM_PLAIN_FP64) {
+      CK(cudaMemcpy2DAsync(band_out, ldab_out * sizeof(double), (const double*)h->d_band + L.nb, L.ldb * sizeof(double),
+                           rows * sizeof(double), L.n, cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+    } else {
+      std::vector<float> tmp((size_t)L.ldb * L.n);
+      CK(cudaMemcpyAsync(tmp.data(), h->d_band, tmp.size() * sizeof(float), cudaMemcpyDeviceToHost, h->st));
+      CK(cudaStreamSynchronize(h->st));
+      for (int64_t j = 0; j < L.n; ++j)
+        for (size_t r = 0; r < rows; ++r) band_out[j * ldab_out + r] = tmp[(size_t)j * L.ldb + L.nb + r];
+    }
+  }
+  CK(cudaStreamSynchronize(h->st));
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_solve(mafem_handle* h, const double* r, double* du_out) {
+  if (!h || !r || !du_out) return MAFEM_ERR_ARG;
+  const int64_t n = h->nmdf;
+  CK(cudaMemcpyAsync(h->d_res, r, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  // keep the right-hand side in d_dx for the plain path (factor_and_solve reads rhs_dev)
+  double* rhs = h->precision == MAFEM_PLAIN_FP64 ? h->d_dx : h->d_r;
+  if (h->precision != MAFEM_PLAIN_FP64) {
+    // d_r is the assembled residual; the refinement uses d_res as workspace, so
+    // stage the caller's rhs in d_r only for this call
+    CK(cudaMemcpyAsync(h->d_r, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  } else {
+    CK(cudaMemcpyAsync(h->d_dx, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  }
+  int sweeps = 0;
+  int rc = factor_and_solve(h, rhs, &sweeps);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(du_out, h->d_x, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int64_t i = 0; i < n; ++i) du_out[i] = -du_out[i];
+  int info = 0;
+  std::memcpy(&info, h->h_out + 5, sizeof(int));
+  if (info) {
+    h->err = "zero pivot in column " + std::to_string(info);
+    return MAFEM_ZERO_PIVOT;
+  }
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_predict(mafem_handle* h, double dt) {
+  if (!h) return MAFEM_ERR_ARG;
+  launch_predictor(h->P, h->pp, dt, h->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(h->st));
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_time_step(mafem_handle* h, double time, double dt, mafem_step_stats* stats) {
+  if (!h) return MAFEM_ERR_ARG;
+  mafem_step_stats S;
+  std::memset(&S, 0, sizeof S);
+  double eps = INFINITY;
+  int iter = 1;
+  cudaEventRecord(h->ev[5], h->st);
+  while (iter < 15) {  // FiniteElement.jl:29
+    cudaEventRecord(h->ev[0], h->st);
+    int rc = assemble(h, time, dt);
+    if (rc) return rc;
+    cudaEventRecord(h->ev[1], h->st);
+    int sweeps = 0;
+    rc = factor_and_solve(h, h->d_r, &sweeps);
+    if (rc) return rc;
+    cudaEventRecord(h->ev[3], h->st);
+    launch_newton_update(h->P, h->pp, dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    cudaEventRecord(h->ev[4], h->st);
+    CK(cudaStreamSynchronize(h->st));
+    float ms_a = 0, ms_f = 0, ms_s = 0;
+    cudaEventElapsedTime(&ms_a, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&ms_f, h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&ms_s, h->ev[2], h->ev[4]);
+    S.ms_assemble += ms_a;
+    S.ms_factor += ms_f;
+    S.ms_solve += ms_s;
+    S.refine_iters += sweeps;
+    int info = 0;
+    std::memcpy(&info, h->h_out + 5, sizeof(int));
+    eps = h->h_out[0];
+    S.eps[iter - 1] = eps;
+    S.res_norm[iter - 1] = h->h_out[1];
+    S.newton_iters = iter;
+    if (info) {
+      h->err = "zero pivot in column " + std::to_string(info);
+      if (stats) *stats = S;
+      return MAFEM_ZERO_PIVOT;
+    }
+    if (h->h_out[2] != 0.0 || !std::isfinite(eps)) {
+      h->err = "non-finite residual or Newton update";
+      if (stats) *stats = S;
+      return MAFEM_NAN_DETECTED;
+    }
+    iter += 1;
+    if (eps < h->p.eps_nr) break;
+  }
+  float ms_t = 0;
+  cudaEventElapsedTime(&ms_t, h->ev[5], h->ev[4]);
+  S.ms_total = ms_t;
+  if (stats) *stats = S;
+  if (!(eps < h->p.eps_nr)) {  // FiniteElement.jl:61
+    h->err = "did not reach Newton--Raphson tolerance";
+    return MAFEM_NEWTON_NOT_CONVERGED;
+  }
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_time_step_host(mafem_handle* h, double* xms, double* cps, double time, double dt,
+                                    mafem_step_stats* stats) {
+  int rc = mafem_upload_state(h, xms, cps);
+  if (rc) return rc;
+  rc = mafem_time_step(h, time, dt, stats);
+  int rc2 = mafem_download_state(h, xms, cps);
+  return rc ? rc : rc2;
+}
+
+extern "C" int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, mafem_step_stats* last) {
+  if (!h || (!dts && nsteps > 0)) return MAFEM_ERR_ARG;
+  double t = t0;
+  for (int k = 0; k < nsteps; ++k) {
+    t += dts[k];  // times = cumsum(Δts) + t0 (Analysis.jl:154)
+    launch_predictor(h->P, h->pp, dts[k], h->st);
+    CK(cudaGetLastError());
+    int rc = mafem_time_step(h, t, dts[k], last);
+    if (rc) return rc;
+  }
+  return MAFEM_OK;
+}

@@ -1,0 +1,226 @@
+// assemble.cu -- scatter of element blocks into the global residual and banded
+// tangent (FiniteElement.jl:128-136, 186-194), the Newton update
+// (FiniteElement.jl:40-48), update_xms! (FiniteElement.jl:408-423), and the
+// FP64 refinement residual of the FP32 solve.
+//
+// The reference scatters with LM into per-thread sparse matrices and sums them.
+// Here the scatter is inverted into a gather over the tensor-product
+// connectivity: element (e1, e2) owns nodes (e1..e1+2) x (e2..e2+2)
+// (Mesh.jl:582-589), so a band entry (i, j) receives contributions only from
+// the <= 2x2 elements that contain both node(i) and node(j), and each output
+// is produced by exactly one thread -- no atomics, deterministic sums.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "mafem_internal.h"
+
+namespace mafem {
+
+__host__ __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
+__host__ __device__ __forceinline__ int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
+
+// One thread per stored entry of band column j; entries outside the element
+// stencil (structural zeros, pivoting-fill rows, padding) are written as zero,
+// so the band needs no separate clearing pass.
+template <class T>
+__global__ void band_gather_kernel(DevPatch P, int ndf, int nq, BandLayout L, const T* __restrict__ K_el,
+                                   T* __restrict__ ab) {
+  for (int64_t j = blockIdx.y; j < L.n; j += gridDim.y) {
+    const int NJ = P.unk_node[j], dj = P.unk_dof[j];
+    const int s1J = NJ % P.num1np, s2J = NJ / P.num1np;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < L.ldb;
+         s += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t i = j + s - L.off;
+      T val = T(0);
+      if (i >= 0 && i < L.n && i - j >= -L.ku && i - j <= L.kl) {
+        const int NI = P.unk_node[i], di = P.unk_dof[i];
+        const int s1I = NI % P.num1np, s2I = NI / P.num1np;
+        if (abs(s1I - s1J) <= 2 && abs(s2I - s2J) <= 2) {
+          const int e1lo = max(max(s1I, s1J) - 2, 0), e1hi = min(min(s1I, s1J), P.num1el - 1);
+          const int e2lo = max(max(s2I, s2J) - 2, 0), e2hi = min(min(s2I, s2J), P.num2el - 1);
+          for (int e2 = e2lo; e2 <= e2hi; ++e2)
+            for (int e1 = e1lo; e1 <= e1hi; ++e1) {
+              const int e = e1 + P.num1el * e2;
+              const int a = (s1I - e1) + 3 * (s2I - e2), b = (s1J - e1) + 3 * (s2J - e2);
+              val += K_el[(size_t)e * nq * nq + (size_t)(b * ndf + dj) * nq + a * ndf + di];
+            }
+        }
+      }
+      ab[j * L.ldb + s] = val;
+    }
+  }
+}
+
+// r[i] = Σ_e r_el[e][(a, di)] over the elements containing node(i) (FiniteElement.jl:131)
+__global__ void resid_gather_kernel(DevPatch P, int ndf, int nq, const double* __restrict__ r_el,
+                                    double* __restrict__ r) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.nmdf; i += (int64_t)gridDim.x * blockDim.x) {
+    const int NI = P.unk_node[i], di = P.unk_dof[i];
+    const int s1 = NI % P.num1np, s2 = NI / P.num1np;
+    double acc = 0.0;
+    for (int e2 = max(s2 - 2, 0); e2 <= min(s2, P.num2el - 1); ++e2)
+      for (int e1 = max(s1 - 2, 0); e1 <= min(s1, P.num1el - 1); ++e1) {
+        const int e = e1 + P.num1el * e2;
+        const int a = (s1 - e1) + 3 * (s2 - e2);
+        acc += r_el[(size_t)e * nq + a * ndf + di];
+      }
+    r[i] = acc;
+  }
+}
+
+// update_xms! (FiniteElement.jl:408-423) used as the predictor (Analysis.jl:193):
+// xms[:, j] += dt * cps[:, m_motion_order[j]]
+__global__ void predictor_kernel(DevPatch P, PhysParams pp, double dt) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < 3LL * P.numnp;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(k / P.numnp), node = (int)(k - (int64_t)j * P.numnp);
+    const int d = pp.mmo[j];
+    if (d >= 0) P.xms[k] += dt * P.cps[(size_t)d * P.numnp + node];
+  }
+}
+
+// Newton update (FiniteElement.jl:41-46): Δu = -x, Δcps[ID_inv] = Δu, cps += Δcps,
+// xms[:, j] += dt Δcps[:, m_motion_order[j]]; per-block partial sums of Δu² and r².
+__global__ void newton_update_kernel(DevPatch P, PhysParams pp, double dt, const double* __restrict__ x,
+                                     const double* __restrict__ r, double* __restrict__ part) {
+  __shared__ double s_du[32], s_r[32];
+  double du2 = 0.0, r2 = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P.nmdf; q += (int64_t)gridDim.x * blockDim.x) {
+    const double du = -x[q];
+    const int node = P.unk_node[q], d = P.unk_dof[q];
+    P.cps[(size_t)d * P.numnp + node] += du;
+    for (int j = 0; j < 3; ++j)
+      if (pp.mmo[j] == d) P.xms[(size_t)j * P.numnp + node] += dt * du;
+    du2 += du * du;
+    r2 += r[q] * r[q];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    du2 += __shfl_down_sync(0xffffffffu, du2, o);
+    r2 += __shfl_down_sync(0xffffffffu, r2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_du[threadIdx.x >> 5] = du2;
+    s_r[threadIdx.x >> 5] = r2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      a += s_du[k];
+      b += s_r[k];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// Fixed-order final reduction: out[0] = ‖Δu‖₂ / nmdf (the Newton ε,
+// FiniteElement.jl:48), out[1] = ‖r‖₂, out[2] = 1 if either is not finite.
+__global__ void newton_norm_kernel(const double* __restrict__ part, int nblk, int64_t nmdf, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double a = 0, b = 0;
+    for (int k = 0; k < nblk; ++k) {
+      a += part[2 * k];
+      b += part[2 * k + 1];
+    }
+    out[0] = sqrt(a) / (double)nmdf;
+    out[1] = sqrt(b);
+    out[2] = (isfinite(a) && isfinite(b)) ? 0.0 : 1.0;
+  }
+}
+
+// Refinement residual res = r - A0 x in FP64 arithmetic, A0 = the unfactored
+// band (any storage type).  A warp owns 32 consecutive rows and walks the
+// columns of its band window, so every load of A0 is a coalesced 32-row
+// column segment.
+template <class T>
+__global__ void band_residual_kernel(const T* __restrict__ a0, BandLayout L, const double* __restrict__ x,
+                                     const double* __restrict__ r, double* __restrict__ res,
+                                     double* __restrict__ part) {
+  __shared__ double s_p[32];
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  double nrm = 0.0;
+  for (int64_t wi = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); wi * 32 < L.n; wi += nwarps) {
+    const int64_t i0 = wi * 32, i = i0 + lane;
+    const int64_t jlo = max64(0, i0 - L.kl), jhi = min64(L.n - 1, i0 + 31 + L.ku);
+    double acc = 0.0;
+    for (int64_t j = jlo; j <= jhi; ++j) {
+      const double xj = x[j];
+      if (i < L.n && i - j >= -L.ku && i - j <= L.kl) acc += (double)a0[j * L.ldb + L.off + i - j] * xj;
+    }
+    if (i < L.n) {
+      const double v = r[i] - acc;
+      res[i] = v;
+      nrm += v * v;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) nrm += __shfl_down_sync(0xffffffffu, nrm, o);
+  if (lane == 0) s_p[threadIdx.x >> 5] = nrm;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) a += s_p[k];
+    part[blockIdx.x] = a;
+  }
+}
+__global__ void sqrt_sum_kernel(const double* __restrict__ part, int n, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double a = 0;
+    for (int k = 0; k < n; ++k) a += part[k];
+    *out = sqrt(a);
+  }
+}
+__global__ void axpy_kernel(int64_t n, const double* __restrict__ dx, double* __restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] += dx[i];
+}
+
+// ---- launchers -------------------------------------------------------------------
+template <class T>
+void launch_band_gather(const DevPatch& P, int ndf, int nq, const BandLayout& L, const T* K_el, T* ab,
+                        cudaStream_t st) {
+  dim3 grid((unsigned)((L.ldb + 255) / 256), (unsigned)min64(L.n, 65535));
+  band_gather_kernel<T><<<grid, 256, 0, st>>>(P, ndf, nq, L, K_el, ab);
+}
+void launch_resid_gather(const DevPatch& P, int ndf, int nq, const double* r_el, double* r, cudaStream_t st) {
+  const int blocks = (int)min64(1024, (P.nmdf + 255) / 256);
+  resid_gather_kernel<<<blocks, 256, 0, st>>>(P, ndf, nq, r_el, r);
+}
+void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaStream_t st) {
+  const int blocks = (int)min64(1024, (3LL * P.numnp + 255) / 256);
+  predictor_kernel<<<blocks, 256, 0, st>>>(P, pp, dt);
+}
+int newton_update_blocks(int64_t nmdf) { return (int)min64(256, (nmdf + 255) / 256); }
+void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
+                          double* part, double* out, cudaStream_t st) {
+  const int blocks = newton_update_blocks(P.nmdf);
+  newton_update_kernel<<<blocks, 256, 0, st>>>(P, pp, dt, x, r, part);
+  newton_norm_kernel<<<1, 32, 0, st>>>(part, blocks, P.nmdf, out);
+}
+int band_residual_blocks(int64_t n) { return (int)min64(304, (n + 255) / 256); }
+template <class T>
+void launch_band_residual(const T* a0, const BandLayout& L, const double* x, const double* r, double* res,
+                          double* part, double* out, cudaStream_t st) {
+  const int blocks = band_residual_blocks(L.n);
+  band_residual_kernel<T><<<blocks, 256, 0, st>>>(a0, L, x, r, res, part);
+  sqrt_sum_kernel<<<1, 32, 0, st>>>(part, blocks, out);
+}
+void launch_axpy(int64_t n, const double* dx, double* x, cudaStream_t st) {
+  const int blocks = (int)min64(1024, (n + 255) / 256);
+  axpy_kernel<<<blocks, 256, 0, st>>>(n, dx, x);
+}
+
+template void launch_band_gather<double>(const DevPatch&, int, int, const BandLayout&, const double*, double*,
+                                         cudaStream_t);
+template void launch_band_gather<float>(const DevPatch&, int, int, const BandLayout&, const float*, float*,
+                                        cudaStream_t);
+template void launch_band_residual<double>(const double*, const BandLayout&, const double*, const double*, double*,
+                                           double*, double*, cudaStream_t);
+template void launch_band_residual<float>(const float*, const BandLayout&, const double*, const double*, double*,
+                                          double*, double*, cudaStream_t);
+
+}  // namespace mafem

@@ -1,0 +1,129 @@
+// mafem_internal.h -- internal types shared by the library's translation units.
+#pragma once
+
+#include <array>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "mafem.h"
+
+namespace mafem {
+
+// Host copy of the reference's Mesh fields, in the C ABI's layout
+// (mafem_mesh_desc): 1-based, column-major, int64.
+struct HostMesh {
+  int num1el = 0, num2el = 0, numel = 0, num1np = 0, num2np = 0, numnp = 0, ndf = 0;
+  int64_t nmdf = 0;
+  int64_t dofs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  std::vector<double> kv1, kv2;
+  std::vector<int64_t> IX, ID;
+  int64_t n_uel = 0;
+  std::vector<int64_t> uel_ids;
+  std::vector<double> ufns;
+  int64_t bdry_n_uel[4] = {0, 0, 0, 0};
+  std::vector<int64_t> bdry_uel_ids[4];
+  std::vector<double> bdry_ufns[4];
+  std::vector<int64_t> neu_bdry, neu_type;
+  std::vector<double> neu_val;
+  std::vector<int64_t> dir_unknown, dir_node;
+  std::vector<double> dir_val;
+};
+
+int build_mesh(const mafem_params& p, const mafem_args& a, HostMesh& m, std::string& err);
+void mesh_desc(const HostMesh& m, mafem_mesh_desc& d);
+int prepare_input(const HostMesh& m, const mafem_params& p, double* xms, double* cps, std::string& err);
+void set_global_error(const std::string& s);
+
+// ---------------------------------------------------------------------------
+// Device-side description of one patch.  All pointers are device pointers.
+// Control-point state is stored exactly like the host arrays: xms as 3
+// columns of numnp doubles, cps as ndf columns of numnp doubles (SoA).
+constexpr int kMaxNeu = 8;
+constexpr int kTab = 56;  // doubles per GP record: w, N[9], dN[18], ddN[27], pad
+
+struct PhysParams {
+  int motion, scenario, ndf, nq;      // nq = 9*ndf element dofs (tangent directions)
+  double kb, kg, zv, pn, adb, am;
+  int dof_of[8];                      // 0-based dof of Unknown u (vx..pm), -1 if absent
+  int unk_of[8];                      // Unknown (0..7) of dof d (0-based), for d < ndf
+  int mmo[3];                         // 0-based dof of m_motion_order[j], -1 if none
+  int n_neu;
+  int neu_bdry[kMaxNeu];              // 0..3 = BOTTOM, RIGHT, TOP, LEFT
+  int neu_type[kMaxNeu];              // SHEAR/STRETCH/MOMENT
+  double neu_val[kMaxNeu];
+  double bend_tm;
+};
+
+struct DevPatch {
+  int numel, numnp, num1el, num2el, num1np, num2np;
+  int64_t nmdf;
+  int kl, ku;                         // half bandwidths of K
+  // mesh tables
+  const int* ix;                      // [numel][9] 0-based node numbers
+  const int* lm;                      // [numel][nq] 0-based unknown, -1 = Dirichlet
+  const int* uel;                     // [numel] unique area element (0-based)
+  const double* tab;                  // [n_uel][9][kTab]
+  const double* db;                   // [n_uel][81] Dohrmann-Bochev Gᵀ H⁻¹ G
+  const int* bref;                    // [numel][4] boundary GP table row per boundary, -1 if not on it
+  const double* btab;                 // [rows][3][kTab] boundary GP tables
+  const int* unk_node;                // [nmdf] node of unknown q (0-based)
+  const int* unk_dof;                 // [nmdf] dof of unknown q (0-based)
+  const int* node_unk;                // [numnp][ndf] unknown of (node, dof), -1 if Dirichlet
+  // state
+  double* xms;                        // [3][numnp]
+  double* cps;                        // [ndf][numnp]
+};
+
+// Band storage of an n x n matrix with lower/upper half bandwidths kl, ku and
+// panel width nb: column-major, ldb rows per column; A(i, j) lives at
+// ab[(size_t)j * ldb + off + i - j] with off = kl + ku + nb.  Rows
+// [0, nb) hold U entries beyond the pivoting fill (kept zero), rows
+// [off + kl + 1, off + kl + nb] hold panel-local L fill (lower-left triangle).
+struct BandLayout {
+  int64_t n;
+  int kl, ku, nb;
+  int64_t ldb, off;
+};
+BandLayout make_band_layout(int64_t n, int kl, int ku, int nb);
+
+}  // namespace mafem
+
+// ---- kernel launchers (elem.cu, assemble.cu, band_lu.cu) ----------------------
+#include <cuda_runtime.h>
+namespace mafem {
+template <class T>
+size_t elem_smem_bytes(int nq, int epb);
+template <class T>
+cudaError_t launch_elem(const DevPatch& P, const PhysParams& pp, double time, double dt, double* r_el, T* K_el,
+                        cudaStream_t st);
+template <class T>
+void launch_band_gather(const DevPatch& P, int ndf, int nq, const BandLayout& L, const T* K_el, T* ab,
+                        cudaStream_t st);
+void launch_resid_gather(const DevPatch& P, int ndf, int nq, const double* r_el, double* r, cudaStream_t st);
+void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaStream_t st);
+int newton_update_blocks(int64_t nmdf);
+void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
+                          double* part, double* out, cudaStream_t st);
+int band_residual_blocks(int64_t n);
+template <class T>
+void launch_band_residual(const T* a0, const BandLayout& L, const double* x, const double* r, double* res,
+                          double* part, double* out, cudaStream_t st);
+void launch_axpy(int64_t n, const double* dx, double* x, cudaStream_t st);
+
+template <class T>
+size_t panel_smem_bytes(const BandLayout& L);
+template <class T>
+size_t apply_smem_bytes(const BandLayout& L, int threads);
+template <class T>
+cudaError_t band_lu_setup(const BandLayout& L, int apply_threads);
+template <class T>
+void band_lu_factor(T* ab, const BandLayout& L, int* ipiv, int* perm_all, int rmax, int* info, T* rhs,
+                    int apply_threads, int apply_blocks, cudaStream_t st);
+template <class T, class V>
+cudaError_t band_solve_setup(const BandLayout& L);
+template <class T, class V>
+void band_forward(const T* ab, const BandLayout& L, const int* perm_all, int rmax, V* b, cudaStream_t st);
+template <class T, class V>
+void band_backward(const T* ab, const BandLayout& L, V* y, cudaStream_t st);
+}  // namespace mafem

@@ -1,0 +1,412 @@
+"""Python host API over libmafem.so, mirroring MembraneAleFem.jl's entry points.
+
+The names, argument meanings and error behaviour follow the reference:
+
+=======================================  ==========================================
+reference (Julia)                        here
+=======================================  ==========================================
+``Params(...)`` (Params.jl:36-55)        :class:`Params`
+``Mesh(p; args...)`` (Mesh.jl:79)        :class:`Mesh`
+``prepare_input(p; args...)``            :func:`prepare_input`
+``calc_r_K(mesh, xms, cps, t, Δt, p)``   :meth:`Solver.calc_r_K`
+``-K \\ r``                               :meth:`Solver.solve`
+``update_xms!(...)`` (predictor)         :meth:`Solver.predict`
+``time_step!(mesh, xms, cps, t, Δt, p)`` :meth:`Solver.time_step` (raises
+                                         ``AssertionError`` like the reference's
+                                         @assert when Newton does not converge)
+``run_analysis!`` / ``solve``            :meth:`Solver.run_analysis`, :func:`solve`
+=======================================  ==========================================
+
+Every array uses the reference's layout: ``xms`` is numnp x 3 and ``cps`` numnp
+x ndf (Fortran order, float64), integer maps are 1-based.  All compute runs in
+CUDA kernels on the GPU; there is no CPU fallback -- without the library or a
+GPU every call that computes raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmafem.so")
+
+# enums (src/input/Enums.jl, src/input/Dof.jl) -- same numeric values
+F_CAVI, F_COUE, F_POIS, F_PULL, F_BEND = 1, 2, 3, 4, 5
+STATIC, EUL, LAG, ALEV, ALEVB = 1, 2, 3, 4, 5
+BOTTOM, RIGHT, TOP, LEFT = 1, 2, 3, 4
+SHEAR, STRETCH, MOMENT = 1, 2, 3
+PLAIN_FP64, FP32_REFINE = 0, 1
+
+OK = 0
+NEWTON_NOT_CONVERGED, ZERO_PIVOT, NAN_DETECTED, REFINE_STALLED = 1, 2, 3, 4
+ERR_ARG, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED, ERR_ADMISSION = -1, -2, -3, -4, -5
+
+
+class MafemError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class NewtonNotConverged(AssertionError):
+    """The reference's ``@assert εs[end] < p.εnr`` (FiniteElement.jl:61)."""
+
+
+class _CParams(C.Structure):
+    _fields_ = [("motion", C.c_int32), ("scenario", C.c_int32), ("num1el", C.c_int32),
+                ("num2el", C.c_int32), ("length", C.c_double), ("kb", C.c_double),
+                ("kg", C.c_double), ("zeta_v", C.c_double), ("pn", C.c_double),
+                ("poly", C.c_int32), ("gp1d", C.c_int32), ("nders", C.c_int32),
+                ("nen", C.c_int32), ("alpha_db", C.c_double), ("alpha_m", C.c_double),
+                ("eps_k", C.c_double), ("eps_nr", C.c_double)]
+
+
+class _CArgs(C.Structure):
+    _fields_ = [("pull_speed", C.c_double), ("bend_tm", C.c_double), ("bend_mf", C.c_double)]
+
+
+_P64 = C.POINTER(C.c_int64)
+_PD = C.POINTER(C.c_double)
+
+
+class MeshDesc(C.Structure):
+    """mafem_mesh_desc (include/mafem.h)."""
+    _fields_ = [("num1el", C.c_int64), ("num2el", C.c_int64), ("numel", C.c_int64),
+                ("num1np", C.c_int64), ("num2np", C.c_int64), ("numnp", C.c_int64),
+                ("ndf", C.c_int64), ("nmdf", C.c_int64), ("dofs", C.c_int64 * 8),
+                ("IX", _P64), ("ID", _P64), ("n_uel", C.c_int64), ("uel_ids", _P64),
+                ("ufns", _PD), ("bdry_n_uel", C.c_int64 * 4), ("bdry_uel_ids", _P64 * 4),
+                ("bdry_ufns", _PD * 4), ("n_neu", C.c_int64), ("neu_bdry", _P64),
+                ("neu_type", _P64), ("neu_val", _PD), ("n_dir", C.c_int64),
+                ("dir_unknown", _P64), ("dir_node", _P64), ("dir_val", _PD)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int32), ("refine_iters", C.c_int32),
+                ("eps", C.c_double * 14), ("res_norm", C.c_double * 14),
+                ("ms_assemble", C.c_double), ("ms_factor", C.c_double),
+                ("ms_solve", C.c_double), ("ms_total", C.c_double)]
+
+    def as_dict(self):
+        n = self.newton_iters
+        return {"newton_iters": n, "refine_iters": self.refine_iters,
+                "eps": list(self.eps[:n]), "res_norm": list(self.res_norm[:n]),
+                "ms_assemble": self.ms_assemble, "ms_factor": self.ms_factor,
+                "ms_solve": self.ms_solve, "ms_total": self.ms_total}
+
+
+_lib = None
+
+
+def lib():
+    """Load libmafem.so (built by build.py); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run membranealefem.jl_gb300/build.py "
+                              "(the CUDA library is required; there is no CPU fallback)")
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.mafem_last_error.restype = C.c_char_p
+        L.mafem_last_error.argtypes = [vp]
+        L.mafem_mesh_build.argtypes = [C.POINTER(_CParams), C.POINTER(_CArgs), C.POINTER(vp)]
+        L.mafem_mesh_view.argtypes = [vp, C.POINTER(MeshDesc)]
+        L.mafem_mesh_free.argtypes = [vp]
+        L.mafem_mesh_free.restype = None
+        L.mafem_prepare_input.argtypes = [vp, C.POINTER(_CParams), _PD, _PD]
+        L.mafem_mesh_half_bandwidth.argtypes = [C.POINTER(MeshDesc)]
+        L.mafem_mesh_half_bandwidth.restype = C.c_int64
+        L.mafem_create.argtypes = [C.POINTER(MeshDesc), C.POINTER(_CParams), C.POINTER(_CArgs),
+                                   C.c_int32, C.POINTER(vp)]
+        L.mafem_destroy.argtypes = [vp]
+        L.mafem_device_bytes.argtypes = [vp]
+        L.mafem_device_bytes.restype = C.c_int64
+        L.mafem_footprint_bytes.argtypes = [C.POINTER(MeshDesc), C.c_int32]
+        L.mafem_footprint_bytes.restype = C.c_int64
+        L.mafem_upload_state.argtypes = [vp, _PD, _PD]
+        L.mafem_download_state.argtypes = [vp, _PD, _PD]
+        L.mafem_calc_r_K.argtypes = [vp, C.c_double, C.c_double, _PD, _PD, C.c_int64]
+        L.mafem_solve.argtypes = [vp, _PD, _PD]
+        L.mafem_predict.argtypes = [vp, C.c_double]
+        L.mafem_time_step.argtypes = [vp, C.c_double, C.c_double, C.POINTER(StepStats)]
+        L.mafem_time_step_host.argtypes = [vp, _PD, _PD, C.c_double, C.c_double,
+                                           C.POINTER(StepStats)]
+        L.mafem_run.argtypes = [vp, _PD, C.c_int32, C.c_double, C.POINTER(StepStats)]
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_PD)
+
+
+def _raise(rc: int, h=None):
+    if rc == OK:
+        return
+    msg = lib().mafem_last_error(h).decode()
+    if rc == NEWTON_NOT_CONVERGED:
+        raise NewtonNotConverged(msg)
+    raise MafemError(rc, msg)
+
+
+@dataclass
+class Params:
+    """``Params`` (src/input/Params.jl:36-55) plus the keyword arguments the hot
+    path reads (``pull_speed``, ``bend_tm``, ``bend_mf``)."""
+
+    motion: int = ALEVB
+    scenario: int = F_PULL
+    num1el: int = 17
+    num2el: int = 17
+    output: bool = False
+    length: float = 64.0
+    kb: float = 1.0
+    kg: float = -0.5
+    zeta_v: float = 1.0
+    pn: float = 0.0
+    poly: int = 2
+    gp1d: int = 3
+    nders: int = 2
+    nen: int = 9
+    alpha_db: float | None = None  # default length^2 (Params.jl:51)
+    alpha_m: float = 1.0
+    eps_k: float = 1e-15
+    eps_nr: float = 1e-12
+    pull_speed: float = 0.0
+    bend_tm: float = 1.0
+    bend_mf: float = 0.0
+
+    def c_params(self) -> _CParams:
+        adb = self.length ** 2 if self.alpha_db is None else self.alpha_db
+        return _CParams(self.motion, self.scenario, self.num1el, self.num2el, self.length,
+                        self.kb, self.kg, self.zeta_v, self.pn, self.poly, self.gp1d, self.nders,
+                        self.nen, adb, self.alpha_m, self.eps_k, self.eps_nr)
+
+    def c_args(self) -> _CArgs:
+        return _CArgs(self.pull_speed, self.bend_tm, self.bend_mf)
+
+
+class Mesh:
+    """``Mesh(p; args...)`` built by the library (src/input/Mesh.jl:94-302)."""
+
+    def __init__(self, p: Params):
+        self.p = p
+        self._cp, self._ca = p.c_params(), p.c_args()
+        h = C.c_void_p()
+        _raise(lib().mafem_mesh_build(C.byref(self._cp), C.byref(self._ca), C.byref(h)))
+        self.h = h
+        self.desc = MeshDesc()
+        _raise(lib().mafem_mesh_view(self.h, C.byref(self.desc)))
+        d = self.desc
+        (self.num1el, self.num2el, self.numel, self.num1np, self.num2np, self.numnp, self.ndf,
+         self.nmdf) = (d.num1el, d.num2el, d.numel, d.num1np, d.num2np, d.numnp, d.ndf, d.nmdf)
+        self.dofs = [int(v) for v in d.dofs]
+        self.half_bw = int(lib().mafem_mesh_half_bandwidth(C.byref(d)))
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                lib().mafem_mesh_free(self.h)
+        except Exception:
+            pass
+
+    def _arr(self, ptr, n, dtype):
+        return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True)
+
+    @property
+    def IX(self):
+        return self._arr(self.desc.IX, 9 * self.numel, np.int64).reshape(self.numel, 9).T
+
+    @property
+    def ID(self):
+        return self._arr(self.desc.ID, self.ndf * self.numnp, np.int64).reshape(self.numnp, self.ndf).T
+
+    @property
+    def LM(self):
+        """``reshape(ID[:, IX], ndf*NEN, numel)`` (Mesh.jl:299)."""
+        ID, IX = self.ID, self.IX
+        return ID[:, IX.T.reshape(-1) - 1].T.reshape(self.numel, 9 * self.ndf).T
+
+    @property
+    def ID_inv(self):
+        """(node, dof) of each unknown, 1-based (Mesh.jl:291-296)."""
+        ID = self.ID
+        nodes, dofs = np.nonzero(ID.T)
+        order = np.argsort(ID.T[nodes, dofs])
+        return np.stack([nodes[order] + 1, dofs[order] + 1], axis=1)
+
+    def area_tables(self):
+        uel = self._arr(self.desc.uel_ids, self.numel, np.int64)
+        uf = self._arr(self.desc.ufns, self.desc.n_uel * 9 * 55, np.float64)
+        return uel, uf.reshape(self.desc.n_uel, 9, 55)
+
+    def bdry_tables(self, b: int):
+        k = b - 1
+        nel = self.num1el if b in (BOTTOM, TOP) else self.num2el
+        uel = self._arr(self.desc.bdry_uel_ids[k], nel, np.int64)
+        nu = self.desc.bdry_n_uel[k]
+        uf = self._arr(self.desc.bdry_ufns[k], nu * 3 * 55, np.float64)
+        return uel, uf.reshape(nu, 3, 55)
+
+    def neumann(self):
+        d = self.desc
+        return [(int(d.neu_bdry[k]), int(d.neu_type[k]), float(d.neu_val[k])) for k in range(d.n_neu)]
+
+    def dirichlet(self):
+        d = self.desc
+        return [(int(d.dir_unknown[k]), int(d.dir_node[k]), float(d.dir_val[k])) for k in range(d.n_dir)]
+
+
+def prepare_input(p: Params, mesh: Mesh | None = None):
+    """``prepare_input(p; args...)`` (src/Input.jl:22-121): mesh, xms, cps."""
+    mesh = mesh or Mesh(p)
+    xms = np.zeros((mesh.numnp, 3), order="F")
+    cps = np.zeros((mesh.numnp, mesh.ndf), order="F")
+    _raise(lib().mafem_prepare_input(mesh.h, C.byref(mesh._cp), _dp(xms), _dp(cps)))
+    return mesh, xms, cps
+
+
+def footprint_bytes(mesh: Mesh, precision: int = PLAIN_FP64) -> int:
+    return int(lib().mafem_footprint_bytes(C.byref(mesh.desc), precision))
+
+
+class Solver:
+    """Device-resident state of one patch: the replacement of ``calc_r_K`` + ``\\``
+    and of ``time_step!`` (src/analysis/FiniteElement.jl:11-200)."""
+
+    def __init__(self, mesh: Mesh, p: Params | None = None, precision: int = PLAIN_FP64,
+                 desc: MeshDesc | None = None):
+        self.mesh = mesh
+        self.p = p or mesh.p
+        self.precision = precision
+        self._cp, self._ca = self.p.c_params(), self.p.c_args()
+        self.desc = desc or mesh.desc
+        h = C.c_void_p()
+        _raise(lib().mafem_create(C.byref(self.desc), C.byref(self._cp), C.byref(self._ca),
+                                  precision, C.byref(h)))
+        self.h = h
+        self.nmdf = self.desc.nmdf
+        self.kl = mesh.half_bw if mesh is not None else int(
+            lib().mafem_mesh_half_bandwidth(C.byref(self.desc)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mafem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().mafem_device_bytes(self.h))
+
+    def upload(self, xms, cps):
+        xms = np.asfortranarray(xms, dtype=np.float64)
+        cps = np.asfortranarray(cps, dtype=np.float64)
+        _raise(lib().mafem_upload_state(self.h, _dp(xms), _dp(cps)), self.h)
+
+    def download(self):
+        xms = np.zeros((self.desc.numnp, 3), order="F")
+        cps = np.zeros((self.desc.numnp, self.desc.ndf), order="F")
+        _raise(lib().mafem_download_state(self.h, _dp(xms), _dp(cps)), self.h)
+        return xms, cps
+
+    def calc_r_K(self, xms, cps, time: float, dt: float, tangent: bool = True):
+        """r (nmdf) and K in LAPACK band layout ((nmdf, 3kl+1): row j holds column j,
+        A(i, j) at [j, 2kl + i - j]); state is uploaded first."""
+        self.upload(xms, cps)
+        r = np.zeros(self.nmdf)
+        kl = self.kl
+        ldab = 3 * kl + 1
+        ab = np.zeros((self.nmdf, ldab)) if tangent else None
+        _raise(lib().mafem_calc_r_K(self.h, time, dt, _dp(r), _dp(ab) if tangent else None, ldab),
+               self.h)
+        return r, ab
+
+    def solve(self, r):
+        """Δu = -K \\ r for the K of the last calc_r_K (FiniteElement.jl:38)."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        du = np.zeros(self.nmdf)
+        _raise(lib().mafem_solve(self.h, _dp(r), _dp(du)), self.h)
+        return du
+
+    def predict(self, dt: float):
+        _raise(lib().mafem_predict(self.h, dt), self.h)
+
+    def time_step(self, xms, cps, time: float, dt: float):
+        """``time_step!`` with host arrays, updated in place (Fortran-ordered)."""
+        assert xms.flags.f_contiguous and cps.flags.f_contiguous
+        assert xms.dtype == np.float64 and cps.dtype == np.float64
+        st = StepStats()
+        rc = lib().mafem_time_step_host(self.h, _dp(xms), _dp(cps), time, dt, C.byref(st))
+        self.last_stats = st.as_dict()
+        _raise(rc, self.h)
+        return self.last_stats
+
+    def time_step_resident(self, time: float, dt: float):
+        st = StepStats()
+        rc = lib().mafem_time_step(self.h, time, dt, C.byref(st))
+        self.last_stats = st.as_dict()
+        _raise(rc, self.h)
+        return self.last_stats
+
+    def run_analysis(self, dts, t0: float = 0.0):
+        """``run_analysis!``'s time loop on the resident state (Analysis.jl:183-216)."""
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        st = StepStats()
+        rc = lib().mafem_run(self.h, _dp(dts), len(dts), t0, C.byref(st))
+        self.last_stats = st.as_dict()
+        _raise(rc, self.h)
+        return self.last_stats
+
+
+def solve(p: Params, dts, t0: float = 0.0, precision: int = PLAIN_FP64, xms=None, cps=None):
+    """``solve(p; args...)`` (src/MembraneAleFem.jl:44-60) without file output:
+    returns (mesh, xms, cps) after the time steps ``dts``."""
+    mesh, x0, c0 = prepare_input(p)
+    xms = x0 if xms is None else np.asfortranarray(xms, dtype=np.float64)
+    cps = c0 if cps is None else np.asfortranarray(cps, dtype=np.float64)
+    with Solver(mesh, p, precision) as s:
+        s.upload(xms, cps)
+        s.run_analysis(dts, t0)
+        xms, cps = s.download()
+    return mesh, xms, cps
+
+
+def splitmix64(seed: int, n: int) -> np.ndarray:
+    """n uniform doubles in [0, 1) from SplitMix64 (portable, seedable)."""
+    out = np.empty(n, dtype=np.float64)
+    with np.errstate(over="ignore"):
+        s = np.uint64(seed)
+        for i in range(n):
+            s = s + np.uint64(0x9E3779B97F4A7C15)
+            z = s
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            z = z ^ (z >> np.uint64(31))
+            out[i] = float(z >> np.uint64(11)) * (1.0 / 9007199254740992.0)
+    return out
+
+
+def perturb_interior_z(mesh: Mesh, xms: np.ndarray, seed: int = 0, amp: float = 1e-4) -> np.ndarray:
+    """Seeded out-of-plane perturbation z ~ U[-amp, amp] of the nodes not on the
+    outer boundary (the synthetic initial state of the benchmark workloads)."""
+    u = splitmix64(seed, mesh.numnp)
+    s1 = np.arange(mesh.numnp) % mesh.num1np
+    s2 = np.arange(mesh.numnp) // mesh.num1np
+    interior = (s1 > 0) & (s1 < mesh.num1np - 1) & (s2 > 0) & (s2 < mesh.num2np - 1)
+    xms[:, 2] += np.where(interior, amp * (2.0 * u - 1.0), 0.0)
+    return xms

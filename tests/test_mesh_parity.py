@@ -1,0 +1,65 @@
+"""Host-side parity (CPU): the library's Mesh / prepare_input against the oracle.
+
+The integer maps (IX, ID, LM, ID_inv: Mesh.jl:276-299, 574-593), the Dirichlet
+and Neumann lists (Bc.jl) and the GP tables (GpBasisFn.jl) must be bit-exact.
+"""
+import numpy as np
+import pytest
+
+from _cases import M, O, params_pair
+
+CASES = [(M.LAG, M.F_PULL, 8, 8), (M.ALEVB, M.F_PULL, 32, 32), (M.ALEVB, M.F_PULL, 19, 21),
+         (M.ALEVB, M.F_PULL, 64, 64), (M.EUL, M.F_PULL, 5, 6), (M.ALEV, M.F_PULL, 4, 7),
+         (M.LAG, M.F_PULL, 1, 1), (M.STATIC, M.F_CAVI, 2, 3), (M.STATIC, M.F_COUE, 3, 4),
+         (M.STATIC, M.F_POIS, 5, 4), (M.LAG, M.F_BEND, 3, 3), (M.ALEV, M.F_BEND, 2, 5)]
+
+
+@pytest.mark.parametrize("motion,scenario,n1,n2", CASES)
+def test_mesh_bit_exact(motion, scenario, n1, n2):
+    p, q = params_pair(motion, scenario, n1, n2, bend_mf=0.5)
+    m, o = M.Mesh(p), O.Mesh(q)
+    assert (m.numel, m.numnp, m.ndf, m.nmdf) == (o.numel, o.numnp, o.ndf, o.nmdf)
+    assert m.dofs == o.dofs
+    assert np.array_equal(m.IX, o.IX)
+    assert np.array_equal(m.ID, o.ID)
+    assert np.array_equal(m.LM, o.LM)
+    assert np.array_equal(m.ID_inv, o.ID_inv)
+    assert m.half_bw == o.half_bw
+    u1, t1 = m.area_tables()
+    u2, t2 = o.area_tables()
+    assert np.array_equal(u1, u2) and np.array_equal(t1, t2)
+    for b in (M.BOTTOM, M.RIGHT, M.TOP, M.LEFT):
+        a1, b1 = m.bdry_tables(b)
+        a2, b2 = o.bdry_tables(b)
+        assert np.array_equal(a1, a2) and np.array_equal(b1, b2)
+    assert m.neumann() == o.neumann()
+    assert m.dirichlet() == o.dirichlet()
+
+
+@pytest.mark.parametrize("motion,scenario,n1,n2", [c for c in CASES if c[1] != M.F_BEND and c[2] * c[3] <= 1024])
+def test_prepare_input(motion, scenario, n1, n2):
+    p, q = params_pair(motion, scenario, n1, n2)
+    m, o = M.Mesh(p), O.Mesh(q)
+    _, x1, c1 = M.prepare_input(p, m)
+    x2, c2 = o.prepare_input()
+    # the library solves the separable collocation system per direction, the
+    # reference (and oracle) the dense tensor-product system: same values to rounding
+    assert np.abs(x1 - x2).max() <= 1e-14 * p.length
+    assert np.array_equal(c1, c2)
+
+
+def test_band_sizes_of_the_configs():
+    """Half bandwidths and unknown counts of the benchmark meshes."""
+    expect = {(M.LAG, 8): (309, 80), (M.ALEVB, 32): (8430, 543), (M.ALEVB, 64): (33262, 1055)}
+    for (mot, n), (nmdf, b) in expect.items():
+        m = M.Mesh(M.Params(motion=mot, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0))
+        assert (m.nmdf, m.half_bw) == (nmdf, b)
+
+
+def test_errors_like_the_reference():
+    with pytest.raises(M.MafemError):  # Params.jl:93-95
+        M.Mesh(M.Params(poly=3))
+    with pytest.raises(M.MafemError):  # Bc.jl:266
+        M.Mesh(M.Params(scenario=M.F_PULL, pn=1.0))
+    with pytest.raises(M.MafemError):  # Params.jl:108-115
+        M.Mesh(M.Params(scenario=M.F_CAVI, motion=M.LAG))
