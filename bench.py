@@ -1,0 +1,378 @@
+"""Benchmark: membrane time-steps/s of the GB300 assemble-and-solve path.
+
+Workload (one "step" = one time step of run_analysis!: the predictor
+update_xms! and the Newton loop of time_step!, src/Analysis.jl:193-196):
+ALE-viscous-bending (ALEVB) tether pull on a 32x32-element graded flat patch
+(34x34 control points, 8430 unknowns, half bandwidth 543), L = 1, kb = 1,
+kg = -1/2, ζv = 1, dt = 0.005, velocity-driven pull (pull_speed = 0.1, the
+reference's F_PULL Dirichlet condition), plain FP64.  Synthetic input: the flat
+patch of prepare_input plus a seeded out-of-plane perturbation z ~ U[-1e-4,
+1e-4] of the interior nodes (SplitMix64, seed 0).  Steps W+1..W+K are timed.
+
+Reported: value (resident state, device-timed), e2e (host buffers through the
+C ABI, H2D/D2H per step), p50/p99 step latency, the FP32-tangent + FP32-LU +
+FP64-refinement form on the same steps with its relative error, the roofline
+of the dominant kernel, and the CPU baseline (the oracle's complex-step
+assembly on all host cores + scipy sparse LU).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "membranealefem.jl_gb300"))
+
+WORKLOAD = dict(name="ALEVB tether pull, 32x32 graded patch (34x34 control points), plain FP64",
+                motion=5, n=32, length=1.0, kb=1.0, kg=-0.5, zeta_v=1.0, dt=0.005, pull_speed=0.1,
+                seed=0, amp=1e-4)
+METRIC = "membrane time-steps/s"
+
+
+# ---- distributed plumbing (replicas only: every rank runs its own patch) ---------
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist.get_rank(), ws, int(os.environ.get("LOCAL_RANK", "0")), dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---- CUDA runtime helpers (L2 flush, device sync) through libcudart --------------
+class Cudart:
+    def __init__(self):
+        self.lib = None
+        for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+            try:
+                self.lib = C.CDLL(name)
+                break
+            except OSError:
+                continue
+        if self.lib is None:
+            raise RuntimeError("libcudart not found")
+        self.buf = C.c_void_p()
+        self.nbytes = 512 << 20  # > L2 (129 MB): flush between timed steps
+        if self.lib.cudaMalloc(C.byref(self.buf), C.c_size_t(self.nbytes)) != 0:
+            raise RuntimeError("cudaMalloc for the L2 flush buffer failed")
+        self.k = 0
+
+    def set_device(self, d: int):
+        self.lib.cudaSetDevice(d)
+
+    def sync(self):
+        self.lib.cudaDeviceSynchronize()
+
+    def flush_l2(self):
+        self.k += 1
+        self.lib.cudaMemset(self.buf, C.c_int(self.k & 0xff), C.c_size_t(self.nbytes))
+        self.lib.cudaDeviceSynchronize()
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---- workload --------------------------------------------------------------------
+def make_params(M, wl=WORKLOAD):
+    return M.Params(motion=wl["motion"], scenario=M.F_PULL, num1el=wl["n"], num2el=wl["n"],
+                    length=wl["length"], kb=wl["kb"], kg=wl["kg"], zeta_v=wl["zeta_v"],
+                    pull_speed=wl["pull_speed"])
+
+
+def initial_state(M, p, mesh, wl=WORKLOAD):
+    _, xms, cps = M.prepare_input(p, mesh)
+    M.perturb_interior_z(mesh, xms, seed=wl["seed"], amp=wl["amp"])
+    return xms, cps
+
+
+def lu_flops(n, kl, ku, nb):
+    """FLOPs of the blocked banded LU as the kernels execute it: per panel the
+    trailing columns get w²/2 (unit-lower solve) + 2 (R - w) w (update)."""
+    fl_apply, fl_panel = 0.0, 0.0
+    j0 = 0
+    while j0 < n:
+        w = min(nb, n - j0)
+        R = min(n - j0, w + kl)
+        ncol = max(0, min(n, j0 + w + kl + ku) - (j0 + w))
+        fl_apply += ncol * (w * (w - 1) + 2.0 * (R - w) * w)
+        for jj in range(w):
+            rows = min(R, jj + kl + 1) - (jj + 1)
+            fl_panel += rows * (1 + 2.0 * (w - jj - 1))
+        j0 += w
+    return fl_panel, fl_apply
+
+
+def run_gb300(args, rank, world, local, dist):
+    import mafem as M
+    cu = Cudart()
+    cu.set_device(local)
+    wl = WORKLOAD
+    p = make_params(M)
+    mesh = M.Mesh(p)
+    dt = wl["dt"]
+    out = {}
+
+    # ---- resident state, device-timed (value) ----
+    with M.Solver(mesh, p, M.PLAIN_FP64) as s:
+        x0, c0 = initial_state(M, p, mesh)
+        s.upload(x0, c0)
+        t = 0.0
+        for _ in range(args.warmup):
+            t += dt
+            s.predict(dt)
+            s.time_step_resident(t, dt)
+        lat, iters, dev_ms = [], [], []
+        launches0 = s.launch_count()
+        cu.flush_l2()
+        barrier(dist)
+        cu.sync()
+        with ClockSampler(local) as clk:
+            for _ in range(args.steps):
+                t += dt
+                h0 = time.perf_counter()
+                s.predict(dt)
+                st = s.time_step_resident(t, dt)
+                lat.append((time.perf_counter() - h0) * 1e3)
+                iters.append(st["newton_iters"])
+                dev_ms.append(st["ms_total"])
+                cu.flush_l2()
+        cu.sync()
+        barrier(dist)
+        launches = s.launch_count() - launches0
+        total_ms = allmax(dist, float(sum(lat)))
+        x_fp64, c_fp64 = s.download()
+        # per-kernel timing of one factorisation (roofline)
+        kt = s.profile_factor(t, dt)
+    out["resident"] = dict(total_ms=total_ms, lat=lat, iters=iters, dev_ms=dev_ms, launches=launches,
+                           clocks=clk.summary(), kt=kt)
+
+    # ---- e2e: host buffers through the C ABI, H2D/D2H inside every step ----
+    mmo = [mesh.dofs[d] - 1 for d in (3, 4, 5)] if p.motion != M.LAG else [mesh.dofs[d] - 1 for d in (0, 1, 2)]
+    with M.Solver(mesh, p, M.PLAIN_FP64) as s:
+        xms, cps = initial_state(M, p, mesh)
+        t = 0.0
+
+        def host_step(t):
+            for j, d in enumerate(mmo):  # update_xms! predictor on the host (Analysis.jl:193)
+                xms[:, j] += dt * cps[:, d]
+            return s.time_step(xms, cps, t, dt)
+
+        for _ in range(args.warmup):
+            t += dt
+            host_step(t)
+        cu.flush_l2()
+        barrier(dist)
+        cu.sync()
+        elat = []
+        for _ in range(args.steps):
+            t += dt
+            h0 = time.perf_counter()
+            host_step(t)
+            elat.append((time.perf_counter() - h0) * 1e3)
+            cu.flush_l2()
+        cu.sync()
+        barrier(dist)
+        e2e_ms = allmax(dist, float(sum(elat)))
+        out["e2e"] = dict(total_ms=e2e_ms, lat=elat, bytes=8 * mesh.numnp * (3 + mesh.ndf))
+        out["e2e_state_err"] = float(np.abs(xms - x_fp64).max() / np.abs(x_fp64).max())
+
+    # ---- precision form on the same steps ----
+    with M.Solver(mesh, p, M.FP32_REFINE) as s:
+        x0, c0 = initial_state(M, p, mesh)
+        s.upload(x0, c0)
+        t = 0.0
+        for _ in range(args.warmup):
+            t += dt
+            s.predict(dt)
+            s.time_step_resident(t, dt)
+        cu.flush_l2()
+        cu.sync()
+        flat, fit, fref = [], [], []
+        for _ in range(args.steps):
+            t += dt
+            h0 = time.perf_counter()
+            s.predict(dt)
+            st = s.time_step_resident(t, dt)
+            flat.append((time.perf_counter() - h0) * 1e3)
+            fit.append(st["newton_iters"])
+            fref.append(st["refine_iters"])
+            cu.flush_l2()
+        x32, c32 = s.download()
+    lam = mesh.dofs[6] - 1
+    vel = [d for d in range(mesh.ndf) if d != lam]
+    out["fp32"] = dict(total_ms=float(sum(flat)), lat=flat, iters=fit, refine=fref,
+                       err_x=float(np.abs(x32 - x_fp64).max() / np.abs(x_fp64).max()),
+                       err_v=float(np.abs(c32[:, vel] - c_fp64[:, vel]).max() / np.abs(c_fp64[:, vel]).max()),
+                       err_lam=float(np.abs(c32[:, lam] - c_fp64[:, lam]).max() / np.abs(c_fp64[:, lam]).max()))
+    tf = C.c_double()
+    M.lib().mafem_probe_fp64_tflops(C.byref(tf))
+    out["fp64_tflops"] = tf.value
+    out["mesh"] = dict(numnp=mesh.numnp, ndf=mesh.ndf, nmdf=mesh.nmdf, kl=mesh.half_bw, numel=mesh.numel)
+    return out
+
+
+def cpu_baseline(wl=WORKLOAD, max_seconds=20.0, max_steps=3):
+    """The oracle's threaded complex-step assembly + scipy SuperLU (the stand-in for
+    the reference's Julia calc_r_K + UMFPACK) on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    q = O.Params(motion=wl["motion"], scenario=O.F_PULL, num1el=wl["n"], num2el=wl["n"], length=wl["length"],
+                 kb=wl["kb"], kg=wl["kg"], zv=wl["zeta_v"], pull_speed=wl["pull_speed"])
+    om = O.Mesh(q)
+    import mafem as M
+    mesh = M.Mesh(make_params(M, wl))
+    xms, cps = initial_state(M, make_params(M, wl), mesh, wl)
+    cores = os.cpu_count() or 1
+    t, dt, steps, iters = 0.0, wl["dt"], 0, 0
+    t0 = time.perf_counter()
+    while steps < max_steps and (time.perf_counter() - t0) < max_seconds:
+        t += dt
+        om.update_xms(xms, cps, dt)
+        iters += len(O.time_step_sparse(om, xms, cps, t, dt, nthreads=cores))
+        steps += 1
+    el = time.perf_counter() - t0
+    return {"value": steps / el, "unit": "time-steps/s", "cores": cores, "kind": "port",
+            "sample": f"first {steps} time steps ({iters} Newton iterations) of the workload: oracle complex-step "
+                      f"assembly on {cores} threads + scipy SuperLU, {el:.1f} s"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=47)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local, dist = dist_init()
+    wl = WORKLOAD
+    config = {"workload": wl["name"], "mesh": f"{wl['n']}x{wl['n']} elements", "motion": "ALEVB",
+              "dt": wl["dt"], "pull_speed": wl["pull_speed"], "length": wl["length"], "kb": wl["kb"],
+              "zeta_v": wl["zeta_v"], "time_steps": args.warmup + args.steps,
+              "l2": "flushed between timed steps (512 MB memset)", "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(max_seconds=60.0, max_steps=max(1, min(args.steps, 10)))
+        line = {"metric": METRIC, "value": cb["value"], "unit": "time-steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded flat patch)", "config": config, "impl": "reference",
+                "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "time-steps/s",
+                                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    r = run_gb300(args, rank, world, local, dist)
+    res = r["resident"]
+    K = args.steps
+    value = world * K / (res["total_ms"] / 1e3)
+    lat = sorted(res["lat"])
+    kt = r["kt"]
+    m = r["mesh"]
+    fl_panel, fl_apply = lu_flops(kt["n"], kt["kl"], kt["ku"], kt["nb"])
+    apply_launch_ms = kt["ms_apply"] / kt["n_apply"]
+    achieved = fl_apply / kt["n_apply"] / (apply_launch_ms * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": "time-steps/s", "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": res["total_ms"] / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded flat patch (SplitMix64 seed 0, interior z ~ U[-1e-4, 1e-4])",
+        "config": config,
+        "p50_step_ms": lat[len(lat) // 2], "p99_step_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+        "newton_iters_per_step": statistics.mean(res["iters"]),
+        "e2e": {"value": world * K / (r["e2e"]["total_ms"] / 1e3), "unit": "time-steps/s",
+                "h2d_bytes_per_step": r["e2e"]["bytes"], "d2h_bytes_per_step": r["e2e"]["bytes"],
+                "state_rel_err_vs_resident": r["e2e_state_err"]},
+        "gpu_launches": res["launches"],
+        "roofline": {"bound": "fp64", "kernel": "panel_apply_kernel<double> (banded-LU trailing update)",
+                     "achieved": achieved, "peak": r["fp64_tflops"], "unit": "TFLOP/s",
+                     "frac": achieved / r["fp64_tflops"],
+                     "peak_source": "FP64 FMA throughput measured live on this GPU (mafem_probe_fp64_tflops)",
+                     "flops_per_launch": fl_apply / kt["n_apply"], "launch_ms": apply_launch_ms,
+                     "share_of_factor": kt["ms_apply"] / (kt["ms_apply"] + kt["ms_panel"]),
+                     "traffic": None},
+        "phase_ms_per_iter": {"assemble": kt["ms_assemble"], "lu_panel": kt["ms_panel"], "lu_apply": kt["ms_apply"]},
+        "clocks": res["clocks"],
+        "precision_fp32_refine": {"value": K / (r["fp32"]["total_ms"] / 1e3), "unit": "time-steps/s",
+                                  "newton_iters_per_step": statistics.mean(r["fp32"]["iters"]),
+                                  "refine_sweeps_per_step": statistics.mean(r["fp32"]["refine"]),
+                                  "rel_err_xms": r["fp32"]["err_x"], "rel_err_vel": r["fp32"]["err_v"],
+                                  "rel_err_lambda": r["fp32"]["err_lam"]},
+        "mesh": m,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline()
+    if rank == 0:
+        print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -158,6 +158,24 @@ int mafem_time_step_host(mafem_handle* h, double* xms, double* cps, double time,
  * predictor + time_step! for each Δt; times[k] = t0 + sum(dts[0..k]). */
 int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, mafem_step_stats* last);
 
+/* ---- diagnostics --------------------------------------------------------------- */
+
+/* Number of kernels this handle has enqueued since mafem_create. */
+int64_t mafem_launch_count(const mafem_handle* h);
+
+typedef struct mafem_kernel_times {
+  double ms_assemble;         /* element kernel + gathers */
+  double ms_panel, ms_apply;  /* summed device time of the LU's two kernels */
+  int64_t n_panel, n_apply;   /* launches of each */
+  int64_t n, kl, ku, nb;      /* factorised system */
+} mafem_kernel_times;
+/* Assemble and factor the resident state once, timing every LU launch with
+ * CUDA events on the handle's stream (for roofline reporting). */
+int mafem_profile_factor(mafem_handle* h, double time, double dt, mafem_kernel_times* out);
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (the roof of
+ * the FP64 kernels; a short FMA-chain kernel on every SM). */
+int mafem_probe_fp64_tflops(double* tflops);
+
 #ifdef __cplusplus
 }
 #endif

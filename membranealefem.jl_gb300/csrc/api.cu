@@ -90,6 +90,7 @@ struct mafem_handle {
   bool factored = false;
   int max_refine = 30;
   double refine_tol = 1e-10;
+  int64_t launches = 0;  // kernels enqueued by this handle
 };
 
 #define CK(x)                                                               \
@@ -464,6 +465,7 @@ static int assemble(mafem_handle* h, double time, double dt) {
       return MAFEM_ERR_CUDA;
     }
     launch_band_gather<double>(h->P, h->ndf, h->nq, h->L, (const double*)h->d_Kel, (double*)h->d_band, h->st);
+    h->launches += 2;
   } else {
     e = launch_elem<float>(h->P, h->pp, time, dt, h->d_rel, (float*)h->d_Kel, h->st);
     if (e != cudaSuccess) {
@@ -471,8 +473,10 @@ static int assemble(mafem_handle* h, double time, double dt) {
       return MAFEM_ERR_CUDA;
     }
     launch_band_gather<float>(h->P, h->ndf, h->nq, h->L, (const float*)h->d_Kel, (float*)h->d_band, h->st);
+    h->launches += 2;
   }
   launch_resid_gather(h->P, h->ndf, h->nq, h->d_rel, h->d_r, h->st);
+  h->launches += 1;
   CK(cudaGetLastError());
   h->factored = false;
   return MAFEM_OK;
@@ -487,14 +491,16 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
     CK(cudaMemcpyAsync(h->d_x, rhs_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     if (!h->factored) {
       CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
-      band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, h->d_x,
-                             h->apply_threads, h->apply_blocks, h->st);
+      h->launches += band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info,
+                                            h->d_x, h->apply_threads, h->apply_blocks, h->st);
       h->factored = true;
     } else {
       band_forward<double, double>((const double*)h->d_band, h->L, h->d_perm, h->rmax, h->d_x, h->st);
+      h->launches += 1;
     }
     cudaEventRecord(h->ev[2], h->st);
     band_backward<double, double>((const double*)h->d_band, h->L, h->d_x, h->st);
+    h->launches += 1;
     CK(cudaGetLastError());
     return MAFEM_OK;
   }
@@ -502,8 +508,8 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   if (!h->factored) {
     CK(cudaMemcpyAsync(h->d_band0, h->d_band, (size_t)h->L.ldb * n * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
     CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
-    band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
-                          h->apply_threads, h->apply_blocks, h->st);
+    h->launches += band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
+                                         h->apply_threads, h->apply_blocks, h->st);
     h->factored = true;
   }
   cudaEventRecord(h->ev[2], h->st);
@@ -512,6 +518,7 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   // ‖rhs‖
   launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part, h->d_out + 4,
                               h->st);
+  h->launches += 2;
   CK(cudaMemcpyAsync(h->h_out + 4, h->d_out + 4, sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   const double r0 = h->h_out[4];
@@ -524,6 +531,7 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
     launch_axpy(n, h->d_dx, h->d_x, h->st);
     launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part,
                                 h->d_out + 3, h->st);
+    h->launches += 5;
     CK(cudaMemcpyAsync(h->h_out + 3, h->d_out + 3, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     *sweeps = k + 1;
@@ -604,6 +612,7 @@ extern "C" int mafem_solve(mafem_handle* h, const double* r, double* du_out) {
 extern "C" int mafem_predict(mafem_handle* h, double dt) {
   if (!h) return MAFEM_ERR_ARG;
   launch_predictor(h->P, h->pp, dt, h->st);
+  h->launches += 1;
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(h->st));
   return MAFEM_OK;
@@ -626,6 +635,7 @@ extern "C" int mafem_time_step(mafem_handle* h, double time, double dt, mafem_st
     if (rc) return rc;
     cudaEventRecord(h->ev[3], h->st);
     launch_newton_update(h->P, h->pp, dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st);
+    h->launches += 2;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
@@ -684,9 +694,106 @@ extern "C" int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, dou
   for (int k = 0; k < nsteps; ++k) {
     t += dts[k];  // times = cumsum(Δts) + t0 (Analysis.jl:154)
     launch_predictor(h->P, h->pp, dts[k], h->st);
+    h->launches += 1;
     CK(cudaGetLastError());
     int rc = mafem_time_step(h, t, dts[k], last);
     if (rc) return rc;
   }
+  return MAFEM_OK;
+}
+
+extern "C" int64_t mafem_launch_count(const mafem_handle* h) { return h ? h->launches : -1; }
+
+// Per-kernel device time of one assembly + factorisation of the resident
+// state (CUDA events on the handle's stream around every launch).
+extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, mafem_kernel_times* out) {
+  if (!h || !out) return MAFEM_ERR_ARG;
+  std::memset(out, 0, sizeof *out);
+  cudaEvent_t a0, a1;
+  CK(cudaEventCreate(&a0));
+  CK(cudaEventCreate(&a1));
+  const int64_t npan = h->npan;
+  std::vector<cudaEvent_t> ev((size_t)3 * npan);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaEventRecord(a0, h->st));
+  int rc = assemble(h, time, dt);
+  if (rc) return rc;
+  CK(cudaEventRecord(a1, h->st));
+  CK(cudaMemcpyAsync(h->d_x, h->d_r, h->nmdf * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  if (h->precision == MAFEM_PLAIN_FP64)
+    band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, h->d_x,
+                           h->apply_threads, h->apply_blocks, h->st, ev.data());
+  else
+    band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
+                          h->apply_threads, h->apply_blocks, h->st, ev.data());
+  h->factored = true;
+  CK(cudaStreamSynchronize(h->st));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a0, a1);
+  out->ms_assemble = ms;
+  for (int64_t p = 0; p < npan; ++p) {
+    float m1 = 0, m2 = 0;
+    cudaEventElapsedTime(&m1, ev[3 * p], ev[3 * p + 1]);
+    cudaEventElapsedTime(&m2, ev[3 * p + 1], ev[3 * p + 2]);
+    out->ms_panel += m1;
+    out->ms_apply += m2;
+  }
+  out->n_panel = npan;
+  out->n_apply = npan;
+  out->n = h->nmdf;
+  out->kl = h->L.kl;
+  out->ku = h->L.ku;
+  out->nb = h->L.nb;
+  for (auto& e : ev) cudaEventDestroy(e);
+  cudaEventDestroy(a0);
+  cudaEventDestroy(a1);
+  return MAFEM_OK;
+}
+
+// FP64 FMA throughput of the current device (independent FMA chains, all SMs):
+// the compute roof of the FP64 kernels, measured rather than assumed.
+__global__ void fp64_fma_probe_kernel(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+extern "C" int mafem_probe_fp64_tflops(double* tflops) {
+  if (!tflops) return MAFEM_ERR_ARG;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    set_global_error("no CUDA device");
+    return MAFEM_ERR_CUDA;
+  }
+  const int nb = sms * 8, nt = 256, iters = 2000;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * nb * nt) != cudaSuccess) return MAFEM_ERR_OOM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int w = 0; w < 2; ++w) fp64_fma_probe_kernel<<<nb, nt>>>(out, iters, 0.999999, 1e-7);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    fp64_fma_probe_kernel<<<nb, nt>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    best = std::min(best, ms);
+  }
+  cudaError_t e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  if (e != cudaSuccess) {
+    set_global_error(cudaGetErrorString(e));
+    return MAFEM_ERR_CUDA;
+  }
+  *tflops = 2.0 * 8 * (double)iters * nb * nt / (best * 1e-3) / 1e12;
   return MAFEM_OK;
 }

@@ -298,20 +298,28 @@ cudaError_t band_lu_setup(const BandLayout& L, int apply_threads) {
 
 // Factor (and, if rhs != nullptr, forward-substitute rhs in the same sweep).
 template <class T>
-void band_lu_factor(T* ab, const BandLayout& L, int* ipiv, int* perm_all, int rmax, int* info, T* rhs,
-                    int apply_threads, int apply_blocks, cudaStream_t st) {
+int band_lu_factor(T* ab, const BandLayout& L, int* ipiv, int* perm_all, int rmax, int* info, T* rhs,
+                   int apply_threads, int apply_blocks, cudaStream_t st, cudaEvent_t* ev) {
   const int64_t npan = (L.n + L.nb - 1) / L.nb;
   const size_t ps = panel_smem_bytes<T>(L), as = apply_smem_bytes<T>(L, apply_threads);
+  int launches = 0;
   for (int64_t p = 0; p < npan; ++p) {
     const int64_t j0 = p * L.nb;
+    if (ev) cudaEventRecord(ev[3 * p], st);
     panel_factor_kernel<T><<<1, 512, ps, st>>>(ab, L, j0, ipiv, perm_all + p * rmax, info);
+    ++launches;
+    if (ev) cudaEventRecord(ev[3 * p + 1], st);
     const int64_t j1 = j0 + min64(L.nb, L.n - j0);
     const int64_t ncol = min64(L.n, j1 + L.kl + L.ku) - j1 + (rhs ? 1 : 0);
-    if (ncol <= 0) continue;
-    int nwarp = apply_threads / 32;
-    int blocks = (int)min64(apply_blocks, (ncol + nwarp - 1) / nwarp);
-    panel_apply_kernel<T><<<blocks, apply_threads, as, st>>>(ab, L, j0, perm_all + p * rmax, rhs);
+    if (ncol > 0) {
+      int nwarp = apply_threads / 32;
+      int blocks = (int)min64(apply_blocks, (ncol + nwarp - 1) / nwarp);
+      panel_apply_kernel<T><<<blocks, apply_threads, as, st>>>(ab, L, j0, perm_all + p * rmax, rhs);
+      ++launches;
+    }
+    if (ev) cudaEventRecord(ev[3 * p + 2], st);
   }
+  return launches;
 }
 
 template <class T, class V>
@@ -334,10 +342,10 @@ template size_t apply_smem_bytes<double>(const BandLayout&, int);
 template size_t apply_smem_bytes<float>(const BandLayout&, int);
 template cudaError_t band_lu_setup<double>(const BandLayout&, int);
 template cudaError_t band_lu_setup<float>(const BandLayout&, int);
-template void band_lu_factor<double>(double*, const BandLayout&, int*, int*, int, int*, double*, int, int,
-                                     cudaStream_t);
-template void band_lu_factor<float>(float*, const BandLayout&, int*, int*, int, int*, float*, int, int,
-                                    cudaStream_t);
+template int band_lu_factor<double>(double*, const BandLayout&, int*, int*, int, int*, double*, int, int,
+                                    cudaStream_t, cudaEvent_t*);
+template int band_lu_factor<float>(float*, const BandLayout&, int*, int*, int, int*, float*, int, int,
+                                   cudaStream_t, cudaEvent_t*);
 template cudaError_t band_solve_setup<double, double>(const BandLayout&);
 template cudaError_t band_solve_setup<float, double>(const BandLayout&);
 template void band_forward<double, double>(const double*, const BandLayout&, const int*, int, double*,

@@ -117,9 +117,11 @@ template <class T>
 size_t apply_smem_bytes(const BandLayout& L, int threads);
 template <class T>
 cudaError_t band_lu_setup(const BandLayout& L, int apply_threads);
+// Enqueues the blocked factorisation; returns the number of kernels launched.
+// With ev != nullptr, records ev[3p], ev[3p+1], ev[3p+2] around panel p's two kernels.
 template <class T>
-void band_lu_factor(T* ab, const BandLayout& L, int* ipiv, int* perm_all, int rmax, int* info, T* rhs,
-                    int apply_threads, int apply_blocks, cudaStream_t st);
+int band_lu_factor(T* ab, const BandLayout& L, int* ipiv, int* perm_all, int rmax, int* info, T* rhs,
+                   int apply_threads, int apply_blocks, cudaStream_t st, cudaEvent_t* ev = nullptr);
 template <class T, class V>
 cudaError_t band_solve_setup(const BandLayout& L);
 template <class T, class V>

@@ -98,6 +98,15 @@ class StepStats(C.Structure):
                 "ms_solve": self.ms_solve, "ms_total": self.ms_total}
 
 
+class KernelTimes(C.Structure):
+    _fields_ = [("ms_assemble", C.c_double), ("ms_panel", C.c_double), ("ms_apply", C.c_double),
+                ("n_panel", C.c_int64), ("n_apply", C.c_int64), ("n", C.c_int64), ("kl", C.c_int64),
+                ("ku", C.c_int64), ("nb", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -135,6 +144,10 @@ def lib():
         L.mafem_time_step_host.argtypes = [vp, _PD, _PD, C.c_double, C.c_double,
                                            C.POINTER(StepStats)]
         L.mafem_run.argtypes = [vp, _PD, C.c_int32, C.c_double, C.POINTER(StepStats)]
+        L.mafem_launch_count.argtypes = [vp]
+        L.mafem_launch_count.restype = C.c_int64
+        L.mafem_profile_factor.argtypes = [vp, C.c_double, C.c_double, C.POINTER(KernelTimes)]
+        L.mafem_probe_fp64_tflops.argtypes = [C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -312,6 +325,16 @@ class Solver:
     @property
     def device_bytes(self) -> int:
         return int(lib().mafem_device_bytes(self.h))
+
+    def launch_count(self) -> int:
+        """Kernels this handle has enqueued so far."""
+        return int(lib().mafem_launch_count(self.h))
+
+    def profile_factor(self, time: float, dt: float) -> dict:
+        """Per-kernel device time of one assembly + factorisation of the resident state."""
+        kt = KernelTimes()
+        _raise(lib().mafem_profile_factor(self.h, time, dt, C.byref(kt)), self.h)
+        return kt.as_dict()
 
     def upload(self, xms, cps):
         xms = np.asfortranarray(xms, dtype=np.float64)

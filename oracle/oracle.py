@@ -497,3 +497,34 @@ def _unpack_gds(out):
         o += sz
         d[name] = float(v[0]) if not shp else v.reshape(shp[::-1]).T.copy()
     return d
+
+
+def time_step_sparse(mesh: Mesh, xms, cps, time: float, dt: float, nthreads: int = 0,
+                     max_iter: int = 14):
+    """time_step! (FiniteElement.jl:11-63) with the oracle's threaded complex-step
+    assembly and scipy's sparse LU (SuperLU) in place of the reference's UMFPACK
+    `K \\ r`.  The CPU baseline of the benchmarks.  Updates xms/cps in place and
+    returns the list of ε = ‖Δu‖/nmdf."""
+    import scipy.sparse.linalg as sla
+    assert xms.flags.f_contiguous and cps.flags.f_contiguous
+    ID_inv = mesh.ID_inv
+    nodes, dofs = ID_inv[:, 0] - 1, ID_inv[:, 1] - 1
+    mmo = {LAG: [1, 2, 3], STATIC: []}.get(mesh.p.motion, [4, 5, 6])
+    mmo = [mesh.dofs[d - 1] for d in mmo]
+    eps = []
+    for _ in range(max_iter):
+        r, ab = mesh.calc_r_K(xms, cps, time, dt, nthreads=nthreads)
+        K = band_to_csr(ab, mesh.half_bw, mesh.half_bw, mesh.nmdf)
+        du = -sla.spsolve(K.tocsc(), r)
+        dc = np.zeros_like(cps)
+        dc[nodes, dofs] = du
+        cps += dc
+        for j, d in enumerate(mmo):
+            if d:
+                xms[:, j] += dt * dc[:, d - 1]
+        eps.append(float(np.linalg.norm(du) / mesh.nmdf))
+        if eps[-1] < mesh.p.eps_nr:
+            break
+    if not eps[-1] < mesh.p.eps_nr:
+        raise AssertionFailed("did not reach Newton--Raphson tolerance")
+    return eps
