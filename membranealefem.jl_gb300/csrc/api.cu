@@ -51,7 +51,7 @@ int64_t half_bandwidth(const mafem_mesh_desc& d) {
 // Panel width: the FP64 panel and its trailing-update CTA keep (nb + kl) x nb
 // values in shared memory.
 static int choose_nb(int kl, int precision) {
-  const size_t limit = 200 * 1024;
+  const size_t limit = 220 * 1024;
   const size_t esz = precision == MAFEM_PLAIN_FP64 ? 8 : 4;
   for (int nb : {32, 16, 8}) {
     size_t R = (size_t)nb + kl;
@@ -86,6 +86,8 @@ struct mafem_handle {
   int *d_ipiv = nullptr, *d_perm = nullptr, *d_info = nullptr;
   double* h_out = nullptr;  // pinned: [0] eps [1] |r| [2] nan [3] refine |res| [4] info
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;          // LU lookahead stream
+  std::vector<cudaEvent_t> ev_pool;    // 2*npan + 2 ordering events for the lookahead
   cudaEvent_t ev[6] = {};
   bool factored = false;
   int max_refine = 30;
@@ -326,6 +328,14 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     return MAFEM_ERR_CUDA;
   }
   for (auto& e : h->ev) cudaEventCreate(&e);
+  ce = cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    set_global_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
+    mafem_destroy(hp.release());
+    return MAFEM_ERR_CUDA;
+  }
+  h->ev_pool.resize((size_t)2 * h->npan + 2);
+  for (auto& e : h->ev_pool) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
   int* d_ix;
   int* d_lm;
   int* d_uel;
@@ -424,8 +434,12 @@ extern "C" int mafem_destroy(mafem_handle* h) {
   if (h->st) cudaStreamSynchronize(h->st);
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_out) cudaFreeHost(h->h_out);
+  if (h->st2) cudaStreamSynchronize(h->st2);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
+  for (auto& e : h->ev_pool)
+    if (e) cudaEventDestroy(e);
+  if (h->st2) cudaStreamDestroy(h->st2);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return MAFEM_OK;
@@ -491,8 +505,14 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
     CK(cudaMemcpyAsync(h->d_x, rhs_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     if (!h->factored) {
       CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
-      h->launches += band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info,
-                                            h->d_x, h->apply_threads, h->apply_blocks, h->st);
+      const int nl = band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info,
+                                            h->d_x, h->apply_threads, h->apply_blocks, h->st, h->st2,
+                                            h->ev_pool.data(), nullptr);
+      if (nl < 0) {
+        h->err = "banded LU launch failed: " + std::string(cudaGetErrorString(cudaGetLastError()));
+        return MAFEM_ERR_CUDA;
+      }
+      h->launches += nl;
       h->factored = true;
     } else {
       band_forward<double, double>((const double*)h->d_band, h->L, h->d_perm, h->rmax, h->d_x, h->st);
@@ -508,8 +528,14 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   if (!h->factored) {
     CK(cudaMemcpyAsync(h->d_band0, h->d_band, (size_t)h->L.ldb * n * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
     CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
-    h->launches += band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
-                                         h->apply_threads, h->apply_blocks, h->st);
+    const int nl = band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
+                                         h->apply_threads, h->apply_blocks, h->st, h->st2, h->ev_pool.data(),
+                                         nullptr);
+    if (nl < 0) {
+      h->err = "banded LU launch failed: " + std::string(cudaGetErrorString(cudaGetLastError()));
+      return MAFEM_ERR_CUDA;
+    }
+    h->launches += nl;
     h->factored = true;
   }
   cudaEventRecord(h->ev[2], h->st);
@@ -721,12 +747,13 @@ extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, maf
   if (rc) return rc;
   CK(cudaEventRecord(a1, h->st));
   CK(cudaMemcpyAsync(h->d_x, h->d_r, h->nmdf * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
   if (h->precision == MAFEM_PLAIN_FP64)
     band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, h->d_x,
-                           h->apply_threads, h->apply_blocks, h->st, ev.data());
+                           h->apply_threads, h->apply_blocks, h->st, nullptr, nullptr, ev.data());
   else
     band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
-                          h->apply_threads, h->apply_blocks, h->st, ev.data());
+                          h->apply_threads, h->apply_blocks, h->st, nullptr, nullptr, ev.data());
   h->factored = true;
   CK(cudaStreamSynchronize(h->st));
   float ms = 0;

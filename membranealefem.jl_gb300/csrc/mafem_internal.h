@@ -112,16 +112,17 @@ void launch_band_residual(const T* a0, const BandLayout& L, const double* x, con
 void launch_axpy(int64_t n, const double* dx, double* x, cudaStream_t st);
 
 template <class T>
-size_t panel_smem_bytes(const BandLayout& L);
-template <class T>
 size_t apply_smem_bytes(const BandLayout& L, int threads);
 template <class T>
 cudaError_t band_lu_setup(const BandLayout& L, int apply_threads);
 // Enqueues the blocked factorisation; returns the number of kernels launched.
-// With ev != nullptr, records ev[3p], ev[3p+1], ev[3p+2] around panel p's two kernels.
+// st2 + ev_pool (2*npan+2 events) enable the two-stream lookahead; with
+// prof != nullptr it runs serially on st and records prof[3p], prof[3p+1],
+// prof[3p+2] around panel p's two kernels.
 template <class T>
 int band_lu_factor(T* ab, const BandLayout& L, int* ipiv, int* perm_all, int rmax, int* info, T* rhs,
-                   int apply_threads, int apply_blocks, cudaStream_t st, cudaEvent_t* ev = nullptr);
+                   int apply_threads, int apply_blocks, cudaStream_t st, cudaStream_t st2, cudaEvent_t* ev_pool,
+                   cudaEvent_t* prof);
 template <class T, class V>
 cudaError_t band_solve_setup(const BandLayout& L);
 template <class T, class V>

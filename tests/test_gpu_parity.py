@@ -142,3 +142,45 @@ def test_newton_failure_is_reported_not_hung():
         with pytest.raises(M.NewtonNotConverged):
             s.time_step(xms, cps, 0.01, 0.01)
         assert s.last_stats["newton_iters"] == 14
+
+
+def _config1():
+    p, q = params_pair(M.ALEVB, M.F_PULL, 32, 32, pull_speed=0.1)
+    mesh, om = M.Mesh(p), O.Mesh(q)
+    _, xms, cps = M.prepare_input(p, mesh)
+    M.perturb_interior_z(mesh, xms, seed=0, amp=1e-4)
+    return p, mesh, om, xms, cps
+
+
+def test_config1_assembly_and_solve():
+    """Full benchmark size (8430 unknowns, half bandwidth 543)."""
+    import scipy.sparse.linalg as sla
+    p, mesh, om, xms, cps = _config1()
+    dt = 0.005
+    om.update_xms(xms, cps, dt)
+    with M.Solver(mesh, p) as s:
+        r, ab = s.calc_r_K(xms, cps, dt, dt)
+        du = s.solve(r)
+    r0, ab0 = om.calc_r_K(xms, cps, dt, dt)
+    kl = mesh.half_bw
+    assert rel(r, r0) < 1e-12
+    assert rel(ab[:, kl:], ab0[:, kl:]) < 1e-11
+    K = O.band_to_csr(ab0, kl, kl, mesh.nmdf).tocsc()
+    ref = -sla.spsolve(K, r0)
+    assert rel(du, ref) < 1e-9
+
+
+def test_config1_steps_match_oracle():
+    p, mesh, om, xms, cps = _config1()
+    x2, c2 = xms.copy(order="F"), cps.copy(order="F")
+    dt, t = 0.005, 0.0
+    with M.Solver(mesh, p) as s:
+        for _ in range(4):
+            t += dt
+            om.update_xms(xms, cps, dt)
+            st = s.time_step(xms, cps, t, dt)
+            om.update_xms(x2, c2, dt)
+            eps = O.time_step_sparse(om, x2, c2, t, dt)
+            assert st["newton_iters"] == len(eps), (st["eps"], eps)
+    assert rel(xms, x2) < 1e-9
+    assert rel(cps, c2) < 1e-9
