@@ -449,21 +449,32 @@ static int cluster_threads(const BandLayout& L) {
   return 4 * ((rc + 7) / 8 * 8);
 }
 
+// Kernel attributes are process-wide, so the dynamic shared-memory cap is set
+// to the device's opt-in maximum (never to one handle's size, which could
+// lower it under another live handle); each layout is then checked against it.
 template <class T>
 cudaError_t band_lu_setup(const BandLayout& L, int apply_threads) {
-  cudaError_t e = cudaFuncSetAttribute(panel_cluster_kernel<T, kClusterCS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)cluster_smem_bytes<T>(L));
+  int dev = 0, cap = 0;
+  cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (kClusterCS > 8) {
-    e = cudaFuncSetAttribute(panel_cluster_kernel<T, kClusterCS>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    if (e != cudaSuccess) return e;
-  }
+  e = cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  const size_t need_cluster = cluster_smem_bytes<T>(L) + 2 * sizeof(PanelInbox<T>) + 1024;
+  const size_t need_apply = apply_smem_bytes<T>(L, apply_threads);
+  const size_t need_col = ((size_t)L.nb + L.kl) * sizeof(T) + 32 * 33 * sizeof(T);
+  if (need_cluster > (size_t)cap || need_apply > (size_t)cap || need_col > (size_t)cap) return cudaErrorInvalidValue;
   if (cluster_threads(L) > 512) return cudaErrorInvalidValue;
-  e = cudaFuncSetAttribute(panel_apply_col_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(((size_t)L.nb + L.kl) * sizeof(T)));
-  if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(panel_apply_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)apply_smem_bytes<T>(L, apply_threads));
+  const int dyn_cap = cap - 20 * 1024;  // room for the kernels' static shared memory
+  if ((e = cudaFuncSetAttribute(panel_cluster_kernel<T, kClusterCS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                dyn_cap)) != cudaSuccess)
+    return e;
+  if (kClusterCS > 8 && (e = cudaFuncSetAttribute(panel_cluster_kernel<T, kClusterCS>,
+                                                  cudaFuncAttributeNonPortableClusterSizeAllowed, 1)) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(panel_apply_col_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_cap)) !=
+      cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(panel_apply_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap);
 }
 
 template <class T>

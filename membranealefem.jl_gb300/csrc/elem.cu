@@ -458,13 +458,10 @@ size_t elem_smem_bytes(int nq, int epb) {
 template <class T, int MOTION, int EPB>
 static cudaError_t launch_elem_t(const DevPatch& P, const PhysParams& pp, double time, double dt, double* r_el,
                                  T* K_el, cudaStream_t st) {
-  static bool attr_done = false;  // one-time shared-memory opt-in per instantiation
-  if (!attr_done) {
-    cudaError_t e = cudaFuncSetAttribute(elem_kernel<T, MOTION, EPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)elem_smem_bytes<T>(72, EPB));
-    if (e != cudaSuccess) return e;
-    attr_done = true;
-  }
+  // the cap is the size needed by the largest element (nq = 72), identical for every caller
+  cudaError_t e = cudaFuncSetAttribute(elem_kernel<T, MOTION, EPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)elem_smem_bytes<T>(72, EPB));
+  if (e != cudaSuccess) return e;
   const int blocks = (P.numel + EPB - 1) / EPB;
   elem_kernel<T, MOTION, EPB><<<blocks, EPB * pp.nq, elem_smem_bytes<T>(pp.nq, EPB), st>>>(P, pp, time, dt, r_el,
                                                                                          K_el);
