@@ -176,6 +176,24 @@ int mafem_profile_factor(mafem_handle* h, double time, double dt, mafem_kernel_t
  * the FP64 kernels; a short FMA-chain kernel on every SM). */
 int mafem_probe_fp64_tflops(double* tflops);
 
+/* ---- allocation-free solve --------------------------------------------------------- */
+
+/* Factor and solve A x = rhs for a banded A (LAPACK band layout, A(i,j) at
+ * band_dev[j*ldab + kl+ku+i-j], kl == ku, ldab >= 2kl+ku+1; all three arrays are
+ * device pointers owned by the caller) without allocating device memory.  No
+ * counterpart in the reference: it exists for callers that must not call
+ * cudaMalloc -- e.g. a Julia host whose CUDA.jl memory pool accounts for every
+ * device byte, or a loop that cannot afford cudaMalloc's device-wide
+ * synchronisation.  Its scratch is one static 32 MiB device array inside the
+ * library (held by every GPU that loads it until exit): systems needing more --
+ * about 8*n*(3kl+65) + 4*n*(kl+33)/32 bytes -- return MAFEM_ERR_ARG.  All calls
+ * share that array, so calls that overlap on the GPU race; order them on one
+ * stream.  The first call on a device looks the array up (cudaGetSymbolAddress)
+ * and must come before any stream capture.  Runs on `stream` (NULL = default
+ * stream) and returns after synchronising it. */
+int mafem_band_solve_noalloc(const double* band_dev, int64_t n, int64_t kl, int64_t ku, int64_t ldab,
+                             const double* rhs_dev, double* x_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
