@@ -93,6 +93,14 @@ struct mafem_handle {
   int max_refine = 30;
   double refine_tol = 1e-10;
   int64_t launches = 0;  // kernels enqueued by this handle
+  // node-block pivoting (band_lu_blk.cu): the default; full partial pivoting
+  // (band_lu.cu) is the fallback for a block without a usable pivot
+  bool use_blk = false;
+  bool last_blk = false;  // which factorisation the band currently holds
+  int ndfp = 0;
+  int* d_blk_end = nullptr;
+  void* d_rdiag = nullptr;
+  int64_t fallbacks = 0;
 };
 
 #define CK(x)                                                               \
@@ -188,6 +196,7 @@ static int64_t footprint(const mafem_mesh_desc* d, int precision, int64_t kl) {
   b += d->numel * nq * nq * esz + d->numel * nq * 8;                             // element staging
   b += d->numnp * (3 + d->ndf) * 8 + d->nmdf * 8 * 6;                           // state + vectors
   b += ((d->nmdf + nb - 1) / std::max(nb, 1)) * ((int64_t)nb + kl) * 4;           // panel permutations
+  b += d->nmdf * (esz + 4);                                                      // pivot reciprocals, blocks
   return b;
 }
 
@@ -370,6 +379,18 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
   UP(d_tab, tab);
   UP(d_db, db);
   UP(d_btab, btab);
+  // pivot blocks: the unknowns of one node (consecutive in the ID numbering)
+  std::vector<int> blk_end(n);
+  int maxblk = 1;
+  for (int64_t q = 0; q < n;) {
+    int64_t e = q;
+    while (e < n && unk_node[e] == unk_node[q]) ++e;
+    for (int64_t k = q; k < e; ++k) blk_end[k] = (int)e;
+    maxblk = std::max(maxblk, (int)(e - q));
+    q = e;
+  }
+  h->ndfp = maxblk - 1;
+  UP(h->d_blk_end, blk_end);
   double *d_xms, *d_cps;
   AL(d_xms, (size_t)numnp * 3);
   AL(d_cps, (size_t)numnp * ndf);
@@ -385,19 +406,23 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
   AL(h->d_info, 4);
   const size_t band_elems = (size_t)h->L.ldb * n;
   if (precision == MAFEM_PLAIN_FP64) {
-    double *kel, *band;
+    double *kel, *band, *rd;
     AL(kel, (size_t)numel * nq * nq);
     AL(band, band_elems);
+    AL(rd, n);
     h->d_Kel = kel;
     h->d_band = band;
+    h->d_rdiag = rd;
   } else {
-    float *kel, *band, *band0;
+    float *kel, *band, *band0, *rd;
     AL(kel, (size_t)numel * nq * nq);
     AL(band, band_elems);
     AL(band0, band_elems);
+    AL(rd, n);
     h->d_Kel = kel;
     h->d_band = band;
     h->d_band0 = band0;
+    h->d_rdiag = rd;
   }
   ce = cudaMallocHost(&h->h_out, 16 * sizeof(double));
   if (ce != cudaSuccess) {
@@ -424,6 +449,12 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     set_global_error(std::string("kernel attribute setup: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
     mafem_destroy(hp.release());
     return MAFEM_ERR_CUDA;
+  }
+  if (h->L.kl >= h->ndfp && h->L.nb + h->ndfp <= 40) {
+    const cudaError_t e3 = precision == MAFEM_PLAIN_FP64 ? blk_lu_setup<double>(h->L, h->ndfp)
+                                                          : blk_lu_setup<float>(h->L, h->ndfp);
+    h->use_blk = (e3 == cudaSuccess);
+    cudaGetLastError();
   }
   *out = hp.release();
   return MAFEM_OK;
@@ -496,6 +527,58 @@ static int assemble(mafem_handle* h, double time, double dt) {
   return MAFEM_OK;
 }
 
+// Factorise the assembled band: node-block pivoting first; if a node block has
+// no usable pivot, re-gather the band from the element blocks and factor it
+// with full partial pivoting.  `x` (may be null) is the right-hand side that
+// rides along the factorisation (forward substitution); `rhs0` restores it for
+// the fallback.
+static int factor(mafem_handle* h, double* x, const double* rhs0) {
+  const int64_t n = h->nmdf;
+  const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
+  CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
+  if (h->use_blk) {
+    const int nl = fp64 ? blk_lu_factor<double>((double*)h->d_band, h->L, h->ndfp, h->d_blk_end, h->d_ipiv, h->d_perm,
+                                                h->rmax, (double*)h->d_rdiag, h->d_info, x, h->st, h->st2,
+                                                h->ev_pool.data(), nullptr)
+                        : blk_lu_factor<float>((float*)h->d_band, h->L, h->ndfp, h->d_blk_end, h->d_ipiv, h->d_perm,
+                                               h->rmax, (float*)h->d_rdiag, h->d_info, nullptr, h->st, h->st2,
+                                               h->ev_pool.data(), nullptr);
+    h->launches += nl;
+    CK(cudaGetLastError());
+    int info = 0;
+    CK(cudaMemcpyAsync(&info, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    if (info == 0) {
+      h->factored = true;
+      h->last_blk = true;
+      return MAFEM_OK;
+    }
+    // fallback: rebuild the band from the element blocks, then full pivoting
+    ++h->fallbacks;
+    if (fp64)
+      launch_band_gather<double>(h->P, h->ndf, h->nq, h->L, (const double*)h->d_Kel, (double*)h->d_band, h->st);
+    else
+      CK(cudaMemcpyAsync(h->d_band, h->d_band0, (size_t)h->L.ldb * n * sizeof(float), cudaMemcpyDeviceToDevice,
+                         h->st));
+    if (x && rhs0) CK(cudaMemcpyAsync(x, rhs0, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
+  }
+  const int nl = fp64 ? band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, x,
+                                               h->apply_threads, h->apply_blocks, h->st, h->st2, h->ev_pool.data(),
+                                               nullptr)
+                      : band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info,
+                                              nullptr, h->apply_threads, h->apply_blocks, h->st, h->st2,
+                                              h->ev_pool.data(), nullptr);
+  if (nl < 0) {
+    h->err = "banded LU launch failed: " + std::string(cudaGetErrorString(cudaGetLastError()));
+    return MAFEM_ERR_CUDA;
+  }
+  h->launches += nl;
+  h->factored = true;
+  h->last_blk = false;
+  return MAFEM_OK;
+}
+
 // Solve K x = rhs (rhs in d_x on entry for the plain form; x in d_x on exit).
 // Factors the band if needed.  Returns the number of refinement sweeps in *sweeps.
 static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps) {
@@ -504,22 +587,21 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   if (h->precision == MAFEM_PLAIN_FP64) {
     CK(cudaMemcpyAsync(h->d_x, rhs_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     if (!h->factored) {
-      CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
-      const int nl = band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info,
-                                            h->d_x, h->apply_threads, h->apply_blocks, h->st, h->st2,
-                                            h->ev_pool.data(), nullptr);
-      if (nl < 0) {
-        h->err = "banded LU launch failed: " + std::string(cudaGetErrorString(cudaGetLastError()));
-        return MAFEM_ERR_CUDA;
-      }
-      h->launches += nl;
-      h->factored = true;
+      int rc = factor(h, h->d_x, rhs_dev);
+      if (rc) return rc;
+    } else if (h->last_blk) {
+      blk_forward<double, double>((const double*)h->d_band, h->L, h->ndfp, h->d_perm, h->rmax,
+                                  (const double*)h->d_rdiag, h->d_x, h->st);
+      h->launches += 1;
     } else {
       band_forward<double, double>((const double*)h->d_band, h->L, h->d_perm, h->rmax, h->d_x, h->st);
       h->launches += 1;
     }
     cudaEventRecord(h->ev[2], h->st);
-    band_backward<double, double>((const double*)h->d_band, h->L, h->d_x, h->st);
+    if (h->last_blk)
+      blk_backward<double, double>((const double*)h->d_band, h->L, h->ndfp, (const double*)h->d_rdiag, h->d_x, h->st);
+    else
+      band_backward<double, double>((const double*)h->d_band, h->L, h->d_x, h->st);
     h->launches += 1;
     CK(cudaGetLastError());
     return MAFEM_OK;
@@ -527,16 +609,8 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   // FP32 factor of the FP32 tangent, FP64 iterative refinement
   if (!h->factored) {
     CK(cudaMemcpyAsync(h->d_band0, h->d_band, (size_t)h->L.ldb * n * sizeof(float), cudaMemcpyDeviceToDevice, h->st));
-    CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
-    const int nl = band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
-                                         h->apply_threads, h->apply_blocks, h->st, h->st2, h->ev_pool.data(),
-                                         nullptr);
-    if (nl < 0) {
-      h->err = "banded LU launch failed: " + std::string(cudaGetErrorString(cudaGetLastError()));
-      return MAFEM_ERR_CUDA;
-    }
-    h->launches += nl;
-    h->factored = true;
+    int rc = factor(h, nullptr, nullptr);
+    if (rc) return rc;
   }
   cudaEventRecord(h->ev[2], h->st);
   CK(cudaMemsetAsync(h->d_x, 0, n * sizeof(double), h->st));
@@ -552,8 +626,14 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   double prev = r0;
   for (int k = 0; k < h->max_refine; ++k) {
     CK(cudaMemcpyAsync(h->d_dx, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-    band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
-    band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
+    if (h->last_blk) {
+      blk_forward<double, float>((const float*)h->d_band, h->L, h->ndfp, h->d_perm, h->rmax, (const float*)h->d_rdiag,
+                                 h->d_dx, h->st);
+      blk_backward<double, float>((const float*)h->d_band, h->L, h->ndfp, (const float*)h->d_rdiag, h->d_dx, h->st);
+    } else {
+      band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
+      band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
+    }
     launch_axpy(n, h->d_dx, h->d_x, h->st);
     launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part,
                                 h->d_out + 3, h->st);
@@ -748,13 +828,23 @@ extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, maf
   CK(cudaEventRecord(a1, h->st));
   CK(cudaMemcpyAsync(h->d_x, h->d_r, h->nmdf * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
   CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
-  if (h->precision == MAFEM_PLAIN_FP64)
+  const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
+  if (h->use_blk) {
+    if (fp64)
+      blk_lu_factor<double>((double*)h->d_band, h->L, h->ndfp, h->d_blk_end, h->d_ipiv, h->d_perm, h->rmax,
+                            (double*)h->d_rdiag, h->d_info, h->d_x, h->st, nullptr, nullptr, ev.data());
+    else
+      blk_lu_factor<float>((float*)h->d_band, h->L, h->ndfp, h->d_blk_end, h->d_ipiv, h->d_perm, h->rmax,
+                           (float*)h->d_rdiag, h->d_info, nullptr, h->st, nullptr, nullptr, ev.data());
+  } else if (fp64) {
     band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, h->d_x,
                            h->apply_threads, h->apply_blocks, h->st, nullptr, nullptr, ev.data());
-  else
+  } else {
     band_lu_factor<float>((float*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, nullptr,
                           h->apply_threads, h->apply_blocks, h->st, nullptr, nullptr, ev.data());
+  }
   h->factored = true;
+  h->last_blk = h->use_blk;
   CK(cudaStreamSynchronize(h->st));
   float ms = 0;
   cudaEventElapsedTime(&ms, a0, a1);
@@ -772,6 +862,7 @@ extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, maf
   out->kl = h->L.kl;
   out->ku = h->L.ku;
   out->nb = h->L.nb;
+  out->ndfp = h->use_blk ? h->ndfp : -1;
   for (auto& e : ev) cudaEventDestroy(e);
   cudaEventDestroy(a0);
   cudaEventDestroy(a1);

@@ -129,4 +129,17 @@ template <class T, class V>
 void band_forward(const T* ab, const BandLayout& L, const int* perm_all, int rmax, V* b, cudaStream_t st);
 template <class T, class V>
 void band_backward(const T* ab, const BandLayout& L, V* y, cudaStream_t st);
+
+// node-block pivoted banded LU (band_lu_blk.cu)
+template <class T>
+cudaError_t blk_lu_setup(const BandLayout& L, int ndfp);
+template <class T>
+int blk_lu_factor(T* ab, const BandLayout& L, int ndfp, const int* blk_end, int* ipiv, int* perm_all, int rmax,
+                  T* rdiag, int* info, T* rhs, cudaStream_t st, cudaStream_t st2, cudaEvent_t* ev_pool,
+                  cudaEvent_t* prof);
+template <class V, class T>
+void blk_forward(const T* ab, const BandLayout& L, int ndfp, const int* perm_all, int rmax, const T* rdiag, V* b,
+                 cudaStream_t st);
+template <class V, class T>
+void blk_backward(const T* ab, const BandLayout& L, int ndfp, const T* rdiag, V* y, cudaStream_t st);
 }  // namespace mafem
