@@ -169,6 +169,7 @@ typedef struct mafem_kernel_times {
   int64_t n_panel, n_apply;   /* launches of each */
   int64_t n, kl, ku, nb;      /* factorised system */
   int64_t ndfp;               /* node-block pivoting: max block size - 1; -1 = full partial pivoting */
+  double flop_panel, flop_apply;  /* FLOPs of the factorisation's panel and trailing-update kernels */
 } mafem_kernel_times;
 /* Assemble and factor the resident state once, timing every LU launch with
  * CUDA events on the handle's stream (for roofline reporting). */

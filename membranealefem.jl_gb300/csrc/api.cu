@@ -97,8 +97,11 @@ struct mafem_handle {
   // (band_lu.cu) is the fallback for a block without a usable pivot
   bool use_blk = false;
   bool last_blk = false;  // which factorisation the band currently holds
-  int ndfp = 0;
+  BlkPlan blk;
   int* d_blk_end = nullptr;
+  int* d_flags = nullptr;  // per-panel completion flags of the cooperative back substitution
+  int epoch = 0;           // value the flags are set to by the next back substitution
+  int bwd_grid = 0;        // CTAs of the cooperative back substitution (0: single-CTA kernel)
   void* d_rdiag = nullptr;
   int64_t fallbacks = 0;
 };
@@ -389,8 +392,26 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     maxblk = std::max(maxblk, (int)(e - q));
     q = e;
   }
-  h->ndfp = maxblk - 1;
   UP(h->d_blk_end, blk_end);
+  {
+    const int wmax = precision == MAFEM_PLAIN_FP64 ? blk_lu_setup<double>(h->L) : blk_lu_setup<float>(h->L);
+    cudaGetLastError();
+    if (wmax && maxblk <= wmax && blk_plan(blk_end, wmax, (int)h->L.ku, h->blk)) {
+      UP(h->blk.d_ps, h->blk.ps);
+      h->blk.d_blk_end = h->d_blk_end;
+      h->use_blk = true;
+      AL(h->d_flags, (size_t)h->blk.npan());
+      cudaMemset(h->d_flags, 0, (size_t)h->blk.npan() * sizeof(int));
+      h->bwd_grid = precision == MAFEM_PLAIN_FP64 ? blk_backward_grid<double, double>() : blk_backward_grid<double, float>();
+      cudaGetLastError();
+      const size_t nev = (size_t)2 * h->blk.npan() + 2;
+      while (h->ev_pool.size() < nev) {
+        cudaEvent_t e = nullptr;
+        cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        h->ev_pool.push_back(e);
+      }
+    }
+  }
   double *d_xms, *d_cps;
   AL(d_xms, (size_t)numnp * 3);
   AL(d_cps, (size_t)numnp * ndf);
@@ -402,8 +423,9 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
   AL(h->d_part, 2048);
   AL(h->d_out, 16);
   AL(h->d_ipiv, n);
-  AL(h->d_perm, (size_t)h->npan * h->rmax);
-  AL(h->d_info, 4);
+  AL(h->d_perm, std::max((size_t)h->npan * h->rmax, (size_t)h->blk.npan() * kBlkW));
+  AL(h->d_info, 4);  // [0] zero-pivot column (1-based), [1] nonzero: a bounded device wait ran out
+  cudaMemset(h->d_info, 0, 4 * sizeof(int));
   const size_t band_elems = (size_t)h->L.ldb * n;
   if (precision == MAFEM_PLAIN_FP64) {
     double *kel, *band, *rd;
@@ -449,12 +471,6 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     set_global_error(std::string("kernel attribute setup: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
     mafem_destroy(hp.release());
     return MAFEM_ERR_CUDA;
-  }
-  if (h->L.kl >= h->ndfp && h->L.nb + h->ndfp <= 40) {
-    const cudaError_t e3 = precision == MAFEM_PLAIN_FP64 ? blk_lu_setup<double>(h->L, h->ndfp)
-                                                          : blk_lu_setup<float>(h->L, h->ndfp);
-    h->use_blk = (e3 == cudaSuccess);
-    cudaGetLastError();
   }
   *out = hp.release();
   return MAFEM_OK;
@@ -537,12 +553,10 @@ static int factor(mafem_handle* h, double* x, const double* rhs0) {
   const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
   CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
   if (h->use_blk) {
-    const int nl = fp64 ? blk_lu_factor<double>((double*)h->d_band, h->L, h->ndfp, h->d_blk_end, h->d_ipiv, h->d_perm,
-                                                h->rmax, (double*)h->d_rdiag, h->d_info, x, h->st, h->st2,
-                                                h->ev_pool.data(), nullptr)
-                        : blk_lu_factor<float>((float*)h->d_band, h->L, h->ndfp, h->d_blk_end, h->d_ipiv, h->d_perm,
-                                               h->rmax, (float*)h->d_rdiag, h->d_info, nullptr, h->st, h->st2,
-                                               h->ev_pool.data(), nullptr);
+    const int nl = fp64 ? blk_lu_factor<double>((double*)h->d_band, h->L, h->blk, h->d_perm, (double*)h->d_rdiag,
+                                                h->d_info, x, h->st, h->st2, h->ev_pool.data(), nullptr)
+                        : blk_lu_factor<float>((float*)h->d_band, h->L, h->blk, h->d_perm, (float*)h->d_rdiag,
+                                               h->d_info, nullptr, h->st, h->st2, h->ev_pool.data(), nullptr);
     h->launches += nl;
     CK(cudaGetLastError());
     int info = 0;
@@ -579,6 +593,38 @@ static int factor(mafem_handle* h, double* x, const double* rhs0) {
   return MAFEM_OK;
 }
 
+// Back substitution with the node-block factors, in place on y (device).
+template <class T>
+static void blk_back_solve(mafem_handle* h, double* y) {
+  if (h->bwd_grid > 0) {
+    ++h->epoch;
+    if (blk_backward<double, T>((const T*)h->d_band, h->L, h->blk, (const T*)h->d_rdiag, y, h->d_flags, h->epoch,
+                                h->d_info + 1, h->bwd_grid, h->st) == 0) {
+      h->launches += 1;
+      return;
+    }
+    cudaGetLastError();
+    h->bwd_grid = 0;  // cooperative launch refused: use the single-CTA kernel from now on
+  }
+  blk_backward_1cta<double, T>((const T*)h->d_band, h->L, h->blk, (const T*)h->d_rdiag, y, h->st);
+  h->launches += 1;
+}
+
+// info[0]: zero-pivot column, info[1]: a bounded device wait ran out (h_out + 5 holds both)
+static int check_info(mafem_handle* h) {
+  int info[2] = {0, 0};
+  std::memcpy(info, h->h_out + 5, sizeof info);
+  if (info[1]) {
+    h->err = "back substitution: a bounded wait for another CTA ran out";
+    return MAFEM_ERR_CUDA;
+  }
+  if (info[0]) {
+    h->err = "zero pivot in column " + std::to_string(info[0]);
+    return MAFEM_ZERO_PIVOT;
+  }
+  return MAFEM_OK;
+}
+
 // Solve K x = rhs (rhs in d_x on entry for the plain form; x in d_x on exit).
 // Factors the band if needed.  Returns the number of refinement sweeps in *sweeps.
 static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps) {
@@ -590,19 +636,20 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
       int rc = factor(h, h->d_x, rhs_dev);
       if (rc) return rc;
     } else if (h->last_blk) {
-      blk_forward<double, double>((const double*)h->d_band, h->L, h->ndfp, h->d_perm, h->rmax,
-                                  (const double*)h->d_rdiag, h->d_x, h->st);
+      blk_forward<double, double>((const double*)h->d_band, h->L, h->blk, h->d_perm, (const double*)h->d_rdiag,
+                                  h->d_x, h->st);
       h->launches += 1;
     } else {
       band_forward<double, double>((const double*)h->d_band, h->L, h->d_perm, h->rmax, h->d_x, h->st);
       h->launches += 1;
     }
     cudaEventRecord(h->ev[2], h->st);
-    if (h->last_blk)
-      blk_backward<double, double>((const double*)h->d_band, h->L, h->ndfp, (const double*)h->d_rdiag, h->d_x, h->st);
-    else
+    if (h->last_blk) {
+      blk_back_solve<double>(h, h->d_x);
+    } else {
       band_backward<double, double>((const double*)h->d_band, h->L, h->d_x, h->st);
-    h->launches += 1;
+      h->launches += 1;
+    }
     CK(cudaGetLastError());
     return MAFEM_OK;
   }
@@ -627,9 +674,9 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   for (int k = 0; k < h->max_refine; ++k) {
     CK(cudaMemcpyAsync(h->d_dx, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     if (h->last_blk) {
-      blk_forward<double, float>((const float*)h->d_band, h->L, h->ndfp, h->d_perm, h->rmax, (const float*)h->d_rdiag,
-                                 h->d_dx, h->st);
-      blk_backward<double, float>((const float*)h->d_band, h->L, h->ndfp, (const float*)h->d_rdiag, h->d_dx, h->st);
+      blk_forward<double, float>((const float*)h->d_band, h->L, h->blk, h->d_perm, (const float*)h->d_rdiag, h->d_dx,
+                                 h->st);
+      blk_back_solve<float>(h, h->d_dx);
     } else {
       band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
       band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
@@ -703,16 +750,10 @@ extern "C" int mafem_solve(mafem_handle* h, const double* r, double* du_out) {
   int rc = factor_and_solve(h, rhs, &sweeps);
   if (rc) return rc;
   CK(cudaMemcpyAsync(du_out, h->d_x, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   for (int64_t i = 0; i < n; ++i) du_out[i] = -du_out[i];
-  int info = 0;
-  std::memcpy(&info, h->h_out + 5, sizeof(int));
-  if (info) {
-    h->err = "zero pivot in column " + std::to_string(info);
-    return MAFEM_ZERO_PIVOT;
-  }
-  return MAFEM_OK;
+  return check_info(h);
 }
 
 extern "C" int mafem_predict(mafem_handle* h, double dt) {
@@ -744,7 +785,7 @@ extern "C" int mafem_time_step(mafem_handle* h, double time, double dt, mafem_st
     h->launches += 2;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
     cudaEventRecord(h->ev[4], h->st);
     CK(cudaStreamSynchronize(h->st));
     float ms_a = 0, ms_f = 0, ms_s = 0;
@@ -755,16 +796,13 @@ extern "C" int mafem_time_step(mafem_handle* h, double time, double dt, mafem_st
     S.ms_factor += ms_f;
     S.ms_solve += ms_s;
     S.refine_iters += sweeps;
-    int info = 0;
-    std::memcpy(&info, h->h_out + 5, sizeof(int));
     eps = h->h_out[0];
     S.eps[iter - 1] = eps;
     S.res_norm[iter - 1] = h->h_out[1];
     S.newton_iters = iter;
-    if (info) {
-      h->err = "zero pivot in column " + std::to_string(info);
+    if ((rc = check_info(h)) != MAFEM_OK) {
       if (stats) *stats = S;
-      return MAFEM_ZERO_PIVOT;
+      return rc;
     }
     if (h->h_out[2] != 0.0 || !std::isfinite(eps)) {
       h->err = "non-finite residual or Newton update";
@@ -812,13 +850,44 @@ extern "C" int64_t mafem_launch_count(const mafem_handle* h) { return h ? h->lau
 
 // Per-kernel device time of one assembly + factorisation of the resident
 // state (CUDA events on the handle's stream around every launch).
+// FLOPs of one factorisation as the kernels execute it (matrix columns only;
+// the fused right-hand side is not counted).
+static void lu_flops(const mafem_handle* h, double* fpanel, double* fapply) {
+  const int64_t n = h->nmdf, kl = h->L.kl, ku = h->L.ku;
+  double fp = 0, fa = 0;
+  if (h->use_blk) {
+    const BlkPlan& B = h->blk;
+    for (int p = 0; p < B.npan(); ++p) {
+      const int64_t j0 = B.ps[p], j1 = B.ps[p + 1], w = j1 - j0;
+      const int64_t R = std::min(n - j0, w + kl);
+      const int64_t ncol = std::min(n, j1 + B.kuf) - j1;
+      // per column: unit-lower solve w(w-1), U11 solve w^2, A21 y 2(R-w)w
+      fa += (double)ncol * (double)(w * (w - 1) + w * w + 2 * (R - w) * w);
+      for (int64_t k = 0; k < w; ++k) fp += (double)(w - k - 1) * (1 + 2 * (w - k - 1));
+    }
+  } else {
+    const int64_t nb = h->L.nb;
+    for (int64_t j0 = 0; j0 < n; j0 += nb) {
+      const int64_t w = std::min(nb, n - j0), R = std::min(n - j0, w + kl);
+      const int64_t ncol = std::min(n, j0 + w + kl + ku) - (j0 + w);
+      fa += (double)ncol * (double)(w * (w - 1) + 2 * (R - w) * w);
+      for (int64_t k = 0; k < w; ++k) {
+        const int64_t rows = std::min(R, k + kl + 1) - (k + 1);
+        fp += (double)rows * (1 + 2 * (w - k - 1));
+      }
+    }
+  }
+  *fpanel = fp;
+  *fapply = fa;
+}
+
 extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, mafem_kernel_times* out) {
   if (!h || !out) return MAFEM_ERR_ARG;
   std::memset(out, 0, sizeof *out);
   cudaEvent_t a0, a1;
   CK(cudaEventCreate(&a0));
   CK(cudaEventCreate(&a1));
-  const int64_t npan = h->npan;
+  const int64_t npan = h->use_blk ? h->blk.npan() : h->npan;
   std::vector<cudaEvent_t> ev((size_t)3 * npan);
   for (auto& e : ev) CK(cudaEventCreate(&e));
   CK(cudaStreamSynchronize(h->st));
@@ -831,11 +900,11 @@ extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, maf
   const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
   if (h->use_blk) {
     if (fp64)
-      blk_lu_factor<double>((double*)h->d_band, h->L, h->ndfp, h->d_blk_end, h->d_ipiv, h->d_perm, h->rmax,
-                            (double*)h->d_rdiag, h->d_info, h->d_x, h->st, nullptr, nullptr, ev.data());
+      blk_lu_factor<double>((double*)h->d_band, h->L, h->blk, h->d_perm, (double*)h->d_rdiag, h->d_info, h->d_x, h->st,
+                            nullptr, nullptr, ev.data());
     else
-      blk_lu_factor<float>((float*)h->d_band, h->L, h->ndfp, h->d_blk_end, h->d_ipiv, h->d_perm, h->rmax,
-                           (float*)h->d_rdiag, h->d_info, nullptr, h->st, nullptr, nullptr, ev.data());
+      blk_lu_factor<float>((float*)h->d_band, h->L, h->blk, h->d_perm, (float*)h->d_rdiag, h->d_info, nullptr, h->st,
+                           nullptr, nullptr, ev.data());
   } else if (fp64) {
     band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, h->d_x,
                            h->apply_threads, h->apply_blocks, h->st, nullptr, nullptr, ev.data());
@@ -862,7 +931,8 @@ extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, maf
   out->kl = h->L.kl;
   out->ku = h->L.ku;
   out->nb = h->L.nb;
-  out->ndfp = h->use_blk ? h->ndfp : -1;
+  out->ndfp = h->use_blk ? h->blk.ndfp : -1;
+  lu_flops(h, &out->flop_panel, &out->flop_apply);
   for (auto& e : ev) cudaEventDestroy(e);
   cudaEventDestroy(a0);
   cudaEventDestroy(a1);

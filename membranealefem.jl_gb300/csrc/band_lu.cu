@@ -44,9 +44,7 @@ BandLayout make_band_layout(int64_t n, int kl, int ku, int nb) {
   L.ku = ku;
   L.nb = nb;
   L.off = (int64_t)kl + ku + nb;
-  // + 8 rows below: the node-block pivoted panels reach kl + ndfp (ndfp <= 7)
-  // rows below their first column (band_lu_blk.cu)
-  int64_t rows = 2 * (int64_t)kl + ku + 2 * nb + 1 + 8;
+  int64_t rows = 2 * (int64_t)kl + ku + 2 * nb + 1;
   L.ldb = (rows + 3) / 4 * 4;  // 32-byte aligned columns (FP64) / 16-byte (FP32)
   return L;
 }

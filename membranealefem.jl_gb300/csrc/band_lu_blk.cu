@@ -3,29 +3,24 @@
 // The tangent is ordered node-major (Mesh.jl:276-284), so the unknowns of one
 // control point are consecutive: a "pivot block" of at most ndf rows.  Here the
 // pivot of column j is searched only among the rows of j's block that are not
-// yet eliminated (rows j .. blk_end[j]-1), instead of among all kl rows below
-// the diagonal as LAPACK's gbtrf does.  On the membrane tangents this is as
-// accurate as full partial pivoting (growth ~1e2, backward error ~1e-15,
-// forward error at the conditioning floor) and it changes the work and the
-// critical path on a GPU completely:
-//   * interchanges stay inside a block, so U fills only to ku + ndfp columns
-//     (ndfp = max block size - 1) instead of kl + ku: half the FP64 work of the
-//     trailing updates;
-//   * the pivot search is a warp shuffle over <= 8 rows -- no panel-wide
-//     reduction per column;
-//   * rows below the panel's diagonal block never take part in a pivot step,
-//     so their multipliers need not be formed: the trailing update applies
-//     L21 u = A21 (U11^-1 u) per column, with the raw panel rows A21.
-// A zero or non-finite pivot inside a block sets `info`; the caller then falls
-// back to the full partial-pivoting factorisation (band_lu.cu).
+// yet eliminated, instead of among all kl rows below the diagonal as LAPACK's
+// gbtrf does.  On the membrane tangents this is as accurate as full partial
+// pivoting (growth ~1e2, backward error ~1e-15, forward error at the
+// conditioning floor) and it changes the work and the critical path on a GPU:
+//   * panels are runs of whole blocks, so interchanges never leave a panel and
+//     U fills only to kuf = ku + ndfp columns (ndfp = largest block - 1)
+//     instead of kl + ku: half the FP64 work of the trailing updates;
+//   * the pivot search is one warp reduction over <= 8 rows;
+//   * rows below a panel never take part in its pivot steps, so their
+//     multipliers L21 = A21 U11^-1 are never formed: the trailing update and
+//     the forward substitution apply L21 u = A21 (U11^-1 u) with the raw A21.
+// A zero or non-finite pivot sets `info`; the caller then falls back to the
+// full partial-pivoting factorisation (band_lu.cu).
 //
-// Panel p covers columns [j0, j1), w = j1 - j0 <= nb, with
-//   diagonal block rows [j0, j0 + Rd), Rd = w + ndfp (it holds every row a
-//   pivot of the panel can come from), and all affected rows [j0, j0 + R),
-//   R = w + kl + ndfp.
-// After the panel kernel the band holds, in the panel's columns: L11 (strict
-// lower) and U11 (upper) in rows [j0, j1); explicit multipliers Lx in rows
-// [j1, j0+Rd); the raw A21 in rows [j0+Rd, j0+R).  rdiag[j] = 1 / U(j, j).
+// After panel p (columns [j0, j1), w = j1 - j0 <= 32) the band holds, in the
+// panel's columns, L11 (unit, strict lower) and U11 in rows [j0, j1) and the
+// untouched A21 in rows [j1, j0 + R), R = w + kl; rdiag[j] = 1 / U(j, j);
+// perm_all[p * kBlkW + i] = the panel row moved to position i.
 
 #include <cuda_runtime.h>
 
@@ -37,279 +32,375 @@
 namespace mafem {
 
 namespace {
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kPanelWarps = 8;
 __host__ __device__ __forceinline__ int64_t min64b(int64_t a, int64_t b) { return a < b ? a : b; }
 __device__ __forceinline__ int64_t bix(const BandLayout& L, int64_t i, int64_t j) { return j * L.ldb + L.off + i - j; }
-__device__ __forceinline__ unsigned long long akey(double v) {
-  unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
-  return b > 0x7ff0000000000000ULL ? 0ULL : b;  // NaN -> 0
+
+// pivot key: |v| ordered as an unsigned integer (top 32 bits of a double);
+// zero, subnormal, NaN and Inf map to 0 (no usable pivot)
+__device__ __forceinline__ unsigned pkey(double v) {
+  const unsigned hi = (unsigned)__double2hiint(v) & 0x7fffffffu;
+  return (hi >= 0x7ff00000u || hi < 0x00100000u) ? 0u : hi;
 }
-__device__ __forceinline__ unsigned long long akey(float v) {
-  unsigned b = (unsigned)__float_as_int(v) & 0x7fffffffu;
-  return b > 0x7f800000u ? 0ULL : (unsigned long long)b;
+__device__ __forceinline__ unsigned pkey(float v) {
+  const unsigned b = __float_as_uint(v) & 0x7fffffffu;
+  return b >= 0x7f800000u ? 0u : b;
 }
-// 1/x: FP32 seed + two Newton steps (GB300 issues FP64 slowly; a divide is a long sequence)
-__device__ __forceinline__ double rcp_fast(double x) {
-  const float xf = (float)x;
-  const float sf = __frcp_rn(xf);
-  if (xf == 0.0f || !isfinite(sf) || sf == 0.0f) return 1.0 / x;
-  double r = (double)sf;
-  r = r * fma(-x, r, 2.0);
-  r = r * fma(-x, r, 2.0);
-  return r;
+
+// Reciprocal of a pivot in two parts, 1/d = r0 (1 + t): r0 is the hardware's
+// approximate FP64 reciprocal (rcp.approx.ftz.f64, a special-function-unit
+// op; |1 - d r0| < 2^-19.9 measured over 2^26 seeded inputs on GB300),
+// e = 1 - d r0 and t = e + e^2, so r0 (1 + t) = (1 - e^3) / d with
+// |e^3| < 2^-59 -- two Newton-Raphson corrections folded into one factor.
+// x / d is then fma(x r0, t, x r0).  On GB300 every FP64 instruction (and
+// every f64<->f32 conversion) occupies a sub-partition's FP64 pipe for ~64
+// cycles, so this takes three pipe slots where a divide takes a long sequence.
+// Pivots are normal numbers here (pkey rejects the rest), which the ftz form
+// requires.
+__device__ __forceinline__ void recip2(double d, double& r0, double& t) {
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r0) : "d"(d));
+  const double e = fma(-d, r0, 1.0);
+  t = fma(e, e, e);
 }
-__device__ __forceinline__ float rcp_fast(float x) { return __frcp_rn(x); }
-constexpr int kMaxRd = 40;  // nb (32) + ndfp (<= 7), rounded up
+__device__ __forceinline__ void recip2(float d, float& r0, float& t) {
+  r0 = __frcp_rn(d);
+  t = 0.0f;
+}
+template <class T>
+__device__ __forceinline__ T mul_recip(T x, T r0, T t) {
+  const T a = x * r0;
+  return fma(a, t, a);
+}
+
+// asynchronous global -> shared copies (sm_80+ cp.async): every copy of a
+// staging loop is in flight at once instead of one L2 round trip per element
+template <class T>
+__device__ __forceinline__ void cp_async(T* smem, const T* gmem) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(s), "l"(gmem), "n"(sizeof(T)) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__device__ __forceinline__ void bar_sync_n(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void bar_arrive_n(int id, int n) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
 }  // namespace
 
-// ---------------------------------------------------------------------------
-// Diagonal-block factorisation of one panel: one CTA, block in shared memory.
+// One pivot step of the panel, run by the warp that owns column k: pick the
+// pivot among the block's rows not yet eliminated, form the multipliers,
+// publish them (shared memory + named-barrier arrive) and record the pivot.
+// Returns the column's final value for this lane: the multiplier below the
+// pivot, the U entry (or the pivot itself) otherwise.
 template <class T>
-__global__ void __launch_bounds__(128) blk_panel_kernel(T* __restrict__ ab, BandLayout L, int ndfp, int64_t j0,
-                                                        const int* __restrict__ blk_end, int* __restrict__ ipiv,
-                                                        int* __restrict__ perm, T* __restrict__ rdiag,
-                                                        int* __restrict__ info) {
-  __shared__ T D[32 * kMaxRd];  // column-major [c][r], stride Rd
-  __shared__ int s_perm[kMaxRd];
-  __shared__ int s_p;
-  __shared__ T s_rinv;
-  const int w = (int)min64b(L.nb, L.n - j0);
-  const int Rd = (int)min64b(L.n - j0, (int64_t)w + ndfp);
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
-  for (int k = tid; k < w * Rd; k += nt) {
-    const int c = k / Rd, r = k - c * Rd;
-    D[c * Rd + r] = ab[bix(L, j0 + r, j0 + c)];
+__device__ __forceinline__ T blk_pivot_step(int k, T col, int w, int lane, int bend, unsigned E, int64_t j0,
+                                            T (*s_l)[32], int* s_p, int* perm, T* rdiag, int* info, int& op,
+                                            T& ol) {
+  const int bk = __shfl_sync(kFull, bend, k);  // the block of position k ends at row bk
+  const bool cand = lane < bk && !((E >> lane) & 1u);
+  const unsigned key = cand ? pkey(col) : 0u;
+  const unsigned mx = __reduce_max_sync(kFull, key);
+  const unsigned bal = __ballot_sync(kFull, cand && key == mx);
+  const int p = __ffs(bal) - 1;  // the candidates are never empty
+  const T piv = __shfl_sync(kFull, col, p);
+  T r0, t;
+  recip2(piv, r0, t);
+  const bool act = lane < w && lane != p && !((E >> lane) & 1u);
+  const T l = act ? mul_recip(col, r0, t) : T(0);
+  s_l[k & 1][lane] = l;
+  if (lane == 0) s_p[k & 1] = p;
+  bar_arrive_n(1 + (k & 1), 32 * kPanelWarps);
+  if (lane == 0) {
+    perm[k] = p;
+    rdiag[j0 + k] = fma(r0, t, r0);
+    if (mx == 0u) atomicCAS(info, 0, (int)(j0 + k + 1));
   }
-  for (int r = tid; r < Rd; r += nt) s_perm[r] = r;
+  op = p;
+  ol = l;
+  return act ? l : col;
+}
+
+// ---------------------------------------------------------------------------
+// Panel factorisation: one CTA of 8 warps (two per sub-partition, so one
+// warp's FP64 issue stalls overlap the other's work), the w x w diagonal block
+// in registers.  Warp q owns columns q, q + 8, ...; lane i holds panel row i (its
+// original position).  Rows are never moved during the factorisation: a row
+// is marked eliminated at the step that picks it and written to that position
+// at the end.  Step k: the owner of column k finds the pivot (largest |v| among
+// the block's rows not yet eliminated), forms the multipliers of column k,
+// publishes the pivot row index and the multipliers in shared memory and
+// arrives at a named barrier; the other warps wait on it, and every warp
+// updates its own columns.  The owner of column k + 1 updates that column
+// first and publishes step k + 1 before finishing its other columns, so the
+// next pivot step overlaps the rest of step k.  Named barriers 1 and 2
+// alternate between steps; the shared buffers are double-buffered by the same
+// parity.
+template <class T>
+__global__ void __launch_bounds__(32 * kPanelWarps) blk_panel_kernel(T* __restrict__ ab, BandLayout L, int64_t j0, int w,
+                                                        const int* __restrict__ blk_end, int* __restrict__ perm,
+                                                        T* __restrict__ rdiag, int* __restrict__ info) {
+  __shared__ T s_l[2][32];
+  __shared__ int s_p[2];
+  const int tid = threadIdx.x, lane = tid & 31, q = tid >> 5;
+  const int bend = lane < w ? (int)(blk_end[j0 + lane] - j0) : 0;
+  constexpr int NW = kPanelWarps, NCOL = 32 / kPanelWarps;
+  T v[NCOL];
+#pragma unroll
+  for (int m = 0; m < NCOL; ++m) {
+    const int c = q + NW * m;
+    v[m] = (c < w && lane < w) ? ab[bix(L, j0 + lane, j0 + c)] : T(0);
+  }
+  unsigned E = 0u;  // eliminated rows
+  int mypos = 0;
+  int op = 0;
+  T ol = T(0);  // the step this warp published last: pivot row, multiplier of this lane's row
+
+  if (q == 0) v[0] = blk_pivot_step(0, v[0], w, lane, bend, E, j0, s_l, s_p, perm, rdiag, info, op, ol);
+  for (int k = 0; k < w; ++k) {
+    int p;
+    T l;
+    if (q == k % NW) {
+      p = op;
+      l = ol;
+    } else {
+      bar_sync_n(1 + (k & 1), 32 * NW);
+      p = s_p[k & 1];
+      l = s_l[k & 1][lane];
+    }
+    E |= 1u << p;
+    if (lane == p) mypos = k;
+#pragma unroll
+    for (int m = 0; m < NCOL; ++m) {
+      const int c = q + NW * m;
+      if (c > k && c < w) {  // warp-uniform
+        const T u = __shfl_sync(kFull, v[m], p);
+        v[m] = fma(-l, u, v[m]);  // l == 0 on eliminated rows
+        if (c == k + 1) v[m] = blk_pivot_step(k + 1, v[m], w, lane, bend, E, j0, s_l, s_p, perm, rdiag, info, op, ol);
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < NCOL; ++m) {
+    const int c = q + NW * m;
+    if (c < w && lane < w) ab[bix(L, j0 + mypos, j0 + c)] = v[m];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Trailing update of a panel: four columns per CTA, each column run by a pair
+// of warps (warps q and q + 4 share a sub-partition's FP64 pipe, so one warp's
+// issue stalls overlap the other's work).  Per column segment
+// s = A(j0 .. j0+R-1, c), rows [0, w) permuted:
+//   u = L11^-1 s[0:w]   (kept as U12),   y = U11^-1 u,   s[w:R] -= A21 y.
+// Warp q stages the column and runs the two triangular solves, then releases
+// warp q + 4 (named barrier 1 + q); the two split the 32-row chunks of the
+// A21 y update (NCH chunks each per pass).  Before warp q overwrites the
+// column buffer for its next column it waits until warp q + 4 is done with
+// the previous one (named barrier 5 + q).  The panel columns (L11\U11 and
+// A21) are staged in shared memory once per CTA.
+template <class T, int NCH>
+__global__ void __launch_bounds__(256) blk_apply_kernel(T* __restrict__ ab, BandLayout L, int64_t j0, int w,
+                                                        const int* __restrict__ perm, const T* __restrict__ rdiag,
+                                                        T* __restrict__ rhs, int64_t c0, int ncol) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int R = (int)min64b(L.n - j0, (int64_t)w + L.kl);
+  T* Lp = reinterpret_cast<T*>(smem_raw);  // [w][R] + 64 NCH padding (chunk reads past R)
+  T* S = Lp + (size_t)w * R + 64 * NCH;    // [4][R]
+  T* Y = S + (size_t)4 * R;                // [4][32]
+  T* rd = Y + 128;                         // [32]
+  int* sp = reinterpret_cast<int*>(rd + 32);  // [32]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int slot = warp & 3, half = warp >> 2;
+  const int ntot = ncol + (rhs ? 1 : 0);
+  if ((int)blockIdx.x * 4 >= ntot) return;
+  for (int c = 0; c < w; ++c) {
+    const T* src = ab + bix(L, j0, j0 + c);  // A(j0 + r, j0 + c) = src[r]
+    for (int r = tid; r < R; r += 256) cp_async(Lp + (size_t)c * R + r, src + r);
+  }
+  if (tid < w) {
+    rd[tid] = rdiag[j0 + tid];
+    sp[tid] = perm[tid];
+  }
+  cp_async_wait_all();
   __syncthreads();
-  for (int jj = 0; jj < w; ++jj) {
-    if (tid < 32) {
-      const int bend = min(Rd, blk_end[j0 + jj] - (int)j0);  // rows jj .. bend-1 are candidates
-      unsigned long long k = 0ULL;
-      int idx = 0x7fffffff;
-      if (jj + lane < bend) {
-        k = akey(D[jj * Rd + jj + lane]);
-        idx = jj + lane;
-      }
-      for (int o = 4; o > 0; o >>= 1) {  // blocks have <= 8 rows
-        const unsigned long long ok = __shfl_down_sync(0xffffffffu, k, o);
-        const int oi = __shfl_down_sync(0xffffffffu, idx, o);
-        if (ok > k || (ok == k && oi < idx)) { k = ok; idx = oi; }
-      }
-      k = __shfl_sync(0xffffffffu, k, 0);
-      idx = __shfl_sync(0xffffffffu, idx, 0);
-      const int p = (k != 0ULL) ? idx : jj;  // zero / NaN block: keep the diagonal, flag it
-      if (p != jj && lane < w) {
-        const T t = D[lane * Rd + jj];
-        D[lane * Rd + jj] = D[lane * Rd + p];
-        D[lane * Rd + p] = t;
-      }
+  T* s = S + (size_t)slot * R;
+  T* yw = Y + slot * 32;
+  for (int cc = blockIdx.x * 4 + slot; cc < ntot; cc += gridDim.x * 4) {
+    const bool is_rhs = cc == ncol;
+    const bool more = cc + (int)gridDim.x * 4 < ntot;
+    T* dst = is_rhs ? rhs + j0 : ab + bix(L, j0, c0 + cc);  // row j0 + r of the column = dst[r]
+    if (half == 0) {
+      if (cc != (int)blockIdx.x * 4 + slot) bar_sync_n(5 + slot, 64);  // partner done with the previous column
+      for (int r = lane; r < R; r += 32) cp_async(s + r, dst + (r < w ? sp[r] : r));
+      cp_async_wait_all();
       __syncwarp();
-      if (lane == 0) {
-        if (p != jj) {
-          const int t = s_perm[jj];
-          s_perm[jj] = s_perm[p];
-          s_perm[p] = t;
-        }
-        const T piv = D[jj * Rd + jj];
-        const T rv = (k != 0ULL) ? rcp_fast(piv) : T(0);
-        s_rinv = rv;
-        s_p = p;
-        ipiv[j0 + jj] = (int)(j0 + p);
-        rdiag[j0 + jj] = rv;
-        if (k == 0ULL) atomicCAS(info, 0, (int)(j0 + jj + 1));
+      T x = lane < w ? s[lane] : T(0);
+      for (int k = 0; k < w; ++k) {
+        const T xk = __shfl_sync(kFull, x, k);
+        if (lane > k && lane < w) x -= Lp[k * R + lane] * xk;
+      }
+      if (lane < w) dst[lane] = x;  // U12
+      T v = x;
+      for (int k = w - 1; k >= 0; --k) {
+        T yk = lane == k ? v * rd[k] : T(0);
+        yk = __shfl_sync(kFull, yk, k);
+        if (lane == k) v = yk;
+        if (lane < k) v -= Lp[k * R + lane] * yk;
+      }
+      yw[lane] = v;
+      bar_arrive_n(1 + slot, 64);
+    } else {
+      bar_sync_n(1 + slot, 64);
+    }
+    for (int base = w; base < R; base += 64 * NCH) {
+      const int hb = base + half * 32 * NCH;  // this warp's first row
+      T acc[NCH];
+#pragma unroll
+      for (int j = 0; j < NCH; ++j) acc[j] = s[min(hb + 32 * j + lane, R - 1)];
+      for (int k = 0; k < w; ++k) {
+        const T yk = yw[k];
+        const T* lk = Lp + (size_t)k * R + hb + lane;
+#pragma unroll
+        for (int j = 0; j < NCH; ++j)
+          if (hb + 32 * j < R) acc[j] = fma(-lk[32 * j], yk, acc[j]);  // warp-uniform guard
+      }
+#pragma unroll
+      for (int j = 0; j < NCH; ++j) {
+        const int r = hb + 32 * j + lane;
+        if (r < R) dst[r] = acc[j];
       }
     }
-    __syncthreads();
-    const T rinv = s_rinv;
-    for (int r = jj + 1 + tid; r < Rd; r += nt) D[jj * Rd + r] *= rinv;
-    __syncthreads();
-    const int nr = Rd - jj - 1, ncl = w - jj - 1;
-    for (int k = tid; k < nr * ncl; k += nt) {
-      const int c = jj + 1 + k / nr, r = jj + 1 + k % nr;
-      D[c * Rd + r] -= D[jj * Rd + r] * D[c * Rd + jj];
-    }
-    __syncthreads();
-  }
-  for (int k = tid; k < w * Rd; k += nt) {
-    const int c = k / Rd, r = k - c * Rd;
-    ab[bix(L, j0 + r, j0 + c)] = D[c * Rd + r];
-  }
-  for (int r = tid; r < Rd; r += nt) perm[r] = s_perm[r];
-}
-
-// ---------------------------------------------------------------------------
-// Trailing update of panel p: one warp per column c in j1 + [cb, ce) (plus the
-// right-hand side if given).  For the column segment s = A(j0 .. j0+R-1, c):
-//   permute rows [0, Rd); solve L11 (unit lower) on rows [0, w) -> u (U12);
-//   y = U11^-1 u (back substitution with rdiag);
-//   rows [w, Rd) -= Lx u;  rows [Rd, R) -= A21 y.
-// NW warps per CTA; the panel columns are staged in shared memory once per CTA.
-template <class T, int NW>
-__global__ void __launch_bounds__(NW * 32) blk_apply_kernel(T* __restrict__ ab, BandLayout L, int ndfp, int64_t j0,
-                                                            const int* __restrict__ perm,
-                                                            const T* __restrict__ rdiag, T* __restrict__ rhs, int cb,
-                                                            int ce) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int w = (int)min64b(L.nb, L.n - j0);
-  const int Rd = (int)min64b(L.n - j0, (int64_t)w + ndfp);
-  const int R = (int)min64b(L.n - j0, (int64_t)w + L.kl + ndfp);
-  const int64_t j1 = j0 + w;
-  const int ncol = (ce - cb) + (rhs ? 1 : 0);
-  T* Lp = reinterpret_cast<T*>(smem_raw);      // [w][R]
-  T* seg = Lp + (size_t)w * R;                 // [NW][R]
-  T* yb = seg + (size_t)NW * R;                // [NW][32]
-  T* rd = yb + NW * 32;                        // [32]
-  int* sperm = reinterpret_cast<int*>(rd + 32);  // [kMaxRd]
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (int k = tid; k < w * R; k += nt) {
-    const int c = k / R, r = k - c * R;
-    Lp[k] = ab[bix(L, j0 + r, j0 + c)];
-  }
-  for (int k = tid; k < w; k += nt) rd[k] = rdiag[j0 + k];
-  for (int r = tid; r < Rd; r += nt) sperm[r] = perm[r];
-  __syncthreads();
-  const int warp = tid >> 5, lane = tid & 31;
-  T* s = seg + (size_t)warp * R;
-  T* y = yb + warp * 32;
-  for (int cc = blockIdx.x * NW + warp; cc < ncol; cc += gridDim.x * NW) {
-    const bool is_rhs = rhs && cc == ncol - 1;
-    const int64_t c = j1 + cb + cc;
-    if (is_rhs) {
-      for (int r = lane; r < R; r += 32) s[r] = rhs[j0 + (r < Rd ? sperm[r] : r)];
-    } else {
-      for (int r = lane; r < R; r += 32) s[r] = ab[bix(L, j0 + (r < Rd ? sperm[r] : r), c)];
-    }
-    __syncwarp();
-    // u = L11^-1 s[0:w]  (lane k owns row k)
-    T x = lane < w ? s[lane] : T(0);
-    for (int k = 0; k < w; ++k) {
-      const T xk = __shfl_sync(0xffffffffu, x, k);
-      if (lane > k && lane < w) x -= Lp[k * R + lane] * xk;
-    }
-    if (lane < w) s[lane] = x;
-    // y = U11^-1 u
-    T v = x;
-    for (int k = w - 1; k >= 0; --k) {
-      T yk = lane == k ? v * rd[k] : T(0);
-      yk = __shfl_sync(0xffffffffu, yk, k);
-      if (lane == k) v = yk;
-      if (lane < k) v -= Lp[k * R + lane] * yk;
-    }
-    if (lane < w) y[lane] = v;
-    __syncwarp();
-    for (int r = w + lane; r < R; r += 32) {
-      const T* coef = r < Rd ? s : y;
-      T acc = s[r];
-#pragma unroll 8
-      for (int k = 0; k < w; ++k) acc -= Lp[k * R + r] * coef[k];
-      s[r] = acc;
-    }
-    __syncwarp();
-    if (is_rhs) {
-      for (int r = lane; r < R; r += 32) rhs[j0 + r] = s[r];
-    } else {
-      for (int r = lane; r < R; r += 32) ab[bix(L, j0 + r, c)] = s[r];
-    }
-    __syncwarp();
+    if (half == 1 && more) bar_arrive_n(5 + slot, 64);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Critical-path variant: one 4-warp CTA per column of the next panel.  Warp 0
-// runs the two triangular solves; all four warps share the row update, so the
-// column's FP64 work uses the SM's four sub-partitions.
-template <class T>
-__global__ void __launch_bounds__(128) blk_apply_col_kernel(T* __restrict__ ab, BandLayout L, int ndfp, int64_t j0,
+// Critical-path variant for the next panel's columns: one CTA per column.
+// Warp 0 runs the triangular solves; the four warps share the A21 y update,
+// NR rows per thread, reading A21 straight from the band (L2-resident).
+template <class T, int NR>
+__global__ void __launch_bounds__(128) blk_apply_col_kernel(T* __restrict__ ab, BandLayout L, int64_t j0, int w,
                                                             const int* __restrict__ perm,
-                                                            const T* __restrict__ rdiag, int cb) {
+                                                            const T* __restrict__ rdiag, int64_t c0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int w = (int)min64b(L.nb, L.n - j0);
-  const int Rd = (int)min64b(L.n - j0, (int64_t)w + ndfp);
-  const int R = (int)min64b(L.n - j0, (int64_t)w + L.kl + ndfp);
-  const int64_t c = j0 + w + cb + blockIdx.x;
+  const int R = (int)min64b(L.n - j0, (int64_t)w + L.kl);
+  const int64_t c = c0 + blockIdx.x;
   T* s = reinterpret_cast<T*>(smem_raw);  // [R]
-  __shared__ T T11[32][33];               // L11 below, U11 above the diagonal
+  __shared__ T T11[32][33];               // L11 below, U11 on and above the diagonal (transposed: [col][row])
   __shared__ T y[32];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
-  for (int r = tid; r < R; r += nt) s[r] = ab[bix(L, j0 + (r < Rd ? perm[r] : r), c)];
-  for (int k = tid; k < w * w; k += nt) {
+  __shared__ T rd[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid < w) rd[tid] = rdiag[j0 + tid];
+  for (int r = tid; r < R; r += 128) s[r] = ab[bix(L, j0 + (r < w ? perm[r] : r), c)];
+  for (int k = tid; k < w * w; k += 128) {
     const int cc = k / w, i = k - cc * w;
     T11[cc][i] = ab[bix(L, j0 + i, j0 + cc)];
   }
   __syncthreads();
-  if (tid < 32) {
+  if (warp == 0) {
     T x = lane < w ? s[lane] : T(0);
     for (int k = 0; k < w; ++k) {
-      const T xk = __shfl_sync(0xffffffffu, x, k);
+      const T xk = __shfl_sync(kFull, x, k);
       if (lane > k && lane < w) x -= T11[k][lane] * xk;
     }
     if (lane < w) s[lane] = x;
     T v = x;
     for (int k = w - 1; k >= 0; --k) {
-      T yk = lane == k ? v * rdiag[j0 + k] : T(0);
-      yk = __shfl_sync(0xffffffffu, yk, k);
+      T yk = lane == k ? v * rd[k] : T(0);
+      yk = __shfl_sync(kFull, yk, k);
       if (lane == k) v = yk;
       if (lane < k) v -= T11[k][lane] * yk;
     }
-    if (lane < w) y[lane] = v;
+    y[lane] = lane < w ? v : T(0);
   }
   __syncthreads();
-  for (int r = w + tid; r < R; r += nt) {
-    const T* coef = r < Rd ? s : y;
-    T acc = s[r];
-#pragma unroll 8
-    for (int k = 0; k < w; ++k) acc -= ab[bix(L, j0 + r, j0 + k)] * coef[k];
-    s[r] = acc;
+  for (int base = w; base < R; base += 128 * NR) {
+    T acc[NR];
+    int ri[NR];
+#pragma unroll
+    for (int i = 0; i < NR; ++i) {
+      ri[i] = min(base + 128 * i + tid, R - 1);
+      acc[i] = s[ri[i]];
+    }
+    const int wrow = base + warp * 32;
+    const T* col0 = ab + bix(L, j0, j0);  // A(j0 + r, j0 + k) = col0[k * (ldb - 1) + r]
+    for (int k0 = 0; k0 < w; k0 += 8) {
+      T a[8][NR];  // eight columns of A21 in flight per thread
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        const T* col = col0 + (int64_t)min(k0 + kk, w - 1) * (L.ldb - 1);
+#pragma unroll
+        for (int i = 0; i < NR; ++i) a[kk][i] = (wrow + 128 * i < R) ? col[ri[i]] : T(0);
+      }
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) {
+        if (k0 + kk < w) {
+          const T yk = y[k0 + kk];
+#pragma unroll
+          for (int i = 0; i < NR; ++i)
+            if (wrow + 128 * i < R) acc[i] = fma(-a[kk][i], yk, acc[i]);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < NR; ++i) {
+      const int r = base + 128 * i + tid;
+      if (r < R) ab[bix(L, j0 + r, c)] = acc[i];
+    }
   }
-  __syncthreads();
-  for (int r = tid; r < R; r += nt) ab[bix(L, j0 + r, c)] = s[r];
+  for (int r = tid; r < w; r += 128) ab[bix(L, j0 + r, c)] = s[r];
 }
 
 // ---------------------------------------------------------------------------
 // Forward substitution with the stored panels, one CTA (re-solves and the
 // refinement sweeps of the FP32 form).
 template <class T, class V>
-__global__ void __launch_bounds__(1024) blk_forward_kernel(const T* __restrict__ ab, BandLayout L, int ndfp,
-                                                           const int* __restrict__ perm_all, int rmax,
+__global__ void __launch_bounds__(1024) blk_forward_kernel(const T* __restrict__ ab, BandLayout L,
+                                                           const int* __restrict__ ps, int npan,
+                                                           const int* __restrict__ perm_all,
                                                            const T* __restrict__ rdiag, V* __restrict__ b) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* s = reinterpret_cast<V*>(smem_raw);  // [R]
   __shared__ V Ls[32][33];
   __shared__ V y[32];
+  __shared__ V rd[32];
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int64_t j0 = 0, pnl = 0; j0 < L.n; j0 += L.nb, ++pnl) {
-    const int w = (int)min64b(L.nb, L.n - j0);
-    const int Rd = (int)min64b(L.n - j0, (int64_t)w + ndfp);
-    const int R = (int)min64b(L.n - j0, (int64_t)w + L.kl + ndfp);
-    const int* pm = perm_all + pnl * rmax;
-    for (int r = tid; r < R; r += nt) s[r] = b[j0 + (r < Rd ? pm[r] : r)];
+  for (int pnl = 0; pnl < npan; ++pnl) {
+    const int64_t j0 = ps[pnl];
+    const int w = ps[pnl + 1] - ps[pnl];
+    const int R = (int)min64b(L.n - j0, (int64_t)w + L.kl);
+    const int* pm = perm_all + (size_t)pnl * kBlkW;
+    for (int r = tid; r < R; r += nt) s[r] = b[j0 + (r < w ? pm[r] : r)];
     for (int k = tid; k < w * w; k += nt) {
       const int c = k / w, i = k - c * w;
-      Ls[c][i] = V(ab[bix(L, j0 + i, j0 + c)]);  // L11 below, U11 on and above the diagonal
+      Ls[c][i] = V(ab[bix(L, j0 + i, j0 + c)]);
     }
+    if (tid < w) rd[tid] = V(rdiag[j0 + tid]);
     __syncthreads();
     if (tid < 32) {
       V x = tid < w ? s[tid] : V(0);
       for (int k = 0; k < w; ++k) {
-        const V xk = __shfl_sync(0xffffffffu, x, k);
+        const V xk = __shfl_sync(kFull, x, k);
         if (tid > k && tid < w) x -= Ls[k][tid] * xk;
       }
       if (tid < w) s[tid] = x;
       V v = x;
       for (int k = w - 1; k >= 0; --k) {
-        V yk = tid == k ? v * V(rdiag[j0 + k]) : V(0);
-        yk = __shfl_sync(0xffffffffu, yk, k);
+        V yk = tid == k ? v * rd[k] : V(0);
+        yk = __shfl_sync(kFull, yk, k);
         if (tid == k) v = yk;
         if (tid < k) v -= Ls[k][tid] * yk;
       }
-      if (tid < w) y[tid] = v;
+      y[tid] = tid < w ? v : V(0);
     }
     __syncthreads();
     for (int r = w + tid; r < R; r += nt) {
-      const V* coef = r < Rd ? s : y;
       V acc = s[r];
+      const T* row = ab + bix(L, j0 + r, j0);  // A(j0 + r, j0 + k) = row[k * (ldb - 1)]
 #pragma unroll 8
-      for (int k = 0; k < w; ++k) acc -= V(ab[bix(L, j0 + r, j0 + k)]) * coef[k];
+      for (int k = 0; k < w; ++k) acc -= V(row[(int64_t)k * (L.ldb - 1)]) * y[k];
       s[r] = acc;
     }
     __syncthreads();
@@ -318,19 +409,19 @@ __global__ void __launch_bounds__(1024) blk_forward_kernel(const T* __restrict__
   }
 }
 
-// Back substitution U x = y, one CTA, panels in reverse; U has ku + ndfp
+// Back substitution U x = y, one CTA, panels in reverse; U has kuf
 // super-diagonals and its diagonal reciprocals are in rdiag.
 template <class T, class V>
 __global__ void __launch_bounds__(1024) blk_backward_kernel(const T* __restrict__ ab, BandLayout L, int kuf,
+                                                            const int* __restrict__ ps, int npan,
                                                             const T* __restrict__ rdiag, V* __restrict__ y) {
   __shared__ V part[32][33];
   __shared__ V Us[32][33];
   __shared__ V xs[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-  const int64_t npan = (L.n + L.nb - 1) / L.nb;
-  for (int64_t pnl = npan - 1; pnl >= 0; --pnl) {
-    const int64_t j0 = pnl * L.nb;
-    const int w = (int)min64b(L.nb, L.n - j0);
+  for (int pnl = npan - 1; pnl >= 0; --pnl) {
+    const int64_t j0 = ps[pnl];
+    const int w = ps[pnl + 1] - ps[pnl];
     const int64_t j1 = j0 + w;
     const int64_t jend = min64b(L.n, j1 + kuf);
     for (int k = tid; k < w * w; k += blockDim.x) {
@@ -360,7 +451,7 @@ __global__ void __launch_bounds__(1024) blk_backward_kernel(const T* __restrict_
       V v = lane < w ? y[j0 + lane] - sum : V(0);
       for (int k = w - 1; k >= 0; --k) {
         V xk = lane == k ? v * Us[k][k] : V(0);  // Us[k][k] holds 1 / U(k, k)
-        xk = __shfl_sync(0xffffffffu, xk, k);
+        xk = __shfl_sync(kFull, xk, k);
         if (lane == k) v = xk;
         if (lane < k) v -= Us[k][lane] * xk;
       }
@@ -373,73 +464,190 @@ __global__ void __launch_bounds__(1024) blk_backward_kernel(const T* __restrict_
 }
 
 // ---------------------------------------------------------------------------
-// host drivers
-template <class T>
-static size_t blk_apply_smem(const BandLayout& L, int ndfp, int nw) {
-  const size_t R = (size_t)L.nb + L.kl + ndfp;
-  return R * L.nb * sizeof(T) + (size_t)nw * R * sizeof(T) + (size_t)nw * 32 * sizeof(T) + 32 * sizeof(T) +
-         kMaxRd * sizeof(int);
+// Back substitution on many SMs: one cooperative launch, panel q handled by
+// CTA (npan - 1 - q) mod gridDim.x.  A CTA accumulates U(q rows, c) x(c) over
+// the columns of the panels above it as their flags appear (most are done
+// long before it needs them), then solves its U11 triangle and publishes
+// x(q) with a release store of the flag.  Flags hold the epoch of the solve
+// that set them, so they never need clearing.  Waits are bounded: after
+// kSpinLimit polls the kernel records MAFEM status in *err and every CTA
+// returns (no GPU hang; the host reports the error).
+constexpr int kSpinLimit = 1 << 22;
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
-static size_t blk_fwd_smem(const BandLayout& L, int ndfp, size_t vsize) {
-  return ((size_t)L.nb + L.kl + ndfp) * vsize;
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// thread 0 waits for flags[p] == epoch; returns false (all threads) on timeout / abort
+__device__ __forceinline__ bool wait_flag(const int* flags, int p, int epoch, int* err, int* s_ok) {
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    for (int it = 0; ld_acquire(flags + p) != epoch; ++it) {
+      if (it > kSpinLimit || *(volatile int*)err) {
+        atomicCAS(err, 0, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok != 0;
+}
+
+template <class T, class V>
+__global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restrict__ ab, BandLayout L, int kuf,
+                                                                const int* __restrict__ ps, int npan,
+                                                                const T* __restrict__ rdiag, V* y, int* flags,
+                                                                int epoch, int* err) {
+  __shared__ V part[8][33];
+  __shared__ V Us[32][33];
+  __shared__ int s_ok;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int q = npan - 1 - (int)blockIdx.x; q >= 0; q -= gridDim.x) {
+    const int64_t j0 = ps[q], j1 = ps[q + 1];
+    const int w = (int)(j1 - j0);
+    const int64_t jend = min64b(L.n, j1 + kuf);
+    for (int k = tid; k < w * w; k += 256) {
+      const int c = k / w, i = k - c * w;
+      Us[c][i] = i < c ? V(ab[bix(L, j0 + i, j0 + c)]) : (i == c ? V(rdiag[j0 + c]) : V(0));
+    }
+    int pl = q + 1;  // last panel with columns in [j1, jend)
+    while (pl + 1 < npan && ps[pl + 1] < jend) ++pl;
+    V acc = V(0);
+    for (int p = (j1 < jend) ? pl : q; p > q; --p) {
+      if (!wait_flag(flags, p, epoch, err, &s_ok)) return;
+      const int64_t cb = ps[p], ce = min64b(ps[p + 1], jend);
+      if (lane < w)
+        for (int64_t c = cb + warp; c < ce; c += 8) acc += V(ab[bix(L, j0 + lane, c)]) * __ldcg(y + c);
+    }
+    part[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0) {
+      V sum = V(0);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) sum += part[k][lane];
+      V v = lane < w ? __ldcg(y + j0 + lane) - sum : V(0);
+      for (int k = w - 1; k >= 0; --k) {
+        V xk = lane == k ? v * Us[k][k] : V(0);  // Us[k][k] holds 1 / U(k, k)
+        xk = __shfl_sync(kFull, xk, k);
+        if (lane == k) v = xk;
+        if (lane < k) v -= Us[k][lane] * xk;
+      }
+      if (lane < w) __stcg(y + j0 + lane, v);
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_release(flags + q, epoch);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+constexpr int kApplyNR = 9;     // 32-row chunks per warp per pass of the bulk update (two warps per column)
+constexpr int kColNR = 6;       // rows per thread per pass of the critical-path update
+
+template <class T>
+static size_t blk_apply_smem(const BandLayout& L, int w) {
+  const size_t R = (size_t)w + L.kl;
+  return ((size_t)w * R + 64 * kApplyNR) * sizeof(T) + 4 * R * sizeof(T) + 128 * sizeof(T) + 32 * sizeof(T) +
+         32 * sizeof(int);  // Lp (+ padding) S Y rd sp
+}
+
+bool blk_plan(const std::vector<int>& blk_end, int wmax, int ku, BlkPlan& out) {
+  const int n = (int)blk_end.size();
+  out.ps.clear();
+  out.ndfp = 0;
+  out.wmax = 0;
+  int j0 = 0;
+  out.ps.push_back(0);
+  while (j0 < n) {
+    int j1 = j0;
+    while (j1 < n && blk_end[j1] - j0 <= wmax) {
+      out.ndfp = std::max(out.ndfp, blk_end[j1] - j1 - 1);
+      j1 = blk_end[j1];
+    }
+    if (j1 == j0) return false;  // a block wider than wmax
+    out.wmax = std::max(out.wmax, j1 - j0);
+    out.ps.push_back(j1);
+    j0 = j1;
+  }
+  out.kuf = ku + out.ndfp;
+  return true;
 }
 
 template <class T>
-cudaError_t blk_lu_setup(const BandLayout& L, int ndfp) {
+int blk_lu_setup(const BandLayout& L) {
   int dev = 0, cap = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
-  if (L.nb > 32 || L.nb + ndfp > kMaxRd) return cudaErrorInvalidValue;
-  if (blk_apply_smem<T>(L, ndfp, 4) > (size_t)cap || blk_fwd_smem(L, ndfp, sizeof(double)) + 9 * 1024 > (size_t)cap)
-    return cudaErrorInvalidValue;
-  if ((e = cudaFuncSetAttribute(blk_apply_kernel<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap)) !=
-      cudaSuccess)
-    return e;
-  if ((e = cudaFuncSetAttribute(blk_apply_col_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                cap - 10 * 1024)) != cudaSuccess)
-    return e;
-  return cudaFuncSetAttribute(blk_forward_kernel<T, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              cap - 10 * 1024);
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  int wmax = 0;
+  for (int w : {32, 24, 16, 8}) {
+    if (w > L.nb) continue;
+    if (blk_apply_smem<T>(L, w) <= (size_t)cap && ((size_t)w + L.kl) * sizeof(double) + 10 * 1024 <= (size_t)cap) {
+      wmax = w;
+      break;
+    }
+  }
+  if (!wmax) return 0;
+  if (cudaFuncSetAttribute(blk_apply_kernel<T, kApplyNR>, cudaFuncAttributeMaxDynamicSharedMemorySize, cap) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(blk_apply_col_kernel<T, kColNR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           cap - 10 * 1024) != cudaSuccess ||
+      cudaFuncSetAttribute(blk_forward_kernel<T, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           cap - 10 * 1024) != cudaSuccess)
+    return 0;
+  return wmax;
 }
 
 // Factor with node-block pivoting (and forward-substitute rhs when given).
-// Lookahead on two streams as in band_lu_factor: st2 updates the next panel's
-// columns (one 1-warp CTA each) and factors that panel, st carries the bulk.
+// Lookahead on two streams: st2 updates the next panel's columns (one CTA
+// each) and factors that panel while st carries the bulk of the update.
+// With prof != nullptr it runs serially on st, recording prof[3p..3p+2].
 template <class T>
-int blk_lu_factor(T* ab, const BandLayout& L, int ndfp, const int* blk_end, int* ipiv, int* perm_all, int rmax,
-                  T* rdiag, int* info, T* rhs, cudaStream_t st, cudaStream_t st2, cudaEvent_t* ev_pool,
-                  cudaEvent_t* prof) {
-  const int64_t npan = (L.n + L.nb - 1) / L.nb;
-  const int kuf = L.ku + ndfp;
+int blk_lu_factor(T* ab, const BandLayout& L, const BlkPlan& B, int* perm_all, T* rdiag, int* info, T* rhs,
+                  cudaStream_t st, cudaStream_t st2, cudaEvent_t* ev_pool, cudaEvent_t* prof) {
+  const int npan = B.npan();
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t as4 = blk_apply_smem<T>(L, ndfp, 4);
   int launches = 0;
-  auto ncol_of = [&](int64_t p) -> int {
-    const int64_t j1 = p * L.nb + min64b(L.nb, L.n - p * L.nb);
-    return (int)(min64b(L.n, j1 + kuf) - j1);
+  auto w_of = [&](int p) { return B.ps[p + 1] - B.ps[p]; };
+  auto ncol_of = [&](int p) -> int {
+    const int64_t j1 = B.ps[p + 1];
+    return (int)(min64b(L.n, j1 + B.kuf) - j1);
   };
-  auto panel = [&](int64_t p, cudaStream_t s) {
-    blk_panel_kernel<T><<<1, 128, 0, s>>>(ab, L, ndfp, p * L.nb, blk_end, ipiv, perm_all + p * rmax, rdiag, info);
+  auto panel = [&](int p, cudaStream_t s) {
+    blk_panel_kernel<T><<<1, 32 * kPanelWarps, 0, s>>>(ab, L, B.ps[p], w_of(p), B.d_blk_end, perm_all + (size_t)p * kBlkW, rdiag,
+                                          info);
     ++launches;
   };
-  auto apply = [&](int64_t p, int cb, int ce, bool with_rhs, cudaStream_t s, bool narrow) {
-    const int n = (ce - cb) + (with_rhs ? 1 : 0);
-    if (n <= 0) return;
+  // columns [cb, ce) of the trailing block of panel p (relative to its end)
+  auto apply = [&](int p, int cb, int ce, bool with_rhs, cudaStream_t s, bool narrow) {
+    const int ncol = ce - cb;
+    const int ntot = ncol + (with_rhs ? 1 : 0);
+    if (ntot <= 0) return;
+    const int64_t j0 = B.ps[p], c0 = B.ps[p + 1] + cb;
+    const int w = w_of(p);
+    const int* pm = perm_all + (size_t)p * kBlkW;
     if (narrow) {
-      blk_apply_col_kernel<T><<<ce - cb, 128, ((size_t)L.nb + L.kl + ndfp) * sizeof(T), s>>>(
-          ab, L, ndfp, p * L.nb, perm_all + p * rmax, rdiag, cb);
+      const size_t sm = ((size_t)w + L.kl) * sizeof(T);
+      blk_apply_col_kernel<T, kColNR><<<ncol, 128, sm, s>>>(ab, L, j0, w, pm, rdiag, c0);
     } else {
-      const int blocks = (int)min64b(sms, (n + 3) / 4);
-      blk_apply_kernel<T, 4><<<blocks, 128, as4, s>>>(ab, L, ndfp, p * L.nb, perm_all + p * rmax, rdiag,
-                                                      with_rhs ? rhs : nullptr, cb, ce);
+      const int blocks = (int)min64b(sms, (ntot + 3) / 4);
+      blk_apply_kernel<T, kApplyNR><<<blocks, 256, blk_apply_smem<T>(L, w), s>>>(
+          ab, L, j0, w, pm, rdiag, with_rhs ? rhs : nullptr, c0, ncol);
     }
     ++launches;
   };
   if (prof || !st2) {
-    for (int64_t p = 0; p < npan; ++p) {
+    for (int p = 0; p < npan; ++p) {
       if (prof) cudaEventRecord(prof[3 * p], st);
       panel(p, st);
       if (prof) cudaEventRecord(prof[3 * p + 1], st);
@@ -455,10 +663,9 @@ int blk_lu_factor(T* ab, const BandLayout& L, int ndfp, const int* blk_end, int*
   cudaStreamWaitEvent(st2, ev_start, 0);
   panel(0, st2);
   cudaEventRecord(ev_panel[0], st2);
-  for (int64_t p = 0; p < npan; ++p) {
+  for (int p = 0; p < npan; ++p) {
     const int nc = ncol_of(p);
-    const int wnext = (p + 1 < npan) ? (int)min64b(L.nb, L.n - (p + 1) * L.nb) : 0;
-    const int split = std::min(nc, wnext);
+    const int split = (p + 1 < npan) ? std::min(nc, w_of(p + 1)) : 0;
     cudaStreamWaitEvent(st, ev_panel[p], 0);
     apply(p, split, nc, rhs != nullptr, st, false);
     cudaEventRecord(ev_rest[p], st);
@@ -475,26 +682,57 @@ int blk_lu_factor(T* ab, const BandLayout& L, int ndfp, const int* blk_end, int*
 }
 
 template <class V, class T>
-void blk_forward(const T* ab, const BandLayout& L, int ndfp, const int* perm_all, int rmax, const T* rdiag, V* b,
+void blk_forward(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
                  cudaStream_t st) {
-  blk_forward_kernel<T, V><<<1, 1024, blk_fwd_smem(L, ndfp, sizeof(V)), st>>>(ab, L, ndfp, perm_all, rmax, rdiag, b);
+  const size_t sm = ((size_t)B.wmax + L.kl) * sizeof(V);
+  blk_forward_kernel<T, V><<<1, 1024, sm, st>>>(ab, L, B.d_ps, B.npan(), perm_all, rdiag, b);
 }
 template <class V, class T>
-void blk_backward(const T* ab, const BandLayout& L, int ndfp, const T* rdiag, V* y, cudaStream_t st) {
-  blk_backward_kernel<T, V><<<1, 1024, 0, st>>>(ab, L, L.ku + ndfp, rdiag, y);
+int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, int* flags, int epoch,
+                 int* err, int grid, cudaStream_t st) {
+  const int npan = B.npan();
+  int kuf = B.kuf;
+  const int* ps = B.d_ps;
+  void* args[] = {(void*)&ab, (void*)&L, (void*)&kuf, (void*)&ps, (void*)&npan, (void*)&rdiag, (void*)&y,
+                  (void*)&flags, (void*)&epoch, (void*)&err};
+  const cudaError_t e = cudaLaunchCooperativeKernel((const void*)blk_backward_coop_kernel<T, V>,
+                                                    dim3(std::min(grid, npan)), dim3(256), args, 0, st);
+  return e == cudaSuccess ? 0 : -1;
+}
+// single-CTA back substitution (used when a cooperative launch is not possible)
+template <class V, class T>
+void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, cudaStream_t st) {
+  blk_backward_kernel<T, V><<<1, 1024, 0, st>>>(ab, L, B.kuf, B.d_ps, B.npan(), rdiag, y);
+}
+// CTAs of the cooperative back substitution that can be resident at once
+template <class V, class T>
+int blk_backward_grid() {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, blk_backward_coop_kernel<T, V>, 256, 0);
+  return std::max(0, sms * std::min(per, 1));
 }
 
-template cudaError_t blk_lu_setup<double>(const BandLayout&, int);
-template cudaError_t blk_lu_setup<float>(const BandLayout&, int);
-template int blk_lu_factor<double>(double*, const BandLayout&, int, const int*, int*, int*, int, double*, int*, double*,
+template int blk_lu_setup<double>(const BandLayout&);
+template int blk_lu_setup<float>(const BandLayout&);
+template int blk_lu_factor<double>(double*, const BandLayout&, const BlkPlan&, int*, double*, int*, double*,
                                    cudaStream_t, cudaStream_t, cudaEvent_t*, cudaEvent_t*);
-template int blk_lu_factor<float>(float*, const BandLayout&, int, const int*, int*, int*, int, float*, int*, float*,
-                                  cudaStream_t, cudaStream_t, cudaEvent_t*, cudaEvent_t*);
-template void blk_forward<double, double>(const double*, const BandLayout&, int, const int*, int, const double*, double*,
-                                          cudaStream_t);
-template void blk_forward<double, float>(const float*, const BandLayout&, int, const int*, int, const float*, double*,
-                                         cudaStream_t);
-template void blk_backward<double, double>(const double*, const BandLayout&, int, const double*, double*, cudaStream_t);
-template void blk_backward<double, float>(const float*, const BandLayout&, int, const float*, double*, cudaStream_t);
+template int blk_lu_factor<float>(float*, const BandLayout&, const BlkPlan&, int*, float*, int*, float*, cudaStream_t,
+                                  cudaStream_t, cudaEvent_t*, cudaEvent_t*);
+template void blk_forward<double, double>(const double*, const BandLayout&, const BlkPlan&, const int*, const double*,
+                                          double*, cudaStream_t);
+template void blk_forward<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*, const float*,
+                                         double*, cudaStream_t);
+template int blk_backward<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*, double*,
+                                          int*, int, int*, int, cudaStream_t);
+template int blk_backward<double, float>(const float*, const BandLayout&, const BlkPlan&, const float*, double*, int*,
+                                         int, int*, int, cudaStream_t);
+template void blk_backward_1cta<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*,
+                                                double*, cudaStream_t);
+template void blk_backward_1cta<double, float>(const float*, const BandLayout&, const BlkPlan&, const float*, double*,
+                                               cudaStream_t);
+template int blk_backward_grid<double, double>();
+template int blk_backward_grid<double, float>();
 
 }  // namespace mafem

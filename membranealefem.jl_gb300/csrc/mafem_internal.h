@@ -130,16 +130,38 @@ void band_forward(const T* ab, const BandLayout& L, const int* perm_all, int rma
 template <class T, class V>
 void band_backward(const T* ab, const BandLayout& L, V* y, cudaStream_t st);
 
-// node-block pivoted banded LU (band_lu_blk.cu)
+// node-block pivoted banded LU (band_lu_blk.cu).  Panels are runs of whole
+// pivot blocks (the unknowns of one control point), at most wmax <= 32 wide.
+constexpr int kBlkW = 32;  // widest panel; also the stride of the per-panel permutations
+struct BlkPlan {
+  int ndfp = 0;          // largest block size - 1
+  int wmax = 0;          // widest panel
+  int kuf = 0;           // bandwidth of U after the interchanges: ku + ndfp
+  std::vector<int> ps;   // panel starts; ps.back() == n
+  int* d_ps = nullptr;   // device copy of ps
+  const int* d_blk_end = nullptr;  // per unknown: one past the last unknown of its block
+  int npan() const { return (int)ps.size() - 1; }
+};
+// Host: panel starts for blocks `blk_end` (false if a block is wider than wmax).
+bool blk_plan(const std::vector<int>& blk_end, int wmax, int ku, BlkPlan& out);
+// Widest panel (<= kBlkW, <= L.nb) whose kernels fit the device's shared memory; 0 if none.
 template <class T>
-cudaError_t blk_lu_setup(const BandLayout& L, int ndfp);
+int blk_lu_setup(const BandLayout& L);
 template <class T>
-int blk_lu_factor(T* ab, const BandLayout& L, int ndfp, const int* blk_end, int* ipiv, int* perm_all, int rmax,
-                  T* rdiag, int* info, T* rhs, cudaStream_t st, cudaStream_t st2, cudaEvent_t* ev_pool,
-                  cudaEvent_t* prof);
+int blk_lu_factor(T* ab, const BandLayout& L, const BlkPlan& B, int* perm_all, T* rdiag, int* info, T* rhs,
+                  cudaStream_t st, cudaStream_t st2, cudaEvent_t* ev_pool, cudaEvent_t* prof);
 template <class V, class T>
-void blk_forward(const T* ab, const BandLayout& L, int ndfp, const int* perm_all, int rmax, const T* rdiag, V* b,
+void blk_forward(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
                  cudaStream_t st);
+// Back substitution U x = y in place on many SMs (one cooperative launch of
+// `grid` CTAs, grid <= blk_backward_grid()).  flags: npan ints, epoch: a value
+// they do not hold yet (incremented per call); err: nonzero after a bounded
+// wait ran out.  Returns -1 if the launch failed.
 template <class V, class T>
-void blk_backward(const T* ab, const BandLayout& L, int ndfp, const T* rdiag, V* y, cudaStream_t st);
+int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, int* flags, int epoch,
+                 int* err, int grid, cudaStream_t st);
+template <class V, class T>
+int blk_backward_grid();
+template <class V, class T>
+void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, cudaStream_t st);
 }  // namespace mafem

@@ -101,7 +101,8 @@ class StepStats(C.Structure):
 class KernelTimes(C.Structure):
     _fields_ = [("ms_assemble", C.c_double), ("ms_panel", C.c_double), ("ms_apply", C.c_double),
                 ("n_panel", C.c_int64), ("n_apply", C.c_int64), ("n", C.c_int64), ("kl", C.c_int64),
-                ("ku", C.c_int64), ("nb", C.c_int64), ("ndfp", C.c_int64)]
+                ("ku", C.c_int64), ("nb", C.c_int64), ("ndfp", C.c_int64),
+                ("flop_panel", C.c_double), ("flop_apply", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
