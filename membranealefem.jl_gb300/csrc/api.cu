@@ -102,6 +102,8 @@ struct mafem_handle {
   int* d_flags = nullptr;  // per-panel completion flags of the cooperative back substitution
   int epoch = 0;           // value the flags are set to by the next back substitution
   int bwd_grid = 0;        // CTAs of the cooperative back substitution (0: single-CTA kernel)
+  BlkPersist pers;         // persistent cooperative factorisation (grid 0: per-panel launches)
+  int fepoch = 0;          // epoch of the last persistent factorisation
   void* d_rdiag = nullptr;
   int64_t fallbacks = 0;
 };
@@ -404,6 +406,20 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
       cudaMemset(h->d_flags, 0, (size_t)h->blk.npan() * sizeof(int));
       h->bwd_grid = precision == MAFEM_PLAIN_FP64 ? blk_backward_grid<double, double>() : blk_backward_grid<double, float>();
       cudaGetLastError();
+      const int pg = precision == MAFEM_PLAIN_FP64 ? blk_persist_setup<double>(h->L, h->blk, h->pers)
+                                                   : blk_persist_setup<float>(h->L, h->blk, h->pers);
+      cudaGetLastError();
+      if (pg > 0) {
+        const size_t np = (size_t)h->blk.npan();
+        AL(h->pers.d_pdone, np);
+        AL(h->pers.d_critcnt, np);
+        AL(h->pers.d_a21cnt, np);
+        cudaMemset(h->pers.d_pdone, 0, np * sizeof(int));
+        cudaMemset(h->pers.d_critcnt, 0, np * sizeof(int));
+        cudaMemset(h->pers.d_a21cnt, 0, np * sizeof(int));
+      } else {
+        h->pers.grid = 0;
+      }
       const size_t nev = (size_t)2 * h->blk.npan() + 2;
       while (h->ev_pool.size() < nev) {
         cudaEvent_t e = nullptr;
@@ -553,15 +569,39 @@ static int factor(mafem_handle* h, double* x, const double* rhs0) {
   const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
   CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
   if (h->use_blk) {
-    const int nl = fp64 ? blk_lu_factor<double>((double*)h->d_band, h->L, h->blk, h->d_perm, (double*)h->d_rdiag,
-                                                h->d_info, x, h->st, h->st2, h->ev_pool.data(), nullptr)
-                        : blk_lu_factor<float>((float*)h->d_band, h->L, h->blk, h->d_perm, (float*)h->d_rdiag,
-                                               h->d_info, nullptr, h->st, h->st2, h->ev_pool.data(), nullptr);
-    h->launches += nl;
+    bool launched = false;
+    if (h->pers.grid > 0) {
+      ++h->fepoch;
+      const int nl = fp64 ? blk_lu_factor_persist<double>((double*)h->d_band, h->L, h->blk, h->pers, h->fepoch,
+                                                          h->d_perm, (double*)h->d_rdiag, h->d_info, x, h->d_info + 1,
+                                                          h->st)
+                          : blk_lu_factor_persist<float>((float*)h->d_band, h->L, h->blk, h->pers, h->fepoch,
+                                                         h->d_perm, (float*)h->d_rdiag, h->d_info, nullptr,
+                                                         h->d_info + 1, h->st);
+      if (nl < 0) {
+        cudaGetLastError();
+        h->pers.grid = 0;  // cooperative launch refused: per-panel launches from now on
+      } else {
+        h->launches += nl;
+        launched = true;
+      }
+    }
+    if (!launched) {
+      const int nl = fp64 ? blk_lu_factor<double>((double*)h->d_band, h->L, h->blk, h->d_perm, (double*)h->d_rdiag,
+                                                  h->d_info, x, h->st, h->st2, h->ev_pool.data(), nullptr)
+                          : blk_lu_factor<float>((float*)h->d_band, h->L, h->blk, h->d_perm, (float*)h->d_rdiag,
+                                                 h->d_info, nullptr, h->st, h->st2, h->ev_pool.data(), nullptr);
+      h->launches += nl;
+    }
     CK(cudaGetLastError());
-    int info = 0;
-    CK(cudaMemcpyAsync(&info, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    int info2[2] = {0, 0};
+    CK(cudaMemcpyAsync(info2, h->d_info, sizeof info2, cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
+    const int info = info2[0];
+    if (info2[1]) {
+      h->err = "banded LU: a bounded wait for another CTA ran out";
+      return MAFEM_ERR_CUDA;
+    }
     if (info == 0) {
       h->factored = true;
       h->last_blk = true;
@@ -879,6 +919,37 @@ static void lu_flops(const mafem_handle* h, double* fpanel, double* fapply) {
   }
   *fpanel = fp;
   *fapply = fa;
+}
+
+// Diagnostic (not in the public header): assemble at (time, dt), factor once
+// with the persistent kernel and copy its per-panel clock stamps
+// (12 int64 per panel, see blk_lu_factor_persist) to out[0 .. 12 * npan).
+// Returns npan, or a negative status.
+extern "C" int mafem_trace_factor(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap) {
+  if (!h || !out || !h->use_blk || h->pers.grid <= 0) return MAFEM_ERR_UNSUPPORTED;
+  const int npan = h->blk.npan();
+  if (cap < 12LL * npan) return MAFEM_ERR_ARG;
+  long long* d_tr = nullptr;
+  CK(cudaMalloc(&d_tr, sizeof(long long) * 12 * npan));
+  CK(cudaMemsetAsync(d_tr, 0, sizeof(long long) * 12 * npan, h->st));
+  int rc = assemble(h, time, dt);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(h->d_x, h->d_r, h->nmdf * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
+  ++h->fepoch;
+  const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
+  const int nl = fp64 ? blk_lu_factor_persist<double>((double*)h->d_band, h->L, h->blk, h->pers, h->fepoch, h->d_perm,
+                                                      (double*)h->d_rdiag, h->d_info, h->d_x, h->d_info + 1, h->st,
+                                                      d_tr)
+                      : blk_lu_factor_persist<float>((float*)h->d_band, h->L, h->blk, h->pers, h->fepoch, h->d_perm,
+                                                     (float*)h->d_rdiag, h->d_info, nullptr, h->d_info + 1, h->st,
+                                                     d_tr);
+  h->factored = true;
+  h->last_blk = true;
+  CK(cudaMemcpyAsync(out, d_tr, sizeof(long long) * 12 * npan, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  cudaFree(d_tr);
+  return nl < 0 ? MAFEM_ERR_CUDA : npan;
 }
 
 extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, mafem_kernel_times* out) {

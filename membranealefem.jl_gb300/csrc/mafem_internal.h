@@ -162,6 +162,29 @@ int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rd
                  int* err, int grid, cudaStream_t st);
 template <class V, class T>
 int blk_backward_grid();
+// Persistent cooperative factorisation (band_lu_persist.cu): launch shape and
+// per-panel flags.  Flags are zeroed once; epochs make them reusable.
+struct BlkPersist {
+  int grid = 0;
+  size_t smem = 0;
+  int* d_pdone = nullptr;
+  int* d_critcnt = nullptr;
+  int* d_a21cnt = nullptr;
+};
+// Fills S (host part); returns the grid (0: not available on this device / size).
+template <class T>
+int blk_persist_setup(const BandLayout& L, const BlkPlan& B, BlkPersist& S);
+// One launch; returns 1, or -1 if the cooperative launch was refused.
+template <class T>
+// trace (optional, device): 12 globaltimer stamps per panel t -- [0] the
+// factorising CTA starts waiting for t's columns, [1] they are ready, [2] t is
+// published; for the owner of t's first column: [3] it starts step t - 1,
+// [4] its waits are over, [5] panel t - 1 is staged, [6] its columns are
+// solved, [7] the rows t reads are written, [8] the rest of the rows,
+// [9] its column copies are issued, [10] the A21 copies are issued, [11] the
+// diagonal block is in shared memory.
+int blk_lu_factor_persist(T* ab, const BandLayout& L, const BlkPlan& B, const BlkPersist& S, int epoch, int* perm_all,
+                          T* rdiag, int* info, T* rhs, int* err, cudaStream_t st, long long* trace = nullptr);
 template <class V, class T>
 void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, cudaStream_t st);
 }  // namespace mafem
