@@ -247,4 +247,49 @@ __device__ __forceinline__ void blk_panel_factor(T* __restrict__ ab, const BandL
 }
 
 
+// Variant of blk_panel_factor with the block in shared memory (P[c][r],
+// 32 x 33): a warp visits its columns with a run-time index, so the pivot
+// step is one call site instead of one per register slot (smaller code, no
+// per-slot branches); the column of the next pivot is still updated first.
+template <class T, bool CG, int NW = kPanelWarps>
+__device__ __forceinline__ void blk_panel_factor_smem(T* __restrict__ ab, const BandLayout& L, int64_t j0, int w,
+                                                      const int* __restrict__ blk_end, int* __restrict__ perm,
+                                                      T* __restrict__ rdiag, int* __restrict__ info, T (*s_l)[32],
+                                                      int* s_p, T (*P)[33]) {
+  const int tid = threadIdx.x, lane = tid & 31, q = tid >> 5;
+  const int bend = lane < w ? (int)(blk_end[j0 + lane] - j0) : 0;
+  for (int c = q; c < w; c += NW) P[c][lane] = lane < w ? ldx<CG>(ab + bix(L, j0 + lane, j0 + c)) : T(0);
+  __syncwarp();
+  unsigned E = 0u;
+  int mypos = 0, op = 0;
+  T ol = T(0);
+  if (q == 0) P[0][lane] = blk_pivot_step(0, P[0][lane], w, lane, bend, E, j0, s_l, s_p, perm, rdiag, info, op, ol,
+                                          32 * NW);
+  for (int k = 0; k < w; ++k) {
+    int p;
+    T l;
+    if (q == k % NW) {
+      p = op;
+      l = ol;
+    } else {
+      bar_sync_n(1 + (k & 1), 32 * NW);
+      p = s_p[k & 1];
+      l = s_l[k & 1][lane];
+    }
+    E |= 1u << p;
+    if (lane == p) mypos = k;
+    // my columns > k, the next pivot's first
+    for (int c = k + 1 + (((q - (k + 1)) % NW) + NW) % NW; c < w; c += NW) {
+      const T u = P[c][p];
+      T v = fma(-l, u, P[c][lane]);  // l == 0 on eliminated rows
+      if (c == k + 1) v = blk_pivot_step(k + 1, v, w, lane, bend, E, j0, s_l, s_p, perm, rdiag, info, op, ol, 32 * NW);
+      __syncwarp();
+      P[c][lane] = v;
+      __syncwarp();
+    }
+  }
+  for (int c = q; c < w; c += NW)
+    if (lane < w) ab[bix(L, j0 + mypos, j0 + c)] = P[c][lane];
+}
+
 }  // namespace mafem

@@ -1,11 +1,11 @@
 // band_lu_persist.cu -- the node-block pivoted banded LU (band_lu_blk.cu) as
 // ONE persistent cooperative launch per factorisation.
 //
-// Roles.  CTA G-1 only factorises panels.  Column c (and the right-hand side,
-// as column n) is owned by worker CTA c mod (G-1) for the whole
-// factorisation, so the updates of a column by successive panels run in
-// order on one CTA without any flag; a worker has ~(ku + ndfp) / (G-1)
-// columns per panel.
+// Roles.  CTA G-1 only factorises panels; CTA G-2 carries the right-hand side
+// (when there is one).  Column c is owned by worker CTA c mod GW for the
+// whole factorisation, so the updates of a column by successive panels run in
+// order on one CTA without any flag; a worker has ~(ku + ndfp) / GW columns
+// per panel.
 //
 // Per panel p every worker with columns in p's trailing range:
 //   1. waits for pdone[p] (panel p factorised) and a21cnt[p] (every column of
@@ -96,7 +96,11 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
   __shared__ int64_t s_col[kMaxCols];  // this panel's columns (-1: the right-hand side)
   __shared__ T s_part[4][32];          // partial sums of the critical rows
   const BandLayout& L = a.L;
-  const int G = gridDim.x, me = blockIdx.x, GW = G - 1;
+  // CTA G-1 factorises; with a right-hand side CTA G-2 carries it alone (its
+  // extra column would otherwise make one worker late every few panels);
+  // CTAs 0 .. GW-1 own the columns.
+  const int G = gridDim.x, me = blockIdx.x, GW = G - 1 - (a.rhs ? 1 : 0);
+  const bool rhs_cta = a.rhs != nullptr && me == G - 2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if (me == G - 1) {  // the factorising CTA
@@ -131,7 +135,6 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
   int* sp = reinterpret_cast<int*>(rd + 32);          // [32]
   __shared__ __align__(8) uint64_t s_bar[2];          // TMA completion: [0] tops, [1] the panel's A21
   __shared__ int s_sb[4];                             // S slot offsets
-  const int rhs_owner = (int)(L.n % GW);
   if (tid == 0) {
     mbar_init(&s_bar[0], 1);
     mbar_init(&s_bar[1], 1);
@@ -182,8 +185,8 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
     const int64_t jend = min64b(L.n, j1 + a.kuf);
     const int64_t jn = p + 1 < a.npan ? a.ps[p + 2] : j1;  // panel p + 1 = columns [j1, jn)
     const int64_t cend = jend > jn ? jend : jn;
-    const bool is_rhs = a.rhs != nullptr && me == rhs_owner;
-    const int64_t cfirst = j1 + (((me - j1) % GW) + GW) % GW;
+    const bool is_rhs = rhs_cta;
+    const int64_t cfirst = rhs_cta ? cend : j1 + (((me - j1) % GW) + GW) % GW;
     if (cfirst >= cend && !is_rhs) continue;
     const bool tr_owner = p + 1 < a.npan && me == j1 % GW;
     if (tr_owner) stamp(a.trace, p + 1, 3);
@@ -224,11 +227,16 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
       }
       const bool pc = with_panel && lane < w;
       const T* pd_src = pc ? a.ab + bix(L, j0, j0 + lane) : nullptr;
+      // rows [0, P1) of panel column `lane` (diagonal block + chunk 0, the rows the
+      // next factorisation's update reads) on s_bar[0], rows [P1, R) on s_bar[1];
+      // P1 = first 16-byte-aligned row at or after w + 32
+      const int br = min(R, w + 32);
+      const int P1 = min(R, br + (int)((-(L.off - lane + br)) & (E - 1)));
       uint32_t b0b = 0, b1b = 0;
       if (lane < nb) b0b += seg_copy(sd, ss, R, &s_bar[0], 0);
       if (pc) {
-        b0b += seg_copy(lpa(lane), pd_src, w, &s_bar[0], 0);
-        b1b += seg_copy(lpa(lane) + w, pd_src + w, R - w, &s_bar[1], 0);
+        b0b += seg_copy(lpa(lane), pd_src, P1, &s_bar[0], 0);
+        if (R > P1) b1b += seg_copy(lpa(lane) + P1, pd_src + P1, R - P1, &s_bar[1], 0);
       }
       for (int o = 16; o > 0; o >>= 1) {
         b0b += __shfl_xor_sync(kFull, b0b, o);
@@ -242,8 +250,8 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
       for (int mode = 1; mode <= 2; ++mode) {
         if (lane < nb) seg_copy(sd, ss, R, &s_bar[0], mode);
         if (pc) {
-          seg_copy(lpa(lane), pd_src, w, &s_bar[0], mode);
-          seg_copy(lpa(lane) + w, pd_src + w, R - w, &s_bar[1], mode);
+          seg_copy(lpa(lane), pd_src, P1, &s_bar[0], mode);
+          if (R > P1) seg_copy(lpa(lane) + P1, pd_src + P1, R - P1, &s_bar[1], mode);
         }
       }
     };
@@ -270,25 +278,35 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
           const int64_t c = s_col[b0 + warp];
           const T* s = S + s_sb[warp];
           T* dst = c < 0 ? a.rhs + j0 : a.ab + bix(L, j0, c);
+          // this lane's row of the diagonal block in registers (no shared-memory
+          // load on the dependency chains): L(lane, k) for k < lane, U(lane, k) for k > lane
+          T Tr[32];
+#pragma unroll
+          for (int k = 0; k < 32; ++k) Tr[k] = (k < w && lane < w) ? lpa(k)[lane] : T(0);
           T x = lane < w ? s[sp[lane]] : T(0);  // row `lane` of the permuted top
-          for (int k = 0; k < w; ++k) {
-            const T xk = __shfl_sync(kFull, x, k);
-            if (lane > k && lane < w) x -= lpa(k)[lane] * xk;
+#pragma unroll
+          for (int k = 0; k < 32; ++k) {
+            if (k < w) {
+              const T xk = __shfl_sync(kFull, x, k);
+              if (lane > k) x = fma(-Tr[k], xk, x);
+            }
           }
-          if (lane < w) dst[lane] = x;
-          fence_proxy_async_global();
+          if (lane < w) dst[lane] = x;  // U12: not read again by this kernel
           v = x;
-          for (int k = w - 1; k >= 0; --k) {
-            T yk = lane == k ? v * rd[k] : T(0);
-            yk = __shfl_sync(kFull, yk, k);
-            if (lane == k) v = yk;
-            if (lane < k) v -= lpa(k)[lane] * yk;
+          const T rl = lane < w ? rd[lane] : T(0);
+#pragma unroll
+          for (int k = 31; k >= 0; --k) {
+            if (k < w) {
+              T yk = lane == k ? v * rl : T(0);
+              yk = __shfl_sync(kFull, yk, k);
+              if (lane == k) v = yk;
+              if (lane < k) v = fma(-Tr[k], yk, v);
+            }
           }
         }
         Y[warp * 32 + lane] = (warp < nb && lane < w) ? v : T(0);
       }
-      if (b0 == 0 && !wait_bar(&s_bar[1], ph1)) return;  // A21
-      if (b0 > 0) __syncthreads();
+      __syncthreads();
       if (tr_owner && b0 == 0) stamp(a.trace, p + 1, 6);
       // rows [w, R): s -= A21 y, 32-row chunks; tasks (column qq, chunk ci) in [q0, q1) x [c0, c1)
       auto rows = [&](int q0, int q1, int c0, int c1) {
@@ -325,12 +343,12 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
             dst[r] = S[s_sb[0] + min(r, R - 1)] +
                      ((s_part[0][lane] + s_part[1][lane]) + (s_part[2][lane] + s_part[3][lane]));
           }
-          fence_proxy_async_global();
-          __threadfence();
+          __threadfence();  // read by the factorising CTA with L2-only loads (and rewritten by it before any TMA read)
           __syncthreads();
         }
         if (tid == 0) atomicAdd(a.critcnt + p + 1, 1);
         if (tr_owner) stamp(a.trace, p + 1, 7);
+        if (!wait_bar(&s_bar[1], ph1)) return;  // the rest of A21
         if (reach) {
           rows(0, 1, min(1, nch), nch);
           __threadfence();
@@ -340,6 +358,7 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
         if (tr_owner) stamp(a.trace, p + 1, 8);
         q0 = 1;
       }
+      if (b0 == 0 && q0 == 0 && !wait_bar(&s_bar[1], ph1)) return;  // the rest of A21
       if (q0 < nb) rows(q0, nb, 0, nch);
     }
   }
@@ -364,7 +383,7 @@ int blk_persist_setup(const BandLayout& L, const BlkPlan& B, BlkPersist& S) {
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
   const size_t sm = persist_smem<T>(L);
-  if (!coop || sm + 2048 > (size_t)cap || B.wmax > kBlkW) return 0;
+  if (!coop || sm + 12 * 1024 > (size_t)cap || B.wmax > kBlkW) return 0;  // + static shared memory
   if (cudaFuncSetAttribute(blk_factor_persist_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
       cudaSuccess)
     return 0;
@@ -374,7 +393,7 @@ int blk_persist_setup(const BandLayout& L, const BlkPlan& B, BlkPersist& S) {
   // workers need at most kMaxCols columns each per panel (columns c of the
   // trailing range, owned by c mod (G - 1), plus the right-hand side)
   S.grid = sms;
-  if ((int64_t)(S.grid - 1) * kMaxCols < (int64_t)B.kuf + kBlkW + 1) return S.grid = 0;
+  if ((int64_t)(S.grid - 2) * kMaxCols < (int64_t)B.kuf + kBlkW + 1) return S.grid = 0;
   S.smem = sm;
   return S.grid;
 }
