@@ -39,6 +39,10 @@ sys.path.insert(0, os.path.join(ROOT, "membranealefem.jl_gb300"))
 WORKLOAD = dict(name="ALEVB tether pull, 32x32 graded patch (34x34 control points), plain FP64",
                 motion=5, n=32, length=1.0, kb=1.0, kg=-0.5, zeta_v=1.0, dt=0.005, pull_speed=0.02,
                 seed=0, amp=1e-4)
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
+# dominant kernel, from one ncu capture of this workload (profiles/
+# blk_factor_persist_kernel.alevb32.md gives the command); None until captured.
+NCU_TRAFFIC = {"blk_factor_persist_kernel<double>": 74_519_552 + 18_702_336}
 METRIC = "membrane time-steps/s"
 
 
@@ -170,7 +174,7 @@ def run_gb300(args, rank, world, local, dist):
             t += dt
             s.predict(dt)
             s.time_step_resident(t, dt)
-        lat, iters, dev_ms = [], [], []
+        lat, iters, dev_ms, fac_ms, asm_ms, sol_ms = [], [], [], [], [], []
         launches0 = s.launch_count()
         cu.flush_l2()
         barrier(dist)
@@ -184,16 +188,21 @@ def run_gb300(args, rank, world, local, dist):
                 lat.append((time.perf_counter() - h0) * 1e3)
                 iters.append(st["newton_iters"])
                 dev_ms.append(st["ms_total"])
+                fac_ms.append(st["ms_factor"])
+                asm_ms.append(st["ms_assemble"])
+                sol_ms.append(st["ms_solve"])
                 cu.flush_l2()
         cu.sync()
         barrier(dist)
         launches = s.launch_count() - launches0
-        total_ms = allmax(dist, float(sum(lat)))
+        # device time of the K steps: CUDA events on the library's stream around every
+        # Newton loop (the ~3 us predictor launch between steps is not inside them)
+        total_ms = allmax(dist, float(sum(dev_ms)))
         x_fp64, c_fp64 = s.download()
         # per-kernel timing of one factorisation (roofline)
         kt = s.profile_factor(t, dt)
     out["resident"] = dict(total_ms=total_ms, lat=lat, iters=iters, dev_ms=dev_ms, launches=launches,
-                           clocks=clk.summary(), kt=kt)
+                           clocks=clk.summary(), kt=kt, fac_ms=fac_ms, asm_ms=asm_ms, sol_ms=sol_ms)
 
     # ---- e2e: host buffers through the C ABI, H2D/D2H inside every step ----
     mmo = [mesh.dofs[d] - 1 for d in (3, 4, 5)] if p.motion != M.LAG else [mesh.dofs[d] - 1 for d in (0, 1, 2)]
@@ -319,13 +328,12 @@ def main():
     res = r["resident"]
     K = args.steps
     value = world * K / (res["total_ms"] / 1e3)
-    lat = sorted(res["lat"])
+    lat = sorted(res["dev_ms"])
     kt = res["kt"]
-    m = r["mesh"]
-    fl_apply = kt["flop_apply"]  # counted by the library from the factorisation it ran
-    blk = kt["ndfp"] >= 0
-    apply_launch_ms = kt["ms_apply"] / kt["n_apply"]
-    achieved = fl_apply / kt["n_apply"] / (apply_launch_ms * 1e-3) / 1e12
+    n_fact = sum(res["iters"])  # one factorisation per Newton iteration
+    fac_ms = sum(res["fac_ms"]) / n_fact
+    flops = kt["flop_panel"] + kt["flop_apply"]  # counted by the library from the factorisation it ran
+    achieved = flops / (fac_ms * 1e-3) / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": "time-steps/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": res["total_ms"] / K, "higher_is_better": True,
@@ -339,22 +347,24 @@ def main():
                 "state_rel_err_vs_resident": r["e2e_state_err"]},
         "gpu_launches": res["launches"],
         "roofline": {"bound": "fp64",
-                     "kernel": ("blk_apply_kernel<double,4> (node-block pivoted banded-LU trailing update)" if blk
-                                else "panel_apply_kernel<double> (banded-LU trailing update)"),
+                     "kernel": "blk_factor_persist_kernel<double> (persistent node-block pivoted banded LU, "
+                               "one launch per Newton iteration)",
                      "achieved": achieved, "peak": r["fp64_tflops"], "unit": "TFLOP/s",
                      "frac": achieved / r["fp64_tflops"],
-                     "peak_source": "FP64 FMA throughput measured live on this GPU (mafem_probe_fp64_tflops)",
-                     "flops_per_launch": fl_apply / kt["n_apply"], "launch_ms": apply_launch_ms,
-                     "share_of_factor": kt["ms_apply"] / (kt["ms_apply"] + kt["ms_panel"]),
-                     "traffic": None},
-        "phase_ms_per_iter": {"assemble": kt["ms_assemble"], "lu_panel": kt["ms_panel"], "lu_apply": kt["ms_apply"]},
+                     "peak_source": "FP64 FMA throughput measured live on this GPU (mafem_probe_fp64_tflops); "
+                                    "the kernel is bound by the FP64 pipe and its critical path, not by HBM "
+                                    "or tensor cores",
+                     "flops_per_launch": flops, "launch_ms": fac_ms,
+                     "traffic": NCU_TRAFFIC.get("blk_factor_persist_kernel<double>")},
+        "phase_ms_per_iter": {"assemble": sum(res["asm_ms"]) / n_fact, "factor": fac_ms,
+                              "back_substitution": sum(res["sol_ms"]) / n_fact},
         "clocks": res["clocks"],
         "precision_fp32_refine": {"value": K / (r["fp32"]["total_ms"] / 1e3), "unit": "time-steps/s",
                                   "newton_iters_per_step": statistics.mean(r["fp32"]["iters"]),
                                   "refine_sweeps_per_step": statistics.mean(r["fp32"]["refine"]),
                                   "rel_err_xms": r["fp32"]["err_x"], "rel_err_vel": r["fp32"]["err_v"],
                                   "rel_err_lambda": r["fp32"]["err_lam"]},
-        "mesh": m,
+        "mesh": r["mesh"],
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
