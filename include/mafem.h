@@ -49,10 +49,19 @@ enum mafem_neumann { MAFEM_SHEAR = 1, MAFEM_STRETCH = 2, MAFEM_MOMENT = 3 };
 
 /* Linear-algebra form of a handle. */
 enum mafem_precision {
-  MAFEM_PLAIN_FP64 = 0, /* FP64 tangent, FP64 banded LU with partial pivoting */
-  MAFEM_FP32_REFINE = 1 /* FP64 residual; FP32 tangent and FP32 banded LU whose
-                           trailing updates are 3xTF32 tensor-core products;
-                           FP64 iterative refinement of every solve */
+  MAFEM_PLAIN_FP64 = 0, /* FP64 tangent, FP64 banded LU (node-block partial pivoting) */
+  MAFEM_FP32_REFINE = 1 /* FP64 residual; FP32 tangent and FP32 banded LU (same
+                           algorithm); FP64 iterative refinement of every solve */
+};
+
+/* Which banded LU a handle uses (mafem_set_lu_path; no reference counterpart:
+ * the reference calls Julia's sparse `\`).  Testing and diagnostics. */
+enum mafem_lu_path {
+  MAFEM_LU_AUTO = 0,   /* node-block pivoting as one persistent cooperative launch when the
+                          device allows it, else per-panel launches; full partial pivoting
+                          when a node block has no usable pivot (the default) */
+  MAFEM_LU_PANELS = 1, /* node-block pivoting, per-panel launches */
+  MAFEM_LU_FULL = 2    /* full partial pivoting (LAPACK gbtrf's pivot rule) */
 };
 
 /* Params (src/input/Params.jl:36-55), field for field. */
@@ -162,6 +171,11 @@ int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, maf
 
 /* Number of kernels this handle has enqueued since mafem_create. */
 int64_t mafem_launch_count(const mafem_handle* h);
+
+/* Select the banded LU (enum mafem_lu_path) for the following factorisations.
+ * MAFEM_ERR_UNSUPPORTED if the handle cannot run that path (e.g. the node-block
+ * forms when the band is too wide for their shared-memory panels). */
+int mafem_set_lu_path(mafem_handle* h, int32_t path);
 
 typedef struct mafem_kernel_times {
   double ms_assemble;         /* element kernel + gathers */

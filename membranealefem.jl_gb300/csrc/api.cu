@@ -103,6 +103,7 @@ struct mafem_handle {
   int epoch = 0;           // value the flags are set to by the next back substitution
   int bwd_grid = 0;        // CTAs of the cooperative back substitution (0: single-CTA kernel)
   BlkPersist pers;         // persistent cooperative factorisation (grid 0: per-panel launches)
+  int lu_path = MAFEM_LU_AUTO;
   int fepoch = 0;          // epoch of the last persistent factorisation
   void* d_rdiag = nullptr;
   int64_t fallbacks = 0;
@@ -568,9 +569,9 @@ static int factor(mafem_handle* h, double* x, const double* rhs0) {
   const int64_t n = h->nmdf;
   const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
   CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
-  if (h->use_blk) {
+  if (h->use_blk && h->lu_path != MAFEM_LU_FULL) {
     bool launched = false;
-    if (h->pers.grid > 0) {
+    if (h->pers.grid > 0 && h->lu_path == MAFEM_LU_AUTO) {
       ++h->fepoch;
       const int nl = fp64 ? blk_lu_factor_persist<double>((double*)h->d_band, h->L, h->blk, h->pers, h->fepoch,
                                                           h->d_perm, (double*)h->d_rdiag, h->d_info, x, h->d_info + 1,
@@ -950,6 +951,17 @@ extern "C" int mafem_trace_factor(mafem_handle* h, double time, double dt, int64
   CK(cudaStreamSynchronize(h->st));
   cudaFree(d_tr);
   return nl < 0 ? MAFEM_ERR_CUDA : npan;
+}
+
+extern "C" int mafem_set_lu_path(mafem_handle* h, int32_t path) {
+  if (!h || path < MAFEM_LU_AUTO || path > MAFEM_LU_FULL) return MAFEM_ERR_ARG;
+  if (path == MAFEM_LU_PANELS && !h->use_blk) {
+    h->err = "the node-block LU is not available for this band";
+    return MAFEM_ERR_UNSUPPORTED;
+  }
+  h->lu_path = path;
+  h->factored = false;
+  return MAFEM_OK;
 }
 
 extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, mafem_kernel_times* out) {

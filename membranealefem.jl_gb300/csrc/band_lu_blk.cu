@@ -357,15 +357,21 @@ __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restr
     part[warp][lane] = acc;
     __syncthreads();
     if (warp == 0) {
-      V sum = V(0);
+      const V sum = ((part[0][lane] + part[1][lane]) + (part[2][lane] + part[3][lane])) +
+                    ((part[4][lane] + part[5][lane]) + (part[6][lane] + part[7][lane]));  // tree: 3 dependent adds
+      // U11 x = v with this lane's row in registers, pre-scaled by 1/U(lane, lane)
+      // (unit diagonal): each step of the chain is one shuffle and one FMA
+      const V rl = lane < w ? Us[lane][lane] : V(0);  // 1 / U(lane, lane)
+      V Ur[32];
 #pragma unroll
-      for (int k = 0; k < 8; ++k) sum += part[k][lane];
-      V v = lane < w ? __ldcg(y + j0 + lane) - sum : V(0);
-      for (int k = w - 1; k >= 0; --k) {
-        V xk = lane == k ? v * Us[k][k] : V(0);  // Us[k][k] holds 1 / U(k, k)
-        xk = __shfl_sync(kFull, xk, k);
-        if (lane == k) v = xk;
-        if (lane < k) v -= Us[k][lane] * xk;
+      for (int k = 0; k < 32; ++k) Ur[k] = (k < w && lane < k) ? Us[k][lane] * rl : V(0);
+      V v = lane < w ? (__ldcg(y + j0 + lane) - sum) * rl : V(0);
+#pragma unroll
+      for (int k = 31; k >= 0; --k) {
+        if (k < w) {
+          const V xk = __shfl_sync(kFull, v, k);
+          if (lane < k) v = fma(-Ur[k], xk, v);
+        }
       }
       if (lane < w) __stcg(y + j0 + lane, v);
       __threadfence();

@@ -292,14 +292,17 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
             }
           }
           if (lane < w) dst[lane] = x;  // U12: not read again by this kernel
-          v = x;
+          // y = U11^-1 u with this lane's U row pre-scaled by 1/U(lane, lane)
+          // (unit diagonal): each step is one shuffle and one FMA
           const T rl = lane < w ? rd[lane] : T(0);
+#pragma unroll
+          for (int k = 0; k < 32; ++k)
+            if (k > lane) Tr[k] *= rl;
+          v = x * rl;
 #pragma unroll
           for (int k = 31; k >= 0; --k) {
             if (k < w) {
-              T yk = lane == k ? v * rl : T(0);
-              yk = __shfl_sync(kFull, yk, k);
-              if (lane == k) v = yk;
+              const T yk = __shfl_sync(kFull, v, k);
               if (lane < k) v = fma(-Tr[k], yk, v);
             }
           }

@@ -39,6 +39,7 @@ STATIC, EUL, LAG, ALEV, ALEVB = 1, 2, 3, 4, 5
 BOTTOM, RIGHT, TOP, LEFT = 1, 2, 3, 4
 SHEAR, STRETCH, MOMENT = 1, 2, 3
 PLAIN_FP64, FP32_REFINE = 0, 1
+LU_AUTO, LU_PANELS, LU_FULL = 0, 1, 2  # mafem_set_lu_path
 
 OK = 0
 NEWTON_NOT_CONVERGED, ZERO_PIVOT, NAN_DETECTED, REFINE_STALLED = 1, 2, 3, 4
@@ -147,6 +148,7 @@ def lib():
         L.mafem_run.argtypes = [vp, _PD, C.c_int32, C.c_double, C.POINTER(StepStats)]
         L.mafem_launch_count.argtypes = [vp]
         L.mafem_launch_count.restype = C.c_int64
+        L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
         L.mafem_profile_factor.argtypes = [vp, C.c_double, C.c_double, C.POINTER(KernelTimes)]
         L.mafem_probe_fp64_tflops.argtypes = [C.POINTER(C.c_double)]
         _lib = L
@@ -330,6 +332,10 @@ class Solver:
     def launch_count(self) -> int:
         """Kernels this handle has enqueued so far."""
         return int(lib().mafem_launch_count(self.h))
+
+    def set_lu_path(self, path: int) -> None:
+        """Select the banded LU: LU_AUTO (default), LU_PANELS or LU_FULL."""
+        _raise(lib().mafem_set_lu_path(self.h, path), self.h)
 
     def profile_factor(self, time: float, dt: float) -> dict:
         """Per-kernel device time of one assembly + factorisation of the resident state."""
