@@ -167,6 +167,13 @@ int mafem_time_step_host(mafem_handle* h, double* xms, double* cps, double time,
  * predictor + time_step! for each Δt; times[k] = t0 + sum(dts[0..k]). */
 int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, mafem_step_stats* last);
 
+/* calc_pull_force (src/analysis/PullForce.jl:61-80) on the resident state:
+ * the velocity residual of calc_elem_dof_residuals over the 5x5 elements around
+ * element ceil(numel/2) (get_adj_maps, PullForce.jl:25-53), summed over that
+ * element's nodes -> f_out[3].  The reference writes it to f-pull.txt after
+ * each step of an F_PULL run (src/Analysis.jl:81-91). */
+int mafem_pull_force(mafem_handle* h, double* f_out);
+
 /* ---- diagnostics --------------------------------------------------------------- */
 
 /* Number of kernels this handle has enqueued since mafem_create. */

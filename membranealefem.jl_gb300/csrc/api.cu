@@ -103,6 +103,9 @@ struct mafem_handle {
   int epoch = 0;           // value the flags are set to by the next back substitution
   int bwd_grid = 0;        // CTAs of the cooperative back substitution (0: single-CTA kernel)
   BlkPersist pers;         // persistent cooperative factorisation (grid 0: per-panel launches)
+  std::vector<int> h_ix;   // IX, 0-based [element][9] (pull-force neighbourhood)
+  int* d_pull_list = nullptr;
+  double* d_pull_r = nullptr;
   int lu_path = MAFEM_LU_AUTO;
   int fepoch = 0;          // epoch of the last persistent factorisation
   void* d_rdiag = nullptr;
@@ -376,6 +379,9 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     }                                         \
   } while (0)
   UP(d_ix, ix);
+  h->h_ix = ix;
+  AL(h->d_pull_list, 25);
+  AL(h->d_pull_r, (size_t)25 * nq);
   UP(d_lm, lm);
   UP(d_uel, uel);
   UP(d_bref, bref);
@@ -951,6 +957,50 @@ extern "C" int mafem_trace_factor(mafem_handle* h, double time, double dt, int64
   CK(cudaStreamSynchronize(h->st));
   cudaFree(d_tr);
   return nl < 0 ? MAFEM_ERR_CUDA : npan;
+}
+
+// calc_pull_force (PullForce.jl:61-80) with get_pull_el_id / get_adj_maps
+// (PullForce.jl:8-53): the velocity residual rv of calc_elem_dof_residuals
+// (area Gauss points only) of the (2·poly+1)² elements around element
+// ceil(numel/2), summed over that element's nodes.  The element rows come
+// from the element kernel (area-only mode on the 25-element list); the sum is
+// done here in a fixed order.
+extern "C" int mafem_pull_force(mafem_handle* h, double* f_out) {
+  if (!h || !f_out) return MAFEM_ERR_ARG;
+  const int poly = h->p.poly, n1 = h->p.num1el, numel = h->numel, nq = h->nq, ndf = h->ndf;
+  const int pull = (numel + 1) / 2 - 1;  // ceil(numel / 2), 0-based
+  std::vector<int> adj;
+  for (int i = -poly; i <= poly; ++i)
+    for (int j = -poly; j <= poly; ++j) adj.push_back(pull + i * n1 + j);
+  for (int e : adj)
+    if (e < 0 || e >= numel) {
+      h->err = "the pull element's neighbourhood leaves the patch";
+      return MAFEM_ERR_ARG;
+    }
+  if ((int)adj.size() > 25) {
+    h->err = "pull-force neighbourhood larger than 5 x 5 elements";
+    return MAFEM_ERR_UNSUPPORTED;
+  }
+  const int na = (int)adj.size();
+  CK(cudaMemcpyAsync(h->d_pull_list, adj.data(), na * sizeof(int), cudaMemcpyHostToDevice, h->st));
+  CK(launch_elem<double>(h->P, h->pp, 0.0, 0.0, h->d_pull_r, (double*)nullptr, h->st, h->d_pull_list, na, 1));
+  h->launches += 1;
+  std::vector<double> r((size_t)na * nq);
+  CK(cudaMemcpyAsync(r.data(), h->d_pull_r, r.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  const int* pn = h->h_ix.data() + (size_t)pull * 9;
+  double f[3] = {0.0, 0.0, 0.0};
+  for (int k = 0; k < na; ++k)
+    for (int a = 0; a < 9; ++a) {
+      const int node = h->h_ix[(size_t)adj[k] * 9 + a];
+      if (std::find(pn, pn + 9, node) == pn + 9) continue;
+      for (int c = 0; c < 3; ++c) {
+        const int d = h->pp.dof_of[c];
+        if (d >= 0) f[c] += r[(size_t)k * nq + a * ndf + d];
+      }
+    }
+  for (int c = 0; c < 3; ++c) f_out[c] = f[c];
+  return MAFEM_OK;
 }
 
 extern "C" int mafem_set_lu_path(mafem_handle* h, int32_t path) {

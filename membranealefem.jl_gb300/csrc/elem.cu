@@ -358,15 +358,20 @@ __device__ __forceinline__ void bdry_gp(const PhysParams& pp, const double* X, c
   }
 }
 
+// elist (optional): evaluate only elements elist[0 .. nlist) and write their rows
+// to r_el[k][q]; area_only: the area Gauss points alone (calc_elem_dof_residuals
+// without the Dohrmann-Bochev projection or boundary terms, as PullForce.jl uses
+// it); K_el may be null (no tangent written).
 template <class T, int MOTION, int EPB>
 __global__ void elem_kernel(DevPatch P, PhysParams pp, double time, double dt, double* __restrict__ r_el,
-                            T* __restrict__ K_el) {
+                            T* __restrict__ K_el, const int* __restrict__ elist, int nlist, int area_only) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nq = pp.nq, ndf = pp.ndf;
   const int ldk = nq + 1;
   const int slot = threadIdx.x / nq;
   const int q = threadIdx.x - slot * nq;
-  const int e = blockIdx.x * EPB + slot;
+  const int kk = blockIdx.x * EPB + slot;  // element (or list) index of this slot
+  const int e = elist ? (kk < nlist ? elist[kk] : 0) : kk;
   // per-slot shared memory
   const size_t dbl_per_slot = 27 + 72 + 9 * kTab;
   double* base = reinterpret_cast<double*>(smem_raw);
@@ -374,7 +379,7 @@ __global__ void elem_kernel(DevPatch P, PhysParams pp, double time, double dt, d
   double* C = X + 27;
   double* tab = C + 72;
   T* Ks = reinterpret_cast<T*>(base + EPB * dbl_per_slot) + (size_t)slot * nq * ldk;
-  const bool live = (slot < EPB) && (e < P.numel);
+  const bool live = (slot < EPB) && (elist ? kk < nlist : e < P.numel);
 
   if (live) {
     const int u = P.uel[e];
@@ -403,7 +408,7 @@ __global__ void elem_kernel(DevPatch P, PhysParams pp, double time, double dt, d
 
   // Dohrmann-Bochev projection (FiniteElement.jl:323-327): rλ += Gᵀ H⁻¹ G λ αdb/ζv,
   // and for ALEV/ALEVB rp += Gᵀ H⁻¹ G p αdb/ζv.  Linear in λ / p.
-  {
+  if (!area_only) {
     const double* T81 = P.db + (size_t)P.uel[e] * 81;
     const double s = pp.adb / pp.zv;
     const int lo = pp.dof_of[6], po = pp.dof_of[7];
@@ -427,7 +432,7 @@ __global__ void elem_kernel(DevPatch P, PhysParams pp, double time, double dt, d
 
   // Neumann boundary terms of this element (calc_r_K's boundary loop,
   // FiniteElement.jl:150-197): same LM, so they add into the same block.
-  for (int k = 0; k < pp.n_neu; ++k) {
+  for (int k = 0; k < (area_only ? 0 : pp.n_neu); ++k) {
     int b = pp.neu_bdry[k];
     int row = P.bref[e * 4 + b];
     if (row < 0) continue;
@@ -436,10 +441,10 @@ __global__ void elem_kernel(DevPatch P, PhysParams pp, double time, double dt, d
                  rsum, Ks, ldk);
   }
 
-  r_el[(size_t)e * nq + q] = rsum;
+  r_el[(size_t)(elist ? kk : e) * nq + q] = rsum;
   }
   __syncthreads();
-  if (live) {
+  if (live && K_el) {
     // column-major element block K_el[e][col][row] (coalesced stores)
     T* dst = K_el + (size_t)e * nq * nq;
     for (int idx = q; idx < nq * nq; idx += nq) {
@@ -457,33 +462,34 @@ size_t elem_smem_bytes(int nq, int epb) {
 
 template <class T, int MOTION, int EPB>
 static cudaError_t launch_elem_t(const DevPatch& P, const PhysParams& pp, double time, double dt, double* r_el,
-                                 T* K_el, cudaStream_t st) {
+                                 T* K_el, cudaStream_t st, const int* elist, int nlist, int area_only) {
   // the cap is the size needed by the largest element (nq = 72), identical for every caller
   cudaError_t e = cudaFuncSetAttribute(elem_kernel<T, MOTION, EPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)elem_smem_bytes<T>(72, EPB));
   if (e != cudaSuccess) return e;
-  const int blocks = (P.numel + EPB - 1) / EPB;
+  const int blocks = ((elist ? nlist : P.numel) + EPB - 1) / EPB;
   elem_kernel<T, MOTION, EPB><<<blocks, EPB * pp.nq, elem_smem_bytes<T>(pp.nq, EPB), st>>>(P, pp, time, dt, r_el,
-                                                                                         K_el);
+                                                                                         K_el, elist, nlist,
+                                                                                         area_only);
   return cudaGetLastError();
 }
 
 template <class T>
 cudaError_t launch_elem(const DevPatch& P, const PhysParams& pp, double time, double dt, double* r_el, T* K_el,
-                        cudaStream_t st) {
+                        cudaStream_t st, const int* elist, int nlist, int area_only) {
   switch (pp.motion) {
-    case MAFEM_STATIC: return launch_elem_t<T, STATIC_, 4>(P, pp, time, dt, r_el, K_el, st);
-    case MAFEM_EUL: return launch_elem_t<T, EUL_, 2>(P, pp, time, dt, r_el, K_el, st);
-    case MAFEM_LAG: return launch_elem_t<T, LAG_, 4>(P, pp, time, dt, r_el, K_el, st);
-    case MAFEM_ALEV: return launch_elem_t<T, ALEV_, 2>(P, pp, time, dt, r_el, K_el, st);
-    default: return launch_elem_t<T, ALEVB_, 2>(P, pp, time, dt, r_el, K_el, st);
+    case MAFEM_STATIC: return launch_elem_t<T, STATIC_, 4>(P, pp, time, dt, r_el, K_el, st, elist, nlist, area_only);
+    case MAFEM_EUL: return launch_elem_t<T, EUL_, 2>(P, pp, time, dt, r_el, K_el, st, elist, nlist, area_only);
+    case MAFEM_LAG: return launch_elem_t<T, LAG_, 4>(P, pp, time, dt, r_el, K_el, st, elist, nlist, area_only);
+    case MAFEM_ALEV: return launch_elem_t<T, ALEV_, 2>(P, pp, time, dt, r_el, K_el, st, elist, nlist, area_only);
+    default: return launch_elem_t<T, ALEVB_, 2>(P, pp, time, dt, r_el, K_el, st, elist, nlist, area_only);
   }
 }
 
 template cudaError_t launch_elem<double>(const DevPatch&, const PhysParams&, double, double, double*, double*,
-                                         cudaStream_t);
+                                         cudaStream_t, const int*, int, int);
 template cudaError_t launch_elem<float>(const DevPatch&, const PhysParams&, double, double, double*, float*,
-                                        cudaStream_t);
+                                        cudaStream_t, const int*, int, int);
 template size_t elem_smem_bytes<double>(int, int);
 template size_t elem_smem_bytes<float>(int, int);
 

@@ -96,7 +96,7 @@ template <class T>
 size_t elem_smem_bytes(int nq, int epb);
 template <class T>
 cudaError_t launch_elem(const DevPatch& P, const PhysParams& pp, double time, double dt, double* r_el, T* K_el,
-                        cudaStream_t st);
+                        cudaStream_t st, const int* elist = nullptr, int nlist = 0, int area_only = 0);
 template <class T>
 void launch_band_gather(const DevPatch& P, int ndf, int nq, const BandLayout& L, const T* K_el, T* ab,
                         cudaStream_t st);

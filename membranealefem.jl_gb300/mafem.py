@@ -149,6 +149,7 @@ def lib():
         L.mafem_launch_count.argtypes = [vp]
         L.mafem_launch_count.restype = C.c_int64
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
+        L.mafem_pull_force.argtypes = [vp, _PD]
         L.mafem_profile_factor.argtypes = [vp, C.c_double, C.c_double, C.POINTER(KernelTimes)]
         L.mafem_probe_fp64_tflops.argtypes = [C.POINTER(C.c_double)]
         _lib = L
@@ -332,6 +333,12 @@ class Solver:
     def launch_count(self) -> int:
         """Kernels this handle has enqueued so far."""
         return int(lib().mafem_launch_count(self.h))
+
+    def pull_force(self) -> np.ndarray:
+        """calc_pull_force (PullForce.jl:61-80) on the resident state: 3-vector."""
+        f = np.zeros(3)
+        _raise(lib().mafem_pull_force(self.h, _dp(f)), self.h)
+        return f
 
     def set_lu_path(self, path: int) -> None:
         """Select the banded LU: LU_AUTO (default), LU_PANELS or LU_FULL."""

@@ -1668,6 +1668,45 @@ int orc_band_solve(int n, int kl, int ku, double* ab, int ldab, const int* ipiv,
 }
 void orc_update_xms(void* h, double* xms, const double* c, double dt) { update_xms(*(Mesh*)h, xms, c, dt); }
 
+// calc_pull_force (PullForce.jl:61-80) with get_pull_el_id (:8-13) and
+// get_adj_maps (:25-53): real(rv) of calc_elem_dof_residuals of each element
+// adjacent to element ceil(numel/2), at the nodes it shares with that element,
+// summed over the pulled element's nodes -> f[3].  Ids outside 1..numel are an
+// error (the reference would raise a BoundsError).
+int orc_pull_force(void* h, const double* xms, const double* cps, double* f) {
+  ORC_TRY({
+    Mesh* m = (Mesh*)h;
+    const int poly = m->p.poly, numel = m->numel, n1 = m->p.num1el;
+    const int pull = (numel + 1) / 2;  // ceil(numel / 2), 1-based
+    std::vector<int> pull_nodes;
+    for (int a = 1; a <= NEN; ++a) pull_nodes.push_back(m->IX(a, pull));
+    std::vector<double> rv_pull((size_t)3 * NEN, 0.0);
+    for (int i = -poly; i <= poly; ++i)
+      for (int j = -poly; j <= poly; ++j) {
+        const int adj = pull + i * n1 + j;
+        ORC_ASSERT(adj >= 1 && adj <= numel, "pull-force neighbourhood leaves the patch");
+        Mat1<cd> xel, cel;
+        gather_el(*m, adj, xms, cps, xel, cel);
+        DofRes R = calc_elem_dof_residuals(*m, adj, xel, cel);
+        // (pull-local node, adj-local node) pairs in increasing local order on both sides
+        std::vector<int> pl, al;
+        for (int a = 1; a <= NEN; ++a) {
+          for (int b = 1; b <= NEN; ++b)
+            if (m->IX(b, adj) == pull_nodes[a - 1]) { pl.push_back(a); break; }
+        }
+        for (int b = 1; b <= NEN; ++b)
+          if (std::find(pull_nodes.begin(), pull_nodes.end(), m->IX(b, adj)) != pull_nodes.end()) al.push_back(b);
+        for (size_t t = 0; t < pl.size(); ++t)
+          for (int k = 0; k < 3; ++k) rv_pull[(size_t)3 * (pl[t] - 1) + k] += R.rv[(size_t)3 * (al[t] - 1) + k].real();
+      }
+    for (int k = 0; k < 3; ++k) {
+      double s = 0.0;
+      for (int a = 0; a < NEN; ++a) s += rv_pull[(size_t)3 * a + k];
+      f[k] = s;
+    }
+  })
+}
+
 // time_step! (FiniteElement.jl:11-63) with the banded LU as the linear solver.
 // eps_out receives up to 14 values; returns 1 (assertion) if not converged.
 int orc_time_step(void* h, double* xms, double* cps, double time, double dt, int nthreads, int* iters,

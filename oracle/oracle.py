@@ -96,7 +96,7 @@ def lib():
                      "orc_mesh_LM", "orc_mesh_ID_inv", "orc_mesh_knots", "orc_mesh_area",
                      "orc_mesh_bdry", "orc_mesh_bdry_elems", "orc_mesh_bdry_nodes",
                      "orc_mesh_neu", "orc_mesh_dir", "orc_prepare_input", "orc_gds",
-                     "orc_elem_r_K", "orc_calc_r_K", "orc_update_xms", "orc_time_step"):
+                     "orc_elem_r_K", "orc_calc_r_K", "orc_update_xms", "orc_time_step", "orc_pull_force"):
             getattr(L, name).argtypes = None
         _lib = L
     return _lib
@@ -438,6 +438,12 @@ class Mesh:
     def update_xms(self, xms, c, dt: float):
         assert xms.flags.f_contiguous and c.flags.f_contiguous
         lib().orc_update_xms(self.h, _dp(xms), _dp(np.asfortranarray(c)), C.c_double(dt))
+
+    def pull_force(self, xms, cps) -> np.ndarray:
+        """calc_pull_force (src/analysis/PullForce.jl:61-80) at the given state: 3-vector."""
+        f = np.zeros(3)
+        _chk(lib().orc_pull_force(self.h, _dp(np.asfortranarray(xms)), _dp(np.asfortranarray(cps)), _dp(f)))
+        return f
 
     def time_step(self, xms, cps, time: float, dt: float, nthreads: int = 0):
         """time_step! (src/analysis/FiniteElement.jl:11-63), band-LU solve; in place."""
