@@ -174,6 +174,26 @@ int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, maf
  * each step of an F_PULL run (src/Analysis.jl:81-91). */
 int mafem_pull_force(mafem_handle* h, double* f_out);
 
+/* ---- batching (no reference counterpart: the reference steps one patch) -----------
+ * Many independent patches (handles of any sizes, motions and precisions) advance
+ * together: mafem_batch_step runs predictor + time_step! for every patch, each
+ * patch's Newton iterations enqueued on its own stream and interleaved with the
+ * others', so their kernels overlap on the GPU.  Results are those of
+ * mafem_time_step on each handle alone.  A handle belongs to at most one batch
+ * at a time; the batch does not own the handles. */
+typedef struct mafem_batch mafem_batch;
+/* ctas: CTAs of each patch's persistent factorisation (0: each patch's smallest
+ * grid, which lets the most factorisations run at once). */
+int mafem_batch_create(mafem_handle* const* handles, int32_t n, int32_t ctas, mafem_batch** out);
+/* times[i], dts[i] per patch; status[i] (optional) = the patch's mafem_time_step
+ * status; stats (optional, n entries).  Returns the first nonzero status. */
+int mafem_batch_step(mafem_batch* b, const double* times, const double* dts, int32_t* status,
+                     mafem_step_stats* stats);
+int mafem_batch_destroy(mafem_batch* b);
+/* CTAs of this handle's persistent factorisation and back substitution (0: all
+ * SMs); clamped to what the band needs.  Returns the CTAs the factorisation uses. */
+int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas);
+
 /* ---- diagnostics --------------------------------------------------------------- */
 
 /* Number of kernels this handle has enqueued since mafem_create. */

@@ -104,6 +104,12 @@ struct mafem_handle {
   int bwd_grid = 0;        // CTAs of the cooperative back substitution (0: single-CTA kernel)
   BlkPersist pers;         // persistent cooperative factorisation (grid 0: per-panel launches)
   std::vector<int> h_ix;   // IX, 0-based [element][9] (pull-force neighbourhood)
+  int bwd_max = 0;         // back-substitution CTAs before any cap
+  // the time step in progress (step_begin / iter_enqueue / iter_finish)
+  double ss_time = 0, ss_dt = 0, ss_eps = 0;
+  int ss_iter = 0, ss_sweeps = 0;
+  bool ss_async = false;
+  mafem_step_stats ss_S{};
   int* d_pull_list = nullptr;
   double* d_pull_r = nullptr;
   int lu_path = MAFEM_LU_AUTO;
@@ -412,6 +418,7 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
       AL(h->d_flags, (size_t)h->blk.npan());
       cudaMemset(h->d_flags, 0, (size_t)h->blk.npan() * sizeof(int));
       h->bwd_grid = precision == MAFEM_PLAIN_FP64 ? blk_backward_grid<double, double>() : blk_backward_grid<double, float>();
+      h->bwd_max = h->bwd_grid;
       cudaGetLastError();
       const int pg = precision == MAFEM_PLAIN_FP64 ? blk_persist_setup<double>(h->L, h->blk, h->pers)
                                                    : blk_persist_setup<float>(h->L, h->blk, h->pers);
@@ -571,36 +578,50 @@ static int assemble(mafem_handle* h, double time, double dt) {
 // with full partial pivoting.  `x` (may be null) is the right-hand side that
 // rides along the factorisation (forward substitution); `rhs0` restores it for
 // the fallback.
+// Launch the node-block factorisation (persistent kernel, or per-panel launches)
+// without waiting for it; `info` tells later whether a block had no usable pivot.
+static int factor_enqueue(mafem_handle* h, double* x) {
+  const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
+  CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
+  bool launched = false;
+  if (h->pers.grid > 0 && h->lu_path == MAFEM_LU_AUTO) {
+    ++h->fepoch;
+    const int nl = fp64 ? blk_lu_factor_persist<double>((double*)h->d_band, h->L, h->blk, h->pers, h->fepoch, h->d_perm,
+                                                        (double*)h->d_rdiag, h->d_info, x, h->d_info + 1, h->st)
+                        : blk_lu_factor_persist<float>((float*)h->d_band, h->L, h->blk, h->pers, h->fepoch, h->d_perm,
+                                                       (float*)h->d_rdiag, h->d_info, nullptr, h->d_info + 1, h->st);
+    if (nl < 0) {
+      cudaGetLastError();
+      h->pers.grid = 0;  // cooperative launch refused: per-panel launches from now on
+    } else {
+      h->launches += nl;
+      launched = true;
+    }
+  }
+  if (!launched) {
+    const int nl = fp64 ? blk_lu_factor<double>((double*)h->d_band, h->L, h->blk, h->d_perm, (double*)h->d_rdiag,
+                                                h->d_info, x, h->st, h->st2, h->ev_pool.data(), nullptr)
+                        : blk_lu_factor<float>((float*)h->d_band, h->L, h->blk, h->d_perm, (float*)h->d_rdiag,
+                                               h->d_info, nullptr, h->st, h->st2, h->ev_pool.data(), nullptr);
+    h->launches += nl;
+  }
+  CK(cudaGetLastError());
+  h->factored = true;
+  h->last_blk = true;
+  return MAFEM_OK;
+}
+
+// Factorise the assembled band: node-block pivoting first; if a node block has
+// no usable pivot, re-gather the band from the element blocks and factor it
+// with full partial pivoting.  `x` (may be null) is the right-hand side that
+// rides along the factorisation (forward substitution); `rhs0` restores it for
+// the fallback.
 static int factor(mafem_handle* h, double* x, const double* rhs0) {
   const int64_t n = h->nmdf;
   const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
-  CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
   if (h->use_blk && h->lu_path != MAFEM_LU_FULL) {
-    bool launched = false;
-    if (h->pers.grid > 0 && h->lu_path == MAFEM_LU_AUTO) {
-      ++h->fepoch;
-      const int nl = fp64 ? blk_lu_factor_persist<double>((double*)h->d_band, h->L, h->blk, h->pers, h->fepoch,
-                                                          h->d_perm, (double*)h->d_rdiag, h->d_info, x, h->d_info + 1,
-                                                          h->st)
-                          : blk_lu_factor_persist<float>((float*)h->d_band, h->L, h->blk, h->pers, h->fepoch,
-                                                         h->d_perm, (float*)h->d_rdiag, h->d_info, nullptr,
-                                                         h->d_info + 1, h->st);
-      if (nl < 0) {
-        cudaGetLastError();
-        h->pers.grid = 0;  // cooperative launch refused: per-panel launches from now on
-      } else {
-        h->launches += nl;
-        launched = true;
-      }
-    }
-    if (!launched) {
-      const int nl = fp64 ? blk_lu_factor<double>((double*)h->d_band, h->L, h->blk, h->d_perm, (double*)h->d_rdiag,
-                                                  h->d_info, x, h->st, h->st2, h->ev_pool.data(), nullptr)
-                          : blk_lu_factor<float>((float*)h->d_band, h->L, h->blk, h->d_perm, (float*)h->d_rdiag,
-                                                 h->d_info, nullptr, h->st, h->st2, h->ev_pool.data(), nullptr);
-      h->launches += nl;
-    }
-    CK(cudaGetLastError());
+    int rc = factor_enqueue(h, x);
+    if (rc) return rc;
     int info2[2] = {0, 0};
     CK(cudaMemcpyAsync(info2, h->d_info, sizeof info2, cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
@@ -622,8 +643,8 @@ static int factor(mafem_handle* h, double* x, const double* rhs0) {
       CK(cudaMemcpyAsync(h->d_band, h->d_band0, (size_t)h->L.ldb * n * sizeof(float), cudaMemcpyDeviceToDevice,
                          h->st));
     if (x && rhs0) CK(cudaMemcpyAsync(x, rhs0, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-    CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
   }
+  CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
   const int nl = fp64 ? band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, x,
                                                h->apply_threads, h->apply_blocks, h->st, h->st2, h->ev_pool.data(),
                                                nullptr)
@@ -812,62 +833,207 @@ extern "C" int mafem_predict(mafem_handle* h, double dt) {
   return MAFEM_OK;
 }
 
-extern "C" int mafem_time_step(mafem_handle* h, double time, double dt, mafem_step_stats* stats) {
-  if (!h) return MAFEM_ERR_ARG;
-  mafem_step_stats S;
-  std::memset(&S, 0, sizeof S);
-  double eps = INFINITY;
-  int iter = 1;
+// ---- a time step as step_begin / iter_enqueue / iter_finish: mafem_time_step
+// runs them for one handle, mafem_batch_step interleaves many handles ----
+
+static void step_begin(mafem_handle* h, double time, double dt) {
+  h->ss_time = time;
+  h->ss_dt = dt;
+  h->ss_iter = 1;
+  h->ss_eps = INFINITY;
+  std::memset(&h->ss_S, 0, sizeof h->ss_S);
   cudaEventRecord(h->ev[5], h->st);
-  while (iter < 15) {  // FiniteElement.jl:29
-    cudaEventRecord(h->ev[0], h->st);
-    int rc = assemble(h, time, dt);
-    if (rc) return rc;
-    cudaEventRecord(h->ev[1], h->st);
-    int sweeps = 0;
-    rc = factor_and_solve(h, h->d_r, &sweeps);
-    if (rc) return rc;
-    cudaEventRecord(h->ev[3], h->st);
-    launch_newton_update(h->P, h->pp, dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st);
-    h->launches += 2;
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
-    cudaEventRecord(h->ev[4], h->st);
-    CK(cudaStreamSynchronize(h->st));
-    float ms_a = 0, ms_f = 0, ms_s = 0;
-    cudaEventElapsedTime(&ms_a, h->ev[0], h->ev[1]);
-    cudaEventElapsedTime(&ms_f, h->ev[1], h->ev[2]);
-    cudaEventElapsedTime(&ms_s, h->ev[2], h->ev[4]);
-    S.ms_assemble += ms_a;
-    S.ms_factor += ms_f;
-    S.ms_solve += ms_s;
-    S.refine_iters += sweeps;
-    eps = h->h_out[0];
-    S.eps[iter - 1] = eps;
-    S.res_norm[iter - 1] = h->h_out[1];
-    S.newton_iters = iter;
-    if ((rc = check_info(h)) != MAFEM_OK) {
-      if (stats) *stats = S;
-      return rc;
-    }
-    if (h->h_out[2] != 0.0 || !std::isfinite(eps)) {
-      h->err = "non-finite residual or Newton update";
-      if (stats) *stats = S;
-      return MAFEM_NAN_DETECTED;
-    }
-    iter += 1;
-    if (eps < h->p.eps_nr) break;
+}
+
+// Enqueue Newton iteration ss_iter (FiniteElement.jl:29-57).  The plain FP64
+// node-block path does not wait for its factorisation: a block without a
+// usable pivot shows in `info`, the update kernel then leaves the state
+// unchanged, and iter_finish redoes the iteration with full pivoting.  The
+// other forms run factor_and_solve, which waits where it must.
+static int iter_enqueue(mafem_handle* h) {
+  const int64_t n = h->nmdf;
+  cudaEventRecord(h->ev[0], h->st);
+  int rc = assemble(h, h->ss_time, h->ss_dt);
+  if (rc) return rc;
+  cudaEventRecord(h->ev[1], h->st);
+  h->ss_sweeps = 0;
+  h->ss_async = h->precision == MAFEM_PLAIN_FP64 && h->use_blk && h->lu_path != MAFEM_LU_FULL;
+  if (h->ss_async) {
+    CK(cudaMemcpyAsync(h->d_x, h->d_r, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    if ((rc = factor_enqueue(h, h->d_x)) != MAFEM_OK) return rc;
+    cudaEventRecord(h->ev[2], h->st);
+    blk_back_solve<double>(h, h->d_x);
+  } else if ((rc = factor_and_solve(h, h->d_r, &h->ss_sweeps)) != MAFEM_OK) {
+    return rc;
   }
-  float ms_t = 0;
-  cudaEventElapsedTime(&ms_t, h->ev[5], h->ev[4]);
-  S.ms_total = ms_t;
-  if (stats) *stats = S;
-  if (!(eps < h->p.eps_nr)) {  // FiniteElement.jl:61
+  cudaEventRecord(h->ev[3], h->st);
+  launch_newton_update(h->P, h->pp, h->ss_dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st, h->d_info);
+  h->launches += 2;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  cudaEventRecord(h->ev[4], h->st);
+  return MAFEM_OK;
+}
+
+static void accum_times(mafem_handle* h) {
+  float ms_a = 0, ms_f = 0, ms_s = 0;
+  cudaEventElapsedTime(&ms_a, h->ev[0], h->ev[1]);
+  cudaEventElapsedTime(&ms_f, h->ev[1], h->ev[2]);
+  cudaEventElapsedTime(&ms_s, h->ev[2], h->ev[4]);
+  h->ss_S.ms_assemble += ms_a;
+  h->ss_S.ms_factor += ms_f;
+  h->ss_S.ms_solve += ms_s;
+}
+
+enum { kIterAgain = -100, kIterDone = -101 };
+
+// Wait for the enqueued iteration and apply the Newton criterion: kIterAgain,
+// kIterDone (converged), or a status.
+static int iter_finish(mafem_handle* h) {
+  CK(cudaEventSynchronize(h->ev[4]));
+  accum_times(h);
+  int info[2] = {0, 0};
+  std::memcpy(info, h->h_out + 5, sizeof info);
+  if (info[1] == 0 && info[0] != 0 && h->ss_async) {
+    // a node block without a usable pivot: the update was skipped; redo this
+    // iteration with full partial pivoting
+    ++h->fallbacks;
+    const int saved = h->lu_path;
+    h->lu_path = MAFEM_LU_FULL;
+    const int rc = iter_enqueue(h);
+    h->lu_path = saved;
+    if (rc) return rc;
+    CK(cudaEventSynchronize(h->ev[4]));
+    accum_times(h);
+  }
+  mafem_step_stats& S = h->ss_S;
+  const int iter = h->ss_iter;
+  S.refine_iters += h->ss_sweeps;
+  const double eps = h->h_out[0];
+  h->ss_eps = eps;
+  S.eps[iter - 1] = eps;
+  S.res_norm[iter - 1] = h->h_out[1];
+  S.newton_iters = iter;
+  int rc = check_info(h);
+  if (rc != MAFEM_OK) return rc;
+  if (h->h_out[2] != 0.0 || !std::isfinite(eps)) {
+    h->err = "non-finite residual or Newton update";
+    return MAFEM_NAN_DETECTED;
+  }
+  h->ss_iter = iter + 1;
+  if (eps < h->p.eps_nr) return kIterDone;
+  if (h->ss_iter >= 15) {  // FiniteElement.jl:29,61
     h->err = "did not reach Newton--Raphson tolerance";
     return MAFEM_NEWTON_NOT_CONVERGED;
   }
+  return kIterAgain;
+}
+
+static void step_stats(mafem_handle* h, mafem_step_stats* stats) {
+  float ms_t = 0;
+  cudaEventElapsedTime(&ms_t, h->ev[5], h->ev[4]);
+  h->ss_S.ms_total = ms_t;
+  if (stats) *stats = h->ss_S;
+}
+
+extern "C" int mafem_time_step(mafem_handle* h, double time, double dt, mafem_step_stats* stats) {
+  if (!h) return MAFEM_ERR_ARG;
+  step_begin(h, time, dt);
+  int rc;
+  do {
+    rc = iter_enqueue(h);
+    if (rc != MAFEM_OK) return rc;
+    rc = iter_finish(h);
+  } while (rc == kIterAgain);
+  step_stats(h, stats);
+  return rc == kIterDone ? MAFEM_OK : rc;
+}
+
+extern "C" int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas) {
+  if (!h || ctas < 0) return MAFEM_ERR_ARG;
+  if (h->pers.max_grid > 0)
+    h->pers.grid = ctas == 0 ? h->pers.max_grid : std::max(h->pers.min_grid, std::min(ctas, h->pers.max_grid));
+  if (h->bwd_max > 0) h->bwd_grid = ctas == 0 ? h->bwd_max : std::max(1, std::min((int)ctas, h->bwd_max));
+  return h->pers.max_grid > 0 ? h->pers.grid : h->bwd_grid;
+}
+
+struct mafem_batch {
+  std::vector<mafem_handle*> hs;
+};
+
+extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ctas, mafem_batch** out) {
+  if (!out || n < 0 || (n > 0 && !hs) || ctas < 0) {
+    set_global_error("mafem_batch_create: bad arguments");
+    return MAFEM_ERR_ARG;
+  }
+  auto b = std::make_unique<mafem_batch>();
+  for (int i = 0; i < n; ++i) {
+    if (!hs[i]) {
+      set_global_error("mafem_batch_create: null handle");
+      return MAFEM_ERR_ARG;
+    }
+    for (mafem_handle* o : b->hs)
+      if (o == hs[i]) {
+        set_global_error("mafem_batch_create: a handle appears twice");
+        return MAFEM_ERR_ARG;
+      }
+    b->hs.push_back(hs[i]);
+    // ctas == 0: each patch's smallest persistent grid, so that many patches' factorisations fit at once
+    const int c = ctas > 0 ? ctas : std::max(1, hs[i]->pers.min_grid);
+    mafem_set_launch_ctas(hs[i], c);
+  }
+  *out = b.release();
   return MAFEM_OK;
+}
+
+extern "C" int mafem_batch_destroy(mafem_batch* b) {
+  delete b;
+  return MAFEM_OK;
+}
+
+// One time step of every patch: predictor + Newton, the patches' iterations
+// interleaved -- every active patch's iteration k is enqueued (each handle on
+// its own stream) before any is waited for, so their kernels overlap.
+extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const double* dts, int32_t* status,
+                                mafem_step_stats* stats) {
+  if (!b || !times || !dts) return MAFEM_ERR_ARG;
+  const int n = (int)b->hs.size();
+  std::vector<int> active, st(n, MAFEM_OK);
+  for (int i = 0; i < n; ++i) {
+    mafem_handle* h = b->hs[i];
+    launch_predictor(h->P, h->pp, dts[i], h->st);  // update_xms! (Analysis.jl:193)
+    h->launches += 1;
+    step_begin(h, times[i], dts[i]);
+    active.push_back(i);
+  }
+  while (!active.empty()) {
+    std::vector<int> next;
+    for (int i : active) {
+      const int rc = iter_enqueue(b->hs[i]);
+      if (rc != MAFEM_OK) st[i] = rc;
+    }
+    for (int i : active) {
+      if (st[i] != MAFEM_OK) continue;
+      const int rc = iter_finish(b->hs[i]);
+      if (rc == kIterAgain) {
+        next.push_back(i);
+      } else {
+        st[i] = rc == kIterDone ? MAFEM_OK : rc;
+        step_stats(b->hs[i], stats ? stats + i : nullptr);
+      }
+    }
+    active.swap(next);
+  }
+  int first = MAFEM_OK;
+  for (int i = 0; i < n; ++i) {
+    if (status) status[i] = st[i];
+    if (first == MAFEM_OK && st[i] != MAFEM_OK) {
+      first = st[i];
+      set_global_error("patch " + std::to_string(i) + ": " + b->hs[i]->err);
+    }
+  }
+  return first;
 }
 
 extern "C" int mafem_time_step_host(mafem_handle* h, double* xms, double* cps, double time, double dt,

@@ -84,9 +84,16 @@ __global__ void predictor_kernel(DevPatch P, PhysParams pp, double dt) {
 
 // Newton update (FiniteElement.jl:41-46): Δu = -x, Δcps[ID_inv] = Δu, cps += Δcps,
 // xms[:, j] += dt Δcps[:, m_motion_order[j]]; per-block partial sums of Δu² and r².
+// skip: when *skip != 0 (the factorisation found no usable pivot) the state is
+// left unchanged; the host redoes the iteration with full partial pivoting.
 __global__ void newton_update_kernel(DevPatch P, PhysParams pp, double dt, const double* __restrict__ x,
-                                     const double* __restrict__ r, double* __restrict__ part) {
+                                     const double* __restrict__ r, double* __restrict__ part,
+                                     const int* __restrict__ skip) {
   __shared__ double s_du[32], s_r[32];
+  if (skip && *skip) {
+    if (threadIdx.x == 0) part[2 * blockIdx.x] = part[2 * blockIdx.x + 1] = 0.0;
+    return;
+  }
   double du2 = 0.0, r2 = 0.0;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P.nmdf; q += (int64_t)gridDim.x * blockDim.x) {
     const double du = -x[q];
@@ -196,9 +203,9 @@ void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaSt
 }
 int newton_update_blocks(int64_t nmdf) { return (int)min64(256, (nmdf + 255) / 256); }
 void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
-                          double* part, double* out, cudaStream_t st) {
+                          double* part, double* out, cudaStream_t st, const int* skip) {
   const int blocks = newton_update_blocks(P.nmdf);
-  newton_update_kernel<<<blocks, 256, 0, st>>>(P, pp, dt, x, r, part);
+  newton_update_kernel<<<blocks, 256, 0, st>>>(P, pp, dt, x, r, part, skip);
   newton_norm_kernel<<<1, 32, 0, st>>>(part, blocks, P.nmdf, out);
 }
 int band_residual_blocks(int64_t n) { return (int)min64(304, (n + 255) / 256); }

@@ -44,7 +44,7 @@ struct PersistArgs {
   T* ab;
   BandLayout L;
   const int* ps;
-  int npan, kuf, rmax;
+  int npan, kuf, rmax, wmax;  // rmax = wmax + kl: rows of a staged panel column
   const int* blk_end;
   int* perm_all;
   T* rdiag;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
   constexpr int E = 16 / (int)sizeof(T);
   const int LDp = (a.rmax + 2 * E - 1) / E * E;
   T* Lp = reinterpret_cast<T*>(smem_raw);             // [kBlkW][LDp] (+64: chunk reads past R)
-  T* S = Lp + (size_t)kBlkW * LDp + 64;               // [4][LDp] column segments
+  T* S = Lp + (size_t)a.wmax * LDp + 64;              // [4][LDp] column segments
   T* Y = S + (size_t)4 * LDp;                         // [4][32]
   T* rd = Y + 128;                                    // [32]
   int* sp = reinterpret_cast<int*>(rd + 32);          // [32]
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
     // columns of this panel: the one of panel p + 1 first, then the others, then the right-hand side
     const int nown = cfirst < cend ? (int)((cend - 1 - cfirst) / GW) + 1 : 0;
     const int ncol = nown + (is_rhs ? 1 : 0);
-    if (ncol > kMaxCols) {  // grid too small for this band (the host setup rules this out)
+    if (ncol > kMaxCols || (nown > 1 && cfirst + GW < jn)) {  // grid too small (the host setup rules this out)
       if (tid == 0) atomicCAS(a.err, 0, 2);
       return;
     }
@@ -370,11 +370,11 @@ __global__ void __launch_bounds__(256, 1) blk_factor_persist_kernel(PersistArgs<
 // ---------------------------------------------------------------------------
 // host side
 template <class T>
-static size_t persist_smem(const BandLayout& L) {
+static size_t persist_smem(const BandLayout& L, int wmax) {
   constexpr int E = 16 / (int)sizeof(T);
-  const size_t rmax = (size_t)kBlkW + L.kl;
+  const size_t rmax = (size_t)wmax + L.kl;
   const size_t ldp = (rmax + 2 * E - 1) / E * E;
-  return ((size_t)kBlkW * ldp + 64 + 4 * ldp + 128 + 32) * sizeof(T) + 32 * sizeof(int);
+  return ((size_t)wmax * ldp + 64 + 4 * ldp + 128 + 32) * sizeof(T) + 32 * sizeof(int);
 }
 
 template <class T>
@@ -385,7 +385,7 @@ int blk_persist_setup(const BandLayout& L, const BlkPlan& B, BlkPersist& S) {
   cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-  const size_t sm = persist_smem<T>(L);
+  const size_t sm = persist_smem<T>(L, B.wmax);
   if (!coop || sm + 12 * 1024 > (size_t)cap || B.wmax > kBlkW) return 0;  // + static shared memory
   if (cudaFuncSetAttribute(blk_factor_persist_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) !=
       cudaSuccess)
@@ -396,7 +396,12 @@ int blk_persist_setup(const BandLayout& L, const BlkPlan& B, BlkPersist& S) {
   // workers need at most kMaxCols columns each per panel (columns c of the
   // trailing range, owned by c mod (G - 1), plus the right-hand side)
   S.grid = sms;
-  if ((int64_t)(S.grid - 2) * kMaxCols < (int64_t)B.kuf + kBlkW + 1) return S.grid = 0;
+  // workers: <= kMaxCols columns each per panel, and at least one per column of
+  // the widest panel (a worker owns at most one column of the next panel);
+  // + the right-hand-side CTA + the factorising CTA
+  S.min_grid = std::max((int)((B.kuf + B.wmax + 1 + kMaxCols - 1) / kMaxCols), B.wmax) + 2;
+  if (S.grid < S.min_grid) return S.grid = 0;
+  S.max_grid = S.grid;
   S.smem = sm;
   return S.grid;
 }
@@ -410,7 +415,8 @@ int blk_lu_factor_persist(T* ab, const BandLayout& L, const BlkPlan& B, const Bl
   a.ps = B.d_ps;
   a.npan = B.npan();
   a.kuf = B.kuf;
-  a.rmax = kBlkW + (int)L.kl;
+  a.rmax = B.wmax + (int)L.kl;
+  a.wmax = B.wmax;
   a.blk_end = B.d_blk_end;
   a.perm_all = perm_all;
   a.rdiag = rdiag;

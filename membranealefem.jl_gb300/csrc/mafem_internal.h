@@ -104,7 +104,7 @@ void launch_resid_gather(const DevPatch& P, int ndf, int nq, const double* r_el,
 void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaStream_t st);
 int newton_update_blocks(int64_t nmdf);
 void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
-                          double* part, double* out, cudaStream_t st);
+                          double* part, double* out, cudaStream_t st, const int* skip = nullptr);
 int band_residual_blocks(int64_t n);
 template <class T>
 void launch_band_residual(const T* a0, const BandLayout& L, const double* x, const double* r, double* res,
@@ -165,7 +165,9 @@ int blk_backward_grid();
 // Persistent cooperative factorisation (band_lu_persist.cu): launch shape and
 // per-panel flags.  Flags are zeroed once; epochs make them reusable.
 struct BlkPersist {
-  int grid = 0;
+  int grid = 0;            // CTAs of the launch: min_grid <= grid <= max_grid
+  int min_grid = 0;        // fewest CTAs that give every worker <= kMaxCols columns per panel
+  int max_grid = 0;        // the device's SM count
   size_t smem = 0;
   int* d_pdone = nullptr;
   int* d_critcnt = nullptr;

@@ -150,6 +150,10 @@ def lib():
         L.mafem_launch_count.restype = C.c_int64
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
         L.mafem_pull_force.argtypes = [vp, _PD]
+        L.mafem_set_launch_ctas.argtypes = [vp, C.c_int32]
+        L.mafem_batch_create.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(vp)]
+        L.mafem_batch_step.argtypes = [vp, _PD, _PD, C.POINTER(C.c_int32), C.POINTER(StepStats)]
+        L.mafem_batch_destroy.argtypes = [vp]
         L.mafem_profile_factor.argtypes = [vp, C.c_double, C.c_double, C.POINTER(KernelTimes)]
         L.mafem_probe_fp64_tflops.argtypes = [C.POINTER(C.c_double)]
         _lib = L
@@ -340,6 +344,10 @@ class Solver:
         _raise(lib().mafem_pull_force(self.h, _dp(f)), self.h)
         return f
 
+    def set_launch_ctas(self, ctas: int) -> int:
+        """CTAs of the persistent factorisation (0: all SMs); returns the value in use."""
+        return int(lib().mafem_set_launch_ctas(self.h, ctas))
+
     def set_lu_path(self, path: int) -> None:
         """Select the banded LU: LU_AUTO (default), LU_PANELS or LU_FULL."""
         _raise(lib().mafem_set_lu_path(self.h, path), self.h)
@@ -408,6 +416,40 @@ class Solver:
         self.last_stats = st.as_dict()
         _raise(rc, self.h)
         return self.last_stats
+
+
+class Batch:
+    """Many patches (Solver objects, any sizes, motions and precisions) stepped
+    together: each step is predictor + time_step! for every patch, their Newton
+    iterations interleaved on the GPU (mafem_batch_*).  Results equal each
+    Solver stepped alone.  The Solvers stay owned by the caller."""
+
+    def __init__(self, solvers, ctas: int = 0):
+        self.solvers = list(solvers)
+        arr = (C.c_void_p * len(self.solvers))(*[s.h for s in self.solvers])
+        self.b = C.c_void_p()
+        _raise(lib().mafem_batch_create(arr, len(self.solvers), ctas, C.byref(self.b)))
+
+    def step(self, times, dts):
+        """One time step of every patch; returns (statuses, list of step-stat dicts)."""
+        n = len(self.solvers)
+        times = np.ascontiguousarray(np.broadcast_to(times, (n,)), dtype=np.float64)
+        dts = np.ascontiguousarray(np.broadcast_to(dts, (n,)), dtype=np.float64)
+        status = (C.c_int32 * n)()
+        stats = (StepStats * n)()
+        lib().mafem_batch_step(self.b, _dp(times), _dp(dts), status, stats)
+        return [int(x) for x in status], [st.as_dict() for st in stats]
+
+    def close(self):
+        if self.b:
+            lib().mafem_batch_destroy(self.b)
+            self.b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def solve(p: Params, dts, t0: float = 0.0, precision: int = PLAIN_FP64, xms=None, cps=None):
