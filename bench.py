@@ -269,6 +269,111 @@ def run_gb300(args, rank, world, local, dist):
     return out
 
 
+# The batched form on a mixed set of patches.  Sizes stop at 32: from the flat
+# start with the reference's velocity-controlled pull, every 48x48 patch of this
+# mix loses Newton convergence on its first step (with full partial pivoting as
+# well as node-block pivoting), as do some 32x32 ALE patches with kb > 1.25 at
+# dt 0.01; dt 0.005 and half the pull speed keep the rest converging.  A patch
+# that still fails when stepped alone is left out of both measurements (counted).
+BATCH = dict(name="mixed batch: 256 independent tether-pull patches, n in {8,12,16,24,32} (seed 1), "
+                  "half LAG / half ALEVB, kb log-uniform [0.5, 2], pull speed 0.01 f/6 with f ~ U[2, 10], dt 0.005",
+             patches=256, sizes=(8, 12, 16, 24, 32), seed=1, dt=0.005)
+
+
+def batch_patches(M, wl=BATCH):
+    """The batch's patch set: (Params, Mesh, xms, cps) per patch, seeded."""
+    rng = np.random.default_rng(wl["seed"])
+    out = []
+    for k in range(wl["patches"]):
+        n = int(rng.choice(wl["sizes"]))
+        kb = float(np.exp(rng.uniform(np.log(0.5), np.log(2.0))))
+        f = float(rng.uniform(2.0, 10.0))
+        motion = M.LAG if k % 2 == 0 else M.ALEVB
+        p = M.Params(motion=motion, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, kb=kb,
+                     pull_speed=0.01 * f / 6.0)
+        mesh = M.Mesh(p)
+        _, xms, cps = M.prepare_input(p, mesh)
+        M.perturb_interior_z(mesh, xms, seed=k, amp=1e-4)
+        out.append((p, mesh, xms, cps))
+    return out
+
+
+def run_batched(steps, warmup, wl=BATCH):
+    """The same patches (a) one at a time through the plain FP64 path, each
+    factorisation on all SMs, and (b) as one batch (mafem_batch_step, each
+    patch's factorisation on its smallest grid).  Host wall clock around the
+    steps, device synchronised on both sides; patch time-steps/s.  Patches that
+    fail to converge when stepped alone are left out of both."""
+    import mafem as M
+    cu = Cudart()
+    patches = batch_patches(M, wl)
+    solvers = [M.Solver(mesh, p, M.PLAIN_FP64) for p, mesh, _, _ in patches]
+    dt = wl["dt"]
+    try:
+        # (a) one at a time
+        seq_ms, ok = 0.0, []
+        for i, (s, (p, mesh, x0, c0)) in enumerate(zip(solvers, patches)):
+            s.set_launch_ctas(0)
+            s.upload(x0, c0)
+            t, lat = 0.0, []
+            try:
+                for k in range(warmup + steps):
+                    t += dt
+                    cu.sync()
+                    h0 = time.perf_counter()
+                    s.predict(dt)
+                    s.time_step_resident(t, dt)
+                    cu.sync()
+                    if k >= warmup:
+                        lat.append((time.perf_counter() - h0) * 1e3)
+            except M.NewtonNotConverged:
+                continue
+            seq_ms += sum(lat)
+            ok.append(i)
+        seq_state = {i: solvers[i].download() for i in ok}
+        # (b) batched, from the same initial states
+        bsolvers = [solvers[i] for i in ok]
+        for i in ok:
+            solvers[i].upload(patches[i][2], patches[i][3])
+        with M.Batch(bsolvers) as b:
+            t, bat_lat, fails = 0.0, [], 0
+            for k in range(warmup + steps):
+                t += dt
+                cu.sync()
+                h0 = time.perf_counter()
+                status, _ = b.step(t, dt)
+                cu.sync()
+                fails += sum(1 for x in status if x != M.OK)
+                if k >= warmup:
+                    bat_lat.append((time.perf_counter() - h0) * 1e3)
+        err = 0.0
+        for i in ok:
+            xs, cs = seq_state[i]
+            xb, cb = solvers[i].download()
+            err = max(err, float(np.abs(xb - xs).max() / max(np.abs(xs).max(), 1e-300)),
+                      float(np.abs(cb - cs).max() / max(np.abs(cs).max(), 1e-300)))
+    finally:
+        for s in solvers:
+            s.close()
+    n = len(ok)
+    bat_ms = sum(bat_lat)
+    lat = sorted(bat_lat)
+    sizes = {}
+    for i in ok:
+        sizes[patches[i][0].num1el] = sizes.get(patches[i][0].num1el, 0) + 1
+    return {"workload": wl["name"], "patches": n, "patches_left_out_not_converging": len(patches) - n,
+            "steps": steps, "warmup": warmup,
+            "value": n * steps / (bat_ms / 1e3), "unit": "patch time-steps/s",
+            "one_at_a_time": {"value": n * steps / (seq_ms / 1e3), "unit": "patch time-steps/s",
+                              "form": "plain FP64, patches stepped one after another, all SMs each"},
+            "speedup_vs_one_at_a_time": seq_ms / bat_ms,
+            "p50_batch_step_ms": lat[len(lat) // 2], "p99_batch_step_ms": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+            "max_rel_diff_vs_one_at_a_time": err, "failed_patch_steps_in_batch": fails,
+            "size_histogram": {str(k): v for k, v in sorted(sizes.items())},
+            "form": "plain FP64, mafem_batch_step: every patch's Newton iteration enqueued on its own stream "
+                    "before any is waited for; host wall clock around each batch step"}
+
+
 def cpu_baseline(wl=WORKLOAD, max_seconds=20.0, max_steps=3):
     """The oracle's threaded complex-step assembly + scipy SuperLU (the stand-in for
     the reference's Julia calc_r_K + UMFPACK) on a bounded sample of the workload."""
@@ -301,6 +406,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
+    ap.add_argument("--batch-steps", type=int, default=2)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -366,6 +473,8 @@ def main():
                                   "rel_err_lambda": r["fp32"]["err_lam"]},
         "mesh": r["mesh"],
     }
+    if rank == 0 and not args.no_batch:
+        line["batched"] = run_batched(args.batch_steps, 1)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
