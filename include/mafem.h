@@ -173,6 +173,48 @@ int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, maf
  * element's nodes -> f_out[3].  The reference writes it to f-pull.txt after
  * each step of an F_PULL run (src/Analysis.jl:81-91). */
 int mafem_pull_force(mafem_handle* h, double* f_out);
+/* x_pull of the same f-pull.txt line (src/Analysis.jl:83-84): the mean of the
+ * pull element's nine node positions -> x_out[3]. */
+int mafem_pull_position(mafem_handle* h, double* x_out);
+
+/* ---- state files and checkpoints ---------------------------------------------------
+ * The files run_analysis! writes after every step with writedlm
+ * (src/Analysis.jl:75-78; the initial state at src/Input.jl:113-114) and
+ * prepare_input / restart read back with readdlm (src/Input.jl:35-37,
+ * src/MembraneAleFem.jl:75-107): "<dir>/t<t_id>-xms.txt" (numnp rows of 3) and
+ * "<dir>/t<t_id>-cps.txt" (numnp rows of ndf), one matrix row per line, entries
+ * separated by a tab, each Float64 printed as Julia's print does (shortest
+ * round-trip digits: "1.0", "0.0001", "100000.0", "1.0e-5", "1.0e6"), so a
+ * restart from these files continues bit for bit. */
+
+/* Julia's print(::Float64) into buf (NUL-terminated); returns its length, or
+ * MAFEM_ERR_ARG if cap is too small (32 bytes always suffice). */
+int mafem_format_double(double x, char* buf, int32_t cap);
+/* writedlm / readdlm of a column-major rows x cols matrix (a[i + rows*j]).
+ * readdlm accepts tabs or spaces between entries and fails (MAFEM_ERR_ARG, the
+ * message in mafem_last_error(NULL)) unless the file holds exactly that shape. */
+int mafem_writedlm(const char* path, const double* a, int64_t rows, int64_t cols);
+int mafem_readdlm(const char* path, double* a, int64_t rows, int64_t cols);
+/* Write the resident state as <dir>/t<t_id>-{xms,cps}.txt and wait for the files. */
+int mafem_write_state(mafem_handle* h, const char* dir, int64_t t_id);
+/* The same without waiting: the state (slot -1) or device snapshot `slot` is
+ * copied to pinned host memory on the handle's stream, after every step already
+ * enqueued, and a library thread writes the files while later steps run.
+ * Blocks only while three earlier writes are still pending. */
+int mafem_write_state_async(mafem_handle* h, int32_t slot, const char* dir, int64_t t_id);
+/* Wait for every pending write; returns the first write failure since the last flush. */
+int mafem_flush_state_writes(mafem_handle* h);
+/* readdlm both files into the resident state (restart, or prepare_input's
+ * in_path / in_xms / in_cps initial state). */
+int mafem_read_state(mafem_handle* h, const char* xms_file, const char* cps_file);
+/* Device-resident checkpoints (no reference counterpart): nslots copies of the
+ * state kept in HBM beside it.  mafem_snapshot copies the state into a slot and
+ * mafem_restore copies a slot back, both stream-ordered device-to-device copies
+ * that do not wait -- e.g. to retry a step with a smaller Δt after
+ * MAFEM_NEWTON_NOT_CONVERGED without a host round trip.  Reserve once per handle. */
+int mafem_snapshot_reserve(mafem_handle* h, int32_t nslots);
+int mafem_snapshot(mafem_handle* h, int32_t slot);
+int mafem_restore(mafem_handle* h, int32_t slot);
 
 /* ---- batching (no reference counterpart: the reference steps one patch) -----------
  * Many independent patches (handles of any sizes, motions and precisions) advance

@@ -116,6 +116,9 @@ struct mafem_handle {
   int fepoch = 0;          // epoch of the last persistent factorisation
   void* d_rdiag = nullptr;
   int64_t fallbacks = 0;
+  std::unique_ptr<StateWriter> writer;  // state files, created by the first write
+  double* d_snap = nullptr;             // device snapshots: nsnap x [xms | cps]
+  int nsnap = 0;
 };
 
 #define CK(x)                                                               \
@@ -509,6 +512,7 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
 extern "C" int mafem_destroy(mafem_handle* h) {
   if (!h) return MAFEM_OK;
   if (h->st) cudaStreamSynchronize(h->st);
+  h->writer.reset();  // finishes the pending state files
   for (void* p : h->allocs) cudaFree(p);
   if (h->h_out) cudaFreeHost(h->h_out);
   if (h->st2) cudaStreamSynchronize(h->st2);
@@ -1166,6 +1170,111 @@ extern "C" int mafem_pull_force(mafem_handle* h, double* f_out) {
       }
     }
   for (int c = 0; c < 3; ++c) f_out[c] = f[c];
+  return MAFEM_OK;
+}
+
+// x_pull of run_analysis! (src/Analysis.jl:83-84): the mean position of the
+// pull element's nine nodes, summed in IX order and divided by 9.
+extern "C" int mafem_pull_position(mafem_handle* h, double* x_out) {
+  if (!h || !x_out) return MAFEM_ERR_ARG;
+  const int pull = (h->numel + 1) / 2 - 1;
+  std::vector<double> xms((size_t)h->numnp * 3);
+  CK(cudaMemcpyAsync(xms.data(), h->P.xms, xms.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int c = 0; c < 3; ++c) {
+    double s = 0.0;
+    for (int a = 0; a < 9; ++a) s += xms[(size_t)c * h->numnp + h->h_ix[(size_t)pull * 9 + a]];
+    x_out[c] = s / 9.0;
+  }
+  return MAFEM_OK;
+}
+
+// ---- state files and device snapshots ------------------------------------------
+// The files run_analysis! writes after each step (src/Analysis.jl:75-78) and
+// restart / prepare_input read (src/MembraneAleFem.jl:75-107,
+// src/Input.jl:35-37); the formatting and the writer thread are in
+// state_io.cpp.
+
+static int snap_ptrs(mafem_handle* h, int32_t slot, double** xms, double** cps) {
+  if (slot == -1) {
+    *xms = h->P.xms;
+    *cps = h->P.cps;
+    return MAFEM_OK;
+  }
+  if (slot < 0 || slot >= h->nsnap) {
+    h->err = "snapshot slot " + std::to_string(slot) + " out of range (" + std::to_string(h->nsnap) + " reserved)";
+    return MAFEM_ERR_ARG;
+  }
+  const size_t per = (size_t)h->numnp * (3 + h->ndf);
+  *xms = h->d_snap + per * slot;
+  *cps = *xms + (size_t)h->numnp * 3;
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_write_state_async(mafem_handle* h, int32_t slot, const char* dir, int64_t t_id) {
+  if (!h || !dir) return MAFEM_ERR_ARG;
+  double *xms, *cps;
+  int rc = snap_ptrs(h, slot, &xms, &cps);
+  if (rc) return rc;
+  if (!h->writer) {
+    auto w = std::make_unique<StateWriter>();
+    rc = w->init(h->numnp, h->ndf, 3, h->err);
+    if (rc) return rc;
+    h->writer = std::move(w);
+  }
+  return h->writer->submit(xms, cps, h->st, state_file(dir, t_id, "xms"), state_file(dir, t_id, "cps"), h->err);
+}
+
+extern "C" int mafem_flush_state_writes(mafem_handle* h) {
+  if (!h) return MAFEM_ERR_ARG;
+  return h->writer ? h->writer->flush(h->err) : MAFEM_OK;
+}
+
+extern "C" int mafem_write_state(mafem_handle* h, const char* dir, int64_t t_id) {
+  const int rc = mafem_write_state_async(h, -1, dir, t_id);
+  const int rf = h ? mafem_flush_state_writes(h) : MAFEM_ERR_ARG;
+  return rc ? rc : rf;
+}
+
+extern "C" int mafem_read_state(mafem_handle* h, const char* xms_file, const char* cps_file) {
+  if (!h || !xms_file || !cps_file) return MAFEM_ERR_ARG;
+  std::vector<double> xms((size_t)h->numnp * 3), cps((size_t)h->numnp * h->ndf);
+  int rc = readdlm(xms_file, xms.data(), h->numnp, 3, h->err);
+  if (!rc) rc = readdlm(cps_file, cps.data(), h->numnp, h->ndf, h->err);
+  if (rc) return rc;
+  return mafem_upload_state(h, xms.data(), cps.data());
+}
+
+extern "C" int mafem_snapshot_reserve(mafem_handle* h, int32_t nslots) {
+  if (!h || nslots < 1) return MAFEM_ERR_ARG;
+  if (h->nsnap) {
+    if (nslots == h->nsnap) return MAFEM_OK;
+    h->err = "snapshots are already reserved with another slot count";
+    return MAFEM_ERR_ARG;
+  }
+  const int rc = dalloc(h, &h->d_snap, (size_t)nslots * h->numnp * (3 + h->ndf));
+  if (rc) return rc;
+  h->nsnap = nslots;
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_snapshot(mafem_handle* h, int32_t slot) {
+  if (!h || slot < 0) return MAFEM_ERR_ARG;
+  double *xms, *cps;
+  const int rc = snap_ptrs(h, slot, &xms, &cps);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(xms, h->P.xms, sizeof(double) * h->numnp * 3, cudaMemcpyDeviceToDevice, h->st));
+  CK(cudaMemcpyAsync(cps, h->P.cps, sizeof(double) * h->numnp * h->ndf, cudaMemcpyDeviceToDevice, h->st));
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_restore(mafem_handle* h, int32_t slot) {
+  if (!h || slot < 0) return MAFEM_ERR_ARG;
+  double *xms, *cps;
+  const int rc = snap_ptrs(h, slot, &xms, &cps);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(h->P.xms, xms, sizeof(double) * h->numnp * 3, cudaMemcpyDeviceToDevice, h->st));
+  CK(cudaMemcpyAsync(h->P.cps, cps, sizeof(double) * h->numnp * h->ndf, cudaMemcpyDeviceToDevice, h->st));
   return MAFEM_OK;
 }
 

@@ -30,6 +30,15 @@ struct HostMesh {
   std::vector<double> dir_val;
 };
 
+// ---- state files (state_io.cpp) -------------------------------------------------
+// Julia's print(::Float64), appended to out.
+void format_double(double x, std::string& out);
+// writedlm / readdlm of a column-major rows x cols matrix (a[i + rows*j]).
+int writedlm(const char* path, const double* a, int64_t rows, int64_t cols, std::string& err);
+int readdlm(const char* path, double* a, int64_t rows, int64_t cols, std::string& err);
+// "<dir>/t<t_id>-<which>.txt", the names run_analysis! writes.
+std::string state_file(const char* dir, int64_t t_id, const char* which);
+
 int build_mesh(const mafem_params& p, const mafem_args& a, HostMesh& m, std::string& err);
 void mesh_desc(const HostMesh& m, mafem_mesh_desc& d);
 int prepare_input(const HostMesh& m, const mafem_params& p, double* xms, double* cps, std::string& err);
@@ -189,4 +198,42 @@ int blk_lu_factor_persist(T* ab, const BandLayout& L, const BlkPlan& B, const Bl
                           T* rdiag, int* info, T* rhs, int* err, cudaStream_t st, long long* trace = nullptr);
 template <class V, class T>
 void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, cudaStream_t st);
+}  // namespace mafem
+
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <thread>
+namespace mafem {
+// Writes state files off the time loop's critical path: submit() copies
+// device xms / cps into a free pinned slot on stream st and returns; a thread
+// waits for that copy and writes the two files.  submit() blocks only while
+// every slot is still being written.  flush() waits for all pending files and
+// returns the first failure since the previous flush.
+class StateWriter {
+ public:
+  ~StateWriter();
+  int init(int numnp, int ndf, int depth, std::string& err);
+  int submit(const double* d_xms, const double* d_cps, cudaStream_t st, std::string xms_path,
+             std::string cps_path, std::string& err);
+  int flush(std::string& err);
+
+ private:
+  struct Slot {
+    double* host = nullptr;  // pinned: xms (numnp x 3) then cps (numnp x ndf)
+    cudaEvent_t ev = nullptr;
+    bool busy = false;
+    std::string xms_path, cps_path;
+  };
+  void run();
+  int numnp_ = 0, ndf_ = 0, device_ = 0;
+  std::vector<Slot> slots_;
+  std::deque<int> queue_;
+  std::mutex mu_;
+  std::condition_variable cv_job_, cv_free_;
+  bool stop_ = false;
+  int first_rc_ = 0;
+  std::string first_err_;
+  std::thread th_;
+};
 }  // namespace mafem

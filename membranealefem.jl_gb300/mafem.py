@@ -150,6 +150,17 @@ def lib():
         L.mafem_launch_count.restype = C.c_int64
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
         L.mafem_pull_force.argtypes = [vp, _PD]
+        L.mafem_pull_position.argtypes = [vp, _PD]
+        L.mafem_format_double.argtypes = [C.c_double, C.c_char_p, C.c_int32]
+        L.mafem_writedlm.argtypes = [C.c_char_p, _PD, C.c_int64, C.c_int64]
+        L.mafem_readdlm.argtypes = [C.c_char_p, _PD, C.c_int64, C.c_int64]
+        L.mafem_write_state.argtypes = [vp, C.c_char_p, C.c_int64]
+        L.mafem_write_state_async.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int64]
+        L.mafem_flush_state_writes.argtypes = [vp]
+        L.mafem_read_state.argtypes = [vp, C.c_char_p, C.c_char_p]
+        L.mafem_snapshot_reserve.argtypes = [vp, C.c_int32]
+        L.mafem_snapshot.argtypes = [vp, C.c_int32]
+        L.mafem_restore.argtypes = [vp, C.c_int32]
         L.mafem_set_launch_ctas.argtypes = [vp, C.c_int32]
         L.mafem_batch_create.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(vp)]
         L.mafem_batch_step.argtypes = [vp, _PD, _PD, C.POINTER(C.c_int32), C.POINTER(StepStats)]
@@ -171,6 +182,43 @@ def _raise(rc: int, h=None):
     if rc == NEWTON_NOT_CONVERGED:
         raise NewtonNotConverged(msg)
     raise MafemError(rc, msg)
+
+
+# ---- state files (src/Analysis.jl:75-78, src/Input.jl:35-37) -------------------------
+
+F_PULL_HEADER = "time\txp\typ\tzp\tfx\tfy\tfz"  # first line of f-pull.txt (Analysis.jl:52-54)
+
+
+def format_double(x: float) -> str:
+    """Julia's print(::Float64): shortest round-trip digits, "1.0", "1.0e-5", "1.0e6"."""
+    buf = C.create_string_buffer(32)
+    n = lib().mafem_format_double(float(x), buf, 32)
+    if n < 0:
+        raise MafemError(n, "format_double")
+    return buf.value.decode()
+
+
+def writedlm(path: str, a) -> None:
+    """DelimitedFiles.writedlm of a Float64 matrix (tab-separated rows)."""
+    a = np.asfortranarray(np.atleast_2d(np.asarray(a, dtype=np.float64)))
+    _raise(lib().mafem_writedlm(os.fsencode(path), _dp(a), a.shape[0], a.shape[1]))
+
+
+def readdlm(path: str, rows: int, cols: int) -> np.ndarray:
+    """DelimitedFiles.readdlm of a rows x cols Float64 matrix (the shape is checked)."""
+    a = np.zeros((rows, cols), order="F")
+    _raise(lib().mafem_readdlm(os.fsencode(path), _dp(a), rows, cols))
+    return a
+
+
+def state_files(dir_: str, t_id: int) -> tuple[str, str]:
+    """The names run_analysis! writes: <dir>/t<t_id>-xms.txt, <dir>/t<t_id>-cps.txt."""
+    return (os.path.join(dir_, f"t{t_id}-xms.txt"), os.path.join(dir_, f"t{t_id}-cps.txt"))
+
+
+def f_pull_line(rec) -> str:
+    """One line of f-pull.txt (Analysis.jl:86-90): time, x_pull[3], f_pull[3]."""
+    return "\t".join(format_double(v) for v in rec)
 
 
 @dataclass
@@ -343,6 +391,43 @@ class Solver:
         f = np.zeros(3)
         _raise(lib().mafem_pull_force(self.h, _dp(f)), self.h)
         return f
+
+    def pull_position(self) -> np.ndarray:
+        """x_pull (Analysis.jl:83-84): mean position of the pull element's nine nodes."""
+        x = np.zeros(3)
+        _raise(lib().mafem_pull_position(self.h, _dp(x)), self.h)
+        return x
+
+    def pull_record(self, time: float) -> list:
+        """The f-pull.txt record of run_analysis! (Analysis.jl:81-91) at `time`."""
+        return [float(time), *self.pull_position(), *self.pull_force()]
+
+    def write_state(self, dir_: str, t_id: int) -> None:
+        """writedlm of xms / cps to <dir>/t<t_id>-{xms,cps}.txt; waits for the files."""
+        _raise(lib().mafem_write_state(self.h, os.fsencode(dir_), t_id), self.h)
+
+    def write_state_async(self, dir_: str, t_id: int, slot: int = -1) -> None:
+        """Queue the same files (of the state, or of snapshot `slot`) for the library's
+        writer thread; the copy is ordered after the steps already enqueued."""
+        _raise(lib().mafem_write_state_async(self.h, slot, os.fsencode(dir_), t_id), self.h)
+
+    def flush_state_writes(self) -> None:
+        _raise(lib().mafem_flush_state_writes(self.h), self.h)
+
+    def read_state(self, xms_file: str, cps_file: str) -> None:
+        """readdlm both files into the resident state (restart, MembraneAleFem.jl:75-107)."""
+        _raise(lib().mafem_read_state(self.h, os.fsencode(xms_file), os.fsencode(cps_file)), self.h)
+
+    def snapshot_reserve(self, nslots: int) -> None:
+        _raise(lib().mafem_snapshot_reserve(self.h, nslots), self.h)
+
+    def snapshot(self, slot: int) -> None:
+        """Copy the state into device snapshot `slot` (stream-ordered, does not wait)."""
+        _raise(lib().mafem_snapshot(self.h, slot), self.h)
+
+    def restore(self, slot: int) -> None:
+        """Copy device snapshot `slot` back into the state (stream-ordered)."""
+        _raise(lib().mafem_restore(self.h, slot), self.h)
 
     def set_launch_ctas(self, ctas: int) -> int:
         """CTAs of the persistent factorisation (0: all SMs); returns the value in use."""

@@ -534,3 +534,45 @@ def time_step_sparse(mesh: Mesh, xms, cps, time: float, dt: float, nthreads: int
     if not eps[-1] < mesh.p.eps_nr:
         raise AssertionFailed("did not reach Newton--Raphson tolerance")
     return eps
+
+
+# ---- state files ---------------------------------------------------------------------
+# The reference writes xms / cps with DelimitedFiles.writedlm (src/Analysis.jl:76-77,
+# src/Input.jl:113-114): print(io, x) of each Float64, '\t' between the entries of a
+# row, '\n' after each row.  print(::Float64) is Julia Base's Ryu shortest printer
+# (base/ryu/shortest.jl, `writeshortest`; Julia 1.10, the reference's compat): the
+# shortest digit string that reads back to x, closest to x, written in fixed notation
+# when the decimal point position pt (x = 0.d1d2... x 10^pt) satisfies -4 < pt <= 6,
+# else as d.ddd "e" exponent, with ".0" when there is a single digit.  This restatement
+# takes the digits from Python's repr, which produces the same shortest-closest digits.
+
+def julia_print_float64(x: float) -> str:
+    """print(::Float64) of Julia Base (base/ryu/shortest.jl), restated."""
+    import math
+    x = float(x)
+    if math.isnan(x):
+        return "NaN"
+    if math.isinf(x):
+        return "Inf" if x > 0 else "-Inf"
+    if x == 0.0:
+        return "-0.0" if math.copysign(1.0, x) < 0 else "0.0"
+    sign = "-" if x < 0 else ""
+    mant, _, ex = f"{abs(x)!r}".partition("e")  # repr: '123.45', '1e-05', '1.5e+16'
+    exp10 = int(ex) if ex else 0
+    ip, _, fp = mant.partition(".")
+    digits = (ip + fp).lstrip("0")
+    pt = len(ip.lstrip("0")) + exp10 if ip.strip("0") else exp10 - (len(fp) - len(fp.lstrip("0")))
+    digits = digits.rstrip("0") or "0"
+    if -4 < pt <= 6:
+        if pt <= 0:
+            return sign + "0." + "0" * (-pt) + digits
+        if pt >= len(digits):
+            return sign + digits + "0" * (pt - len(digits)) + ".0"
+        return sign + digits[:pt] + "." + digits[pt:]
+    return sign + digits[0] + "." + (digits[1:] or "0") + "e" + str(pt - 1)
+
+
+def writedlm_text(a) -> str:
+    """The text writedlm produces for a Float64 matrix (rows joined by '\\n')."""
+    a = np.atleast_2d(np.asarray(a, dtype=np.float64))
+    return "".join("\t".join(julia_print_float64(v) for v in row) + "\n" for row in a)
