@@ -36,6 +36,24 @@ def test_calc_r_K_matches_oracle(motion, scenario, n1, n2):
     assert np.all(ab[:, :kl] == 0.0)  # pivoting-fill rows start empty
 
 
+@pytest.mark.parametrize("motion,scenario,n1,n2", ASSEMBLY_CASES)
+def test_fp32_form_assembly_matches_oracle(motion, scenario, n1, n2):
+    """FP32 form: the FP64 residual kernel (one thread per element and Gauss
+    point) to the plain form's 1e-12; the all-FP32 tangent to 2e-5 of the
+    largest entry (FP32 rounding of primal and tangent arithmetic)."""
+    p, q = params_pair(motion, scenario, n1, n2, bend_mf=0.5, bend_tm=2.0)
+    mesh, om = M.Mesh(p), O.Mesh(q)
+    xms, cps = state(p, mesh, seed=3, amp=2e-2, vel_amp=0.05)
+    time, dt = 0.37, 0.01
+    with M.Solver(mesh, p, M.FP32_REFINE) as s:
+        r, ab = s.calc_r_K(xms, cps, time, dt)
+    r0, ab0 = om.calc_r_K(xms, cps, time, dt, nthreads=4)
+    kl = mesh.half_bw
+    assert rel(r, r0) < 1e-12
+    assert rel(ab[:, kl:], ab0[:, kl:]) < 2e-5
+    assert np.all(ab[:, :kl] == 0.0)
+
+
 def test_tangent_is_the_derivative_of_the_residual():
     """Central differences of the GPU residual against the GPU tangent."""
     p, _ = params_pair(M.ALEVB, M.F_PULL, 5, 4)
