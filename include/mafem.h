@@ -232,6 +232,13 @@ int mafem_batch_create(mafem_handle* const* handles, int32_t n, int32_t ctas, ma
 int mafem_batch_step(mafem_batch* b, const double* times, const double* dts, int32_t* status,
                      mafem_step_stats* stats);
 int mafem_batch_destroy(mafem_batch* b);
+/* FP32 + refinement patches whose band fits one CTA's shared memory are, by
+ * default, factored and solved together: one launch factors every such patch
+ * (one CTA each, largest first) and one more runs their FP32 triangular
+ * solves and FP64 iterative refinement.  on = 0 steps them like the other
+ * patches instead (each with its own multi-CTA factorisation).  Returns 1 if
+ * the batched solve is in use. */
+int mafem_batch_set_patch_solve(mafem_batch* b, int32_t on);
 /* CTAs of this handle's persistent factorisation and back substitution (0: all
  * SMs); clamped to what the band needs.  Returns the CTAs the factorisation uses. */
 int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas);
@@ -240,6 +247,13 @@ int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas);
 
 /* Number of kernels this handle has enqueued since mafem_create. */
 int64_t mafem_launch_count(const mafem_handle* h);
+
+/* FP32 form: FP64 iterative refinement of each linear solve stops when
+ * |r - A x| <= tol |r| (default 1e-10) or after max_sweeps sweeps (default 30;
+ * MAFEM_REFINE_STALLED).  A looser tol trades refinement sweeps for Newton
+ * iterations: the Newton criterion (FiniteElement.jl:48) still decides
+ * convergence on the FP64 residual. */
+int mafem_set_refinement(mafem_handle* h, int32_t max_sweeps, double tol);
 
 /* Select the banded LU (enum mafem_lu_path) for the following factorisations.
  * MAFEM_ERR_UNSUPPORTED if the handle cannot run that path (e.g. the node-block

@@ -16,7 +16,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmafem.so")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["mesh.cpp", "elem.cu", "assemble.cu", "band_lu.cu", "band_lu_blk.cu", "band_lu_persist.cu", "api.cu", "noalloc.cu", "state_io.cpp"]
+SOURCES = ["mesh.cpp", "elem.cu", "assemble.cu", "band_lu.cu", "band_lu_blk.cu", "band_lu_persist.cu", "band_lu_patch.cu", "api.cu", "noalloc.cu", "state_io.cpp"]
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]

@@ -116,6 +116,11 @@ struct mafem_handle {
   int fepoch = 0;          // epoch of the last persistent factorisation
   void* d_rdiag = nullptr;
   int64_t fallbacks = 0;
+  // batched FP32 form (band_lu_patch.cu): the handle's job, usable when its band fits
+  float* d_inv = nullptr;
+  bool patch_ok = false;
+  bool ss_patch = false;  // the iteration in progress ran through a batch's patch solve
+  PatchJob job{};
   std::unique_ptr<StateWriter> writer;  // state files, created by the first write
   double* d_snap = nullptr;             // device snapshots: nsnap x [xms | cps]
   int nsnap = 0;
@@ -485,6 +490,31 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     mafem_destroy(hp.release());
     return MAFEM_ERR_OOM;
   }
+  if (precision != MAFEM_PLAIN_FP64 && h->use_blk) {
+    const int dyn = patch_solve_setup();
+    cudaGetLastError();
+    if (dyn > 0 && patch_factor_smem(h->L.kl) <= (size_t)dyn && patch_refine_smem(n) <= (size_t)dyn) {
+      AL(h->d_inv, (size_t)h->blk.npan() * 2 * kBlkW * kBlkW);
+      PatchJob& J = h->job;
+      J.band = (float*)h->d_band;
+      J.band0 = (const float*)h->d_band0;
+      J.inv = h->d_inv;
+      J.ps = h->blk.d_ps;
+      J.blk_end = h->d_blk_end;
+      J.perm = h->d_perm;
+      J.rdiag = (float*)h->d_rdiag;
+      J.info = h->d_info;
+      J.stat = h->d_info + 2;
+      J.rhs = h->d_r;
+      J.x = h->d_x;
+      J.res = h->d_res;
+      J.xs = reinterpret_cast<float2*>(h->d_dx);  // d_dx: n doubles, unused by this form
+      J.L = h->L;
+      J.kuf = h->blk.kuf;
+      J.npan = h->blk.npan();
+      h->patch_ok = true;
+    }
+  }
   DevPatch& P = h->P;
   P.numel = numel; P.numnp = numnp; P.num1el = (int)d->num1el; P.num2el = (int)d->num2el;
   P.num1np = (int)d->num1np; P.num2np = (int)d->num2np; P.nmdf = n;
@@ -551,7 +581,7 @@ extern "C" int mafem_download_state(mafem_handle* h, double* xms, double* cps) {
 }
 
 // element kernel + gathers: r -> d_r, K -> d_band
-static int assemble(mafem_handle* h, double time, double dt) {
+static int assemble(mafem_handle* h, double time, double dt, bool both_bands = false) {
   cudaError_t e;
   if (h->precision == MAFEM_PLAIN_FP64) {
     e = launch_elem<double>(h->P, h->pp, time, dt, h->d_rel, (double*)h->d_Kel, h->st);
@@ -567,7 +597,8 @@ static int assemble(mafem_handle* h, double time, double dt) {
       h->err = std::string("element kernel: ") + cudaGetErrorString(e);
       return MAFEM_ERR_CUDA;
     }
-    launch_band_gather<float>(h->P, h->ndf, h->nq, h->L, (const float*)h->d_Kel, (float*)h->d_band, h->st);
+    launch_band_gather<float>(h->P, h->ndf, h->nq, h->L, (const float*)h->d_Kel, (float*)h->d_band, h->st,
+                              both_bands ? (float*)h->d_band0 : nullptr);
     h->launches += 2;
   }
   launch_resid_gather(h->P, h->ndf, h->nq, h->d_rel, h->d_r, h->st);
@@ -856,6 +887,7 @@ static void step_begin(mafem_handle* h, double time, double dt) {
 // other forms run factor_and_solve, which waits where it must.
 static int iter_enqueue(mafem_handle* h) {
   const int64_t n = h->nmdf;
+  h->ss_patch = false;
   cudaEventRecord(h->ev[0], h->st);
   int rc = assemble(h, h->ss_time, h->ss_dt);
   if (rc) return rc;
@@ -875,7 +907,37 @@ static int iter_enqueue(mafem_handle* h) {
   h->launches += 2;
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  cudaEventRecord(h->ev[4], h->st);
+  return MAFEM_OK;
+}
+
+// Batched FP32 form, first half of a Newton iteration: assembly into both
+// bands (the factorisation overwrites one, the refinement multiplies by the
+// other).  The batch then factors and solves every patch in one launch each
+// (patch_solve) and iter_enqueue_patch_end applies the update.
+static int iter_enqueue_patch_begin(mafem_handle* h) {
+  h->ss_patch = true;
+  h->ss_async = false;
+  h->ss_sweeps = 0;
+  cudaEventRecord(h->ev[0], h->st);
+  int rc = assemble(h, h->ss_time, h->ss_dt, true);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(h->d_info, 0, 4 * sizeof(int), h->st));
+  cudaEventRecord(h->ev[1], h->st);
+  return MAFEM_OK;
+}
+
+static int iter_enqueue_patch_end(mafem_handle* h, cudaEvent_t solved) {
+  CK(cudaStreamWaitEvent(h->st, solved, 0));
+  cudaEventRecord(h->ev[2], h->st);
+  cudaEventRecord(h->ev[3], h->st);
+  // the update is skipped when the patch solve failed (status word nonzero)
+  launch_newton_update(h->P, h->pp, h->ss_dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st, h->d_info + 2);
+  h->launches += 2;
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   cudaEventRecord(h->ev[4], h->st);
   return MAFEM_OK;
 }
@@ -897,6 +959,23 @@ enum { kIterAgain = -100, kIterDone = -101 };
 static int iter_finish(mafem_handle* h) {
   CK(cudaEventSynchronize(h->ev[4]));
   accum_times(h);
+  if (h->ss_patch) {
+    int ps[4];
+    std::memcpy(ps, h->h_out + 5, sizeof ps);
+    h->ss_sweeps = ps[3];
+    if (ps[2] != MAFEM_OK) {
+      // the patch solve found no usable pivot in a node block, or its
+      // refinement failed: the update was skipped; redo this iteration with
+      // the handle's own solve (full partial pivoting where needed)
+      ++h->fallbacks;
+      const int sw = h->ss_sweeps;
+      const int rc = iter_enqueue(h);
+      if (rc) return rc;
+      CK(cudaEventSynchronize(h->ev[4]));
+      accum_times(h);
+      h->ss_sweeps += sw;
+    }
+  }
   int info[2] = {0, 0};
   std::memcpy(info, h->h_out + 5, sizeof info);
   if (info[1] == 0 && info[0] != 0 && h->ss_async) {
@@ -964,6 +1043,26 @@ extern "C" int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas) {
 
 struct mafem_batch {
   std::vector<mafem_handle*> hs;
+  // batched FP32 solve: the handles whose band fits one CTA (patch_ok)
+  bool patch_on = false;
+  std::vector<int> slot;  // per handle: its job index, or -1
+  std::vector<double> cost;
+  PatchJob* d_jobs = nullptr;
+  int* d_order = nullptr;
+  int* h_order = nullptr;  // pinned
+  cudaStream_t bst = nullptr;
+  cudaEvent_t bev = nullptr;
+  size_t smem_f = 0, smem_r = 0;
+  int max_sweeps = 30;
+  double tol = 1e-10;
+  ~mafem_batch() {
+    if (bst) cudaStreamSynchronize(bst);
+    if (d_jobs) cudaFree(d_jobs);
+    if (d_order) cudaFree(d_order);
+    if (h_order) cudaFreeHost(h_order);
+    if (bev) cudaEventDestroy(bev);
+    if (bst) cudaStreamDestroy(bst);
+  }
 };
 
 extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ctas, mafem_batch** out) {
@@ -972,6 +1071,7 @@ extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ct
     return MAFEM_ERR_ARG;
   }
   auto b = std::make_unique<mafem_batch>();
+  std::vector<PatchJob> jobs;
   for (int i = 0; i < n; ++i) {
     if (!hs[i]) {
       set_global_error("mafem_batch_create: null handle");
@@ -982,13 +1082,43 @@ extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ct
         set_global_error("mafem_batch_create: a handle appears twice");
         return MAFEM_ERR_ARG;
       }
-    b->hs.push_back(hs[i]);
+    mafem_handle* h = hs[i];
+    b->hs.push_back(h);
     // ctas == 0: each patch's smallest persistent grid, so that many patches' factorisations fit at once
-    const int c = ctas > 0 ? ctas : std::max(1, hs[i]->pers.min_grid);
-    mafem_set_launch_ctas(hs[i], c);
+    const int c = ctas > 0 ? ctas : std::max(1, h->pers.min_grid);
+    mafem_set_launch_ctas(h, c);
+    if (h->patch_ok) {
+      b->slot.push_back((int)jobs.size());
+      jobs.push_back(h->job);
+      b->cost.push_back((double)h->blk.npan() * h->L.kl * h->blk.kuf);
+      b->smem_f = std::max(b->smem_f, patch_factor_smem(h->L.kl));
+      b->smem_r = std::max(b->smem_r, patch_refine_smem(h->L.n));
+    } else {
+      b->slot.push_back(-1);
+    }
+  }
+  if (!jobs.empty()) {
+    const size_t nj = jobs.size();
+    cudaError_t e = cudaMalloc(&b->d_jobs, nj * sizeof(PatchJob));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_order, nj * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_order, nj * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_jobs, jobs.data(), nj * sizeof(PatchJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->bst, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->bev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+      set_global_error(std::string("mafem_batch_create: ") + cudaGetErrorString(e));
+      return MAFEM_ERR_CUDA;
+    }
+    b->patch_on = true;
   }
   *out = b.release();
   return MAFEM_OK;
+}
+
+extern "C" int mafem_batch_set_patch_solve(mafem_batch* b, int32_t on) {
+  if (!b) return MAFEM_ERR_ARG;
+  b->patch_on = on != 0 && b->d_jobs != nullptr;
+  return b->patch_on ? 1 : 0;
 }
 
 extern "C" int mafem_batch_destroy(mafem_batch* b) {
@@ -998,7 +1128,10 @@ extern "C" int mafem_batch_destroy(mafem_batch* b) {
 
 // One time step of every patch: predictor + Newton, the patches' iterations
 // interleaved -- every active patch's iteration k is enqueued (each handle on
-// its own stream) before any is waited for, so their kernels overlap.
+// its own stream) before any is waited for, so their kernels overlap.  FP32
+// patches whose band fits one CTA are factored and solved together: after
+// their assemblies, one launch factors all of them and one more solves and
+// refines all of them (one CTA per patch, largest first).
 extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const double* dts, int32_t* status,
                                 mafem_step_stats* stats) {
   if (!b || !times || !dts) return MAFEM_ERR_ARG;
@@ -1011,11 +1144,47 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
     step_begin(h, times[i], dts[i]);
     active.push_back(i);
   }
+  std::vector<int> pj;
   while (!active.empty()) {
     std::vector<int> next;
+    pj.clear();
     for (int i : active) {
-      const int rc = iter_enqueue(b->hs[i]);
-      if (rc != MAFEM_OK) st[i] = rc;
+      mafem_handle* h = b->hs[i];
+      const bool patch = b->patch_on && b->slot[i] >= 0;
+      const int rc = patch ? iter_enqueue_patch_begin(h) : iter_enqueue(h);
+      if (rc != MAFEM_OK)
+        st[i] = rc;
+      else if (patch)
+        pj.push_back(i);
+    }
+    if (!pj.empty()) {
+      std::sort(pj.begin(), pj.end(), [&](int x, int y) { return b->cost[b->slot[x]] > b->cost[b->slot[y]]; });
+      // one launch serves every patch: the strictest tolerance and the largest sweep cap among them
+      b->max_sweeps = 1;
+      b->tol = 1.0;
+      for (int i : pj) {
+        b->max_sweeps = std::max(b->max_sweeps, b->hs[i]->max_refine);
+        b->tol = std::min(b->tol, b->hs[i]->refine_tol);
+      }
+      for (size_t k = 0; k < pj.size(); ++k) {
+        b->h_order[k] = b->slot[pj[k]];
+        cudaStreamWaitEvent(b->bst, b->hs[pj[k]]->ev[1], 0);
+      }
+      cudaError_t e = cudaMemcpyAsync(b->d_order, b->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice, b->bst);
+      if (e == cudaSuccess)
+        e = patch_solve(b->d_jobs, b->d_order, (int)pj.size(), b->smem_f, b->smem_r, b->max_sweeps, b->tol, b->bst);
+      if (e == cudaSuccess) e = cudaEventRecord(b->bev, b->bst);
+      for (int i : pj) {
+        mafem_handle* h = b->hs[i];
+        if (e != cudaSuccess) {
+          h->err = std::string("batched FP32 solve: ") + cudaGetErrorString(e);
+          st[i] = MAFEM_ERR_CUDA;
+          continue;
+        }
+        if (i == pj[0]) h->launches += 2;  // the two batched launches, counted once
+        const int rc = iter_enqueue_patch_end(h, b->bev);
+        if (rc != MAFEM_OK) st[i] = rc;
+      }
     }
     for (int i : active) {
       if (st[i] != MAFEM_OK) continue;
@@ -1275,6 +1444,13 @@ extern "C" int mafem_restore(mafem_handle* h, int32_t slot) {
   if (rc) return rc;
   CK(cudaMemcpyAsync(h->P.xms, xms, sizeof(double) * h->numnp * 3, cudaMemcpyDeviceToDevice, h->st));
   CK(cudaMemcpyAsync(h->P.cps, cps, sizeof(double) * h->numnp * h->ndf, cudaMemcpyDeviceToDevice, h->st));
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_set_refinement(mafem_handle* h, int32_t max_sweeps, double tol) {
+  if (!h || max_sweeps < 1 || max_sweeps > 1000 || !(tol > 0.0) || !(tol < 1.0)) return MAFEM_ERR_ARG;
+  h->max_refine = max_sweeps;
+  h->refine_tol = tol;
   return MAFEM_OK;
 }
 

@@ -27,7 +27,7 @@ __host__ __device__ __forceinline__ int64_t max64(int64_t a, int64_t b) { return
 // so the band needs no separate clearing pass.
 template <class T>
 __global__ void band_gather_kernel(DevPatch P, int ndf, int nq, BandLayout L, const T* __restrict__ K_el,
-                                   T* __restrict__ ab) {
+                                   T* __restrict__ ab, T* __restrict__ ab2) {
   for (int64_t j = blockIdx.y; j < L.n; j += gridDim.y) {
     const int NJ = P.unk_node[j], dj = P.unk_dof[j];
     const int s1J = NJ % P.num1np, s2J = NJ / P.num1np;
@@ -50,6 +50,7 @@ __global__ void band_gather_kernel(DevPatch P, int ndf, int nq, BandLayout L, co
         }
       }
       ab[j * L.ldb + s] = val;
+      if (ab2) ab2[j * L.ldb + s] = val;  // the unfactored copy the refinement multiplies by
     }
   }
 }
@@ -189,9 +190,9 @@ __global__ void axpy_kernel(int64_t n, const double* __restrict__ dx, double* __
 // ---- launchers -------------------------------------------------------------------
 template <class T>
 void launch_band_gather(const DevPatch& P, int ndf, int nq, const BandLayout& L, const T* K_el, T* ab,
-                        cudaStream_t st) {
+                        cudaStream_t st, T* ab2) {
   dim3 grid((unsigned)((L.ldb + 255) / 256), (unsigned)min64(L.n, 65535));
-  band_gather_kernel<T><<<grid, 256, 0, st>>>(P, ndf, nq, L, K_el, ab);
+  band_gather_kernel<T><<<grid, 256, 0, st>>>(P, ndf, nq, L, K_el, ab, ab2);
 }
 void launch_resid_gather(const DevPatch& P, int ndf, int nq, const double* r_el, double* r, cudaStream_t st) {
   const int blocks = (int)min64(1024, (P.nmdf + 255) / 256);
@@ -222,9 +223,9 @@ void launch_axpy(int64_t n, const double* dx, double* x, cudaStream_t st) {
 }
 
 template void launch_band_gather<double>(const DevPatch&, int, int, const BandLayout&, const double*, double*,
-                                         cudaStream_t);
+                                         cudaStream_t, double*);
 template void launch_band_gather<float>(const DevPatch&, int, int, const BandLayout&, const float*, float*,
-                                        cudaStream_t);
+                                        cudaStream_t, float*);
 template void launch_band_residual<double>(const double*, const BandLayout&, const double*, const double*, double*,
                                            double*, double*, cudaStream_t);
 template void launch_band_residual<float>(const float*, const BandLayout&, const double*, const double*, double*,

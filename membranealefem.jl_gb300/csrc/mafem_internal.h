@@ -108,7 +108,7 @@ cudaError_t launch_elem(const DevPatch& P, const PhysParams& pp, double time, do
                         cudaStream_t st, const int* elist = nullptr, int nlist = 0, int area_only = 0);
 template <class T>
 void launch_band_gather(const DevPatch& P, int ndf, int nq, const BandLayout& L, const T* K_el, T* ab,
-                        cudaStream_t st);
+                        cudaStream_t st, T* ab2 = nullptr);
 void launch_resid_gather(const DevPatch& P, int ndf, int nq, const double* r_el, double* r, cudaStream_t st);
 void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaStream_t st);
 int newton_update_blocks(int64_t nmdf);
@@ -198,6 +198,35 @@ int blk_lu_factor_persist(T* ab, const BandLayout& L, const BlkPlan& B, const Bl
                           T* rdiag, int* info, T* rhs, int* err, cudaStream_t st, long long* trace = nullptr);
 template <class V, class T>
 void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, cudaStream_t st);
+}  // namespace mafem
+
+namespace mafem {
+// One patch's FP32 solve in the batched form (band_lu_patch.cu): device
+// pointers of the handle that owns them.
+struct PatchJob {
+  float* band;          // factored in place
+  const float* band0;   // the unfactored band (refinement residual)
+  float* inv;           // [npan][2][32][32]: L11^-1, U11^-1 per panel
+  const int* ps;        // panel starts [npan + 1]
+  const int* blk_end;   // [n]
+  int* perm;            // [npan][32]
+  float* rdiag;         // [n]
+  int* info;            // [0] zero-pivot column, [2] status, [3] sweeps
+  int* stat;            // = info + 2
+  const double* rhs;    // [n]
+  double* x;            // [n] solution
+  double* res;          // [n] FP64 residual (workspace)
+  float2* xs;           // [n] x as two floats (workspace)
+  BandLayout L;
+  int kuf, npan;
+};
+size_t patch_factor_smem(int kl);
+size_t patch_refine_smem(int64_t n);
+// Sets the kernels' shared-memory limits; returns the dynamic bytes available (0: unusable).
+int patch_solve_setup();
+// Factor and solve every job listed in d_order[0 .. njobs): one CTA per job.
+cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int njobs, size_t smem_factor, size_t smem_refine,
+                        int max_sweeps, double tol, cudaStream_t st);
 }  // namespace mafem
 
 #include <condition_variable>

@@ -149,6 +149,7 @@ def lib():
         L.mafem_launch_count.argtypes = [vp]
         L.mafem_launch_count.restype = C.c_int64
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
+        L.mafem_set_refinement.argtypes = [vp, C.c_int32, C.c_double]
         L.mafem_pull_force.argtypes = [vp, _PD]
         L.mafem_pull_position.argtypes = [vp, _PD]
         L.mafem_format_double.argtypes = [C.c_double, C.c_char_p, C.c_int32]
@@ -165,6 +166,7 @@ def lib():
         L.mafem_batch_create.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, C.POINTER(vp)]
         L.mafem_batch_step.argtypes = [vp, _PD, _PD, C.POINTER(C.c_int32), C.POINTER(StepStats)]
         L.mafem_batch_destroy.argtypes = [vp]
+        L.mafem_batch_set_patch_solve.argtypes = [vp, C.c_int32]
         L.mafem_profile_factor.argtypes = [vp, C.c_double, C.c_double, C.POINTER(KernelTimes)]
         L.mafem_probe_fp64_tflops.argtypes = [C.POINTER(C.c_double)]
         _lib = L
@@ -433,6 +435,10 @@ class Solver:
         """CTAs of the persistent factorisation (0: all SMs); returns the value in use."""
         return int(lib().mafem_set_launch_ctas(self.h, ctas))
 
+    def set_refinement(self, max_sweeps: int = 30, tol: float = 1e-10) -> None:
+        """FP32 form: refinement stops at |r - A x| <= tol |r| or after max_sweeps sweeps."""
+        _raise(lib().mafem_set_refinement(self.h, max_sweeps, tol), self.h)
+
     def set_lu_path(self, path: int) -> None:
         """Select the banded LU: LU_AUTO (default), LU_PANELS or LU_FULL."""
         _raise(lib().mafem_set_lu_path(self.h, path), self.h)
@@ -514,6 +520,10 @@ class Batch:
         arr = (C.c_void_p * len(self.solvers))(*[s.h for s in self.solvers])
         self.b = C.c_void_p()
         _raise(lib().mafem_batch_create(arr, len(self.solvers), ctas, C.byref(self.b)))
+
+    def set_patch_solve(self, on: bool) -> bool:
+        """Batched one-CTA-per-patch FP32 solve for the FP32 patches (default on)."""
+        return bool(lib().mafem_batch_set_patch_solve(self.b, int(on)))
 
     def step(self, times, dts):
         """One time step of every patch; returns (statuses, list of step-stat dicts)."""
