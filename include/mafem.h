@@ -245,14 +245,25 @@ int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas);
 
 /* ---- diagnostics --------------------------------------------------------------- */
 
+/* FP32 form: assemble the resident state and run the batched one-CTA solve on
+ * this handle alone, its factorisation traced -- 6 globaltimer stamps (ns) per
+ * panel in out[6p .. 6p+5] (start, diagonal block factored, panel staged and
+ * inverses formed, first chunk's U12/Y, its trailing update, panel done), then
+ * the factor and refine kernels' event times in ns.  cap >= 6 npan + 2.
+ * Returns npan, or MAFEM_ERR_UNSUPPORTED if the handle cannot use that solve. */
+int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap);
+
 /* Number of kernels this handle has enqueued since mafem_create. */
 int64_t mafem_launch_count(const mafem_handle* h);
 
-/* FP32 form: FP64 iterative refinement of each linear solve stops when
- * |r - A x| <= tol |r| (default 1e-10) or after max_sweeps sweeps (default 30;
- * MAFEM_REFINE_STALLED).  A looser tol trades refinement sweeps for Newton
- * iterations: the Newton criterion (FiniteElement.jl:48) still decides
- * convergence on the FP64 residual. */
+/* FP32 form: FP64 iterative refinement of each linear solve stops at
+ * tolerance tol (default 1e-10) or after max_sweeps sweeps (default 30;
+ * MAFEM_REFINE_STALLED).  A handle stepped alone stops when |r - A x| <= tol |r|;
+ * the batched solve of mafem_batch_step stops when its last correction is at
+ * most tol |x|, a bound on the forward error of x that holds on ill-conditioned
+ * tangents too.  A looser tol trades refinement sweeps for Newton iterations:
+ * the Newton criterion (FiniteElement.jl:48) still decides convergence on the
+ * FP64 residual. */
 int mafem_set_refinement(mafem_handle* h, int32_t max_sweeps, double tol);
 
 /* Select the banded LU (enum mafem_lu_path) for the following factorisations.

@@ -1298,6 +1298,57 @@ extern "C" int mafem_trace_factor(mafem_handle* h, double time, double dt, int64
   return nl < 0 ? MAFEM_ERR_CUDA : npan;
 }
 
+// Assemble the resident state and run the batched FP32 solve on this handle
+// alone with its factorisation traced: 6 stamps per panel into out (see
+// patch_factor_kernel), plus the factor and refine kernels' device times in
+// out[6 npan], out[6 npan + 1] (ns).  Returns npan.
+extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap) {
+  if (!h || !out || !h->patch_ok) return MAFEM_ERR_UNSUPPORTED;
+  const int npan = h->blk.npan();
+  if (cap < 6LL * npan + 2) return MAFEM_ERR_ARG;
+  long long* d_tr = nullptr;
+  PatchJob* d_job = nullptr;
+  int* d_ord = nullptr;
+  CK(cudaMalloc(&d_tr, sizeof(long long) * 6 * npan));
+  CK(cudaMalloc(&d_job, sizeof(PatchJob)));
+  CK(cudaMalloc(&d_ord, sizeof(int)));
+  PatchJob J = h->job;
+  J.trace = d_tr;
+  CK(cudaMemcpyAsync(d_job, &J, sizeof J, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemsetAsync(d_ord, 0, sizeof(int), h->st));
+  CK(cudaMemsetAsync(d_tr, 0, sizeof(long long) * 6 * npan, h->st));
+  int rc = assemble(h, time, dt, true);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(h->d_info, 0, 4 * sizeof(int), h->st));
+  cudaEvent_t e0, e1, e2;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  const int dyn = patch_solve_setup();
+  cudaEventRecord(e0, h->st);
+  patch_solve_stage(d_job, d_ord, 1, patch_factor_smem(h->L.kl), 0, 0, 0.0, h->st);
+  cudaEventRecord(e1, h->st);
+  patch_solve_stage(d_job, d_ord, 1, 0, patch_refine_smem(h->L.n), h->max_refine, h->refine_tol, h->st);
+  cudaEventRecord(e2, h->st);
+  std::vector<long long> tr((size_t)6 * npan);
+  CK(cudaMemcpyAsync(tr.data(), d_tr, tr.size() * sizeof(long long), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  float mf = 0, mr = 0;
+  cudaEventElapsedTime(&mf, e0, e1);
+  cudaEventElapsedTime(&mr, e1, e2);
+  for (size_t k = 0; k < tr.size(); ++k) out[k] = tr[k];
+  out[6 * npan] = (int64_t)(mf * 1e6);
+  out[6 * npan + 1] = (int64_t)(mr * 1e6);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  cudaFree(d_tr);
+  cudaFree(d_job);
+  cudaFree(d_ord);
+  h->factored = false;
+  return dyn > 0 ? npan : MAFEM_ERR_CUDA;
+}
+
 // calc_pull_force (PullForce.jl:61-80) with get_pull_el_id / get_adj_maps
 // (PullForce.jl:8-53): the velocity residual rv of calc_elem_dof_residuals
 // (area Gauss points only) of the (2·poly+1)² elements around element

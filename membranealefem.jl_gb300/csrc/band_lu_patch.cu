@@ -5,8 +5,8 @@
 // node-block pivoting (the same factors as band_lu_blk.cu: L11\U11 with the
 // panel's rows permuted, U12 = L11^-1 P A12, raw A21, rdiag = 1/U(j,j),
 // perm_all[p * 32 + i]), and `patch_refine_kernel` runs the FP32 triangular
-// solves and FP64 iterative refinement x += LU^-1 (r - A0 x) until
-// |r - A0 x| <= tol |r| -- the role of `K_gl \ r_gl` (FiniteElement.jl:38).
+// solves and FP64 iterative refinement x += LU^-1 (r - A0 x) until the last
+// correction is at most tol |x| -- the role of `K_gl \ r_gl` (FiniteElement.jl:38).
 // A single patch's LU is a chain of dependent panels; across a batch the
 // chains are independent, so one CTA per patch keeps every SM busy without
 // any inter-CTA synchronisation (the multi-CTA persistent kernel spends most
@@ -35,16 +35,44 @@
 namespace mafem {
 
 constexpr int kPT = 512;   // threads per CTA (16 warps)
-constexpr int kPCH = 512;  // trailing columns per chunk: one thread per column for U12 and Y
+constexpr int kPCH = 576;  // trailing columns per chunk (kuf of a 32 x 32 patch fits one chunk)
+constexpr int kYS = kPCH + 8;  // row stride of Y in shared memory (== 8 mod 32: conflict-free fragments)
 constexpr int kIS = 36;    // shared-memory row stride of the 32 x 32 inverses (16-byte rows)
 
-__host__ __device__ inline int patch_rp(int kl) { return (kBlkW + kl + 3) & ~3; }
+// panel column stride in shared memory: >= 32 + kl, == 8 mod 32 (conflict-free MMA fragments)
+__host__ __device__ inline int patch_rp(int kl) { return ((kBlkW + kl + 23) & ~31) + 8; }
 
 size_t patch_factor_smem(int kl) {
-  return sizeof(float) * ((size_t)kBlkW * patch_rp(kl) + (size_t)kBlkW * kPCH + 3 * (size_t)kBlkW * kIS);
+  return sizeof(float) * ((size_t)kBlkW * patch_rp(kl) + (size_t)kBlkW * kYS + 3 * (size_t)kBlkW * kIS);
+}
+
+// D += A B on the tensor cores: A 16 x 8 (row), B 8 x 8 (col), TF32 in, FP32 accumulate
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+      "{%0, %1, %2, %3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+// x = hi + lo with hi, lo TF32 (round to nearest): the 3xTF32 split
+__device__ __forceinline__ void split_tf32(float x, unsigned& hi, unsigned& lo) {
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+  const float r = x - __uint_as_float(hi);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
 }
 size_t patch_refine_smem(int64_t n) { return sizeof(float) * (size_t)n; }
 
+__device__ __forceinline__ void stamp(long long* tr, int slot) {
+  if (tr && threadIdx.x == 0) {
+    unsigned long long v;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
+    tr[slot] = (long long)v;
+  }
+}
+
+// trace (J.trace, optional): per panel 6 globaltimer stamps -- [0] start,
+// [1] diagonal block factored, [2] panel staged and inverses formed,
+// [3] U12 / Y of the first chunk, [4] its trailing update, [5] panel done
 __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __restrict__ jobs,
                                                              const int* __restrict__ order) {
   const PatchJob& J = jobs[order[blockIdx.x]];
@@ -53,8 +81,8 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
   const int Rp = patch_rp(L.kl);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* Lp = reinterpret_cast<float*>(smem_raw);  // [32][Rp]: A(j0 + r, j0 + c) at Lp[c * Rp + r]
-  float* Ys = Lp + (size_t)kBlkW * Rp;              // [32][kPCH]: Y = Mi P A12 (row k at Ys + k * kPCH)
-  float* Li = Ys + kBlkW * kPCH;                    // [32][kIS]
+  float* Ys = Lp + (size_t)kBlkW * Rp;              // [32][kYS]: Y = Mi P A12 (row k at Ys + k * kYS)
+  float* Li = Ys + kBlkW * kYS;                     // [32][kIS]
   float* Ui = Li + kBlkW * kIS;
   float* Mi = Ui + kBlkW * kIS;
   __shared__ float s_l[2][32];
@@ -70,10 +98,13 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
     const int R = (int)min64b(L.n - j0, (int64_t)w + L.kl);
     const int C = (int)(min64b(L.n, j1 + J.kuf) - j1);
     int* perm = J.perm + (size_t)p * kBlkW;
+    long long* tr = J.trace ? J.trace + (size_t)p * 6 : nullptr;
+    stamp(tr, 0);
 
     // 1. the diagonal block
     if (warp < kPanelWarps) blk_panel_factor<float, false>(ab, L, j0, w, J.blk_end, perm, J.rdiag, J.info, s_l, s_p);
     __syncthreads();
+    stamp(tr, 1);
 
     // 2. panel columns (all copies in flight at once), then the inverses of
     //    L11 and U11 by column, each lane's column in registers
@@ -125,14 +156,15 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
       inv[kBlkW * kBlkW + idx] = Ui[i * kIS + c];
     }
     __syncthreads();
+    stamp(tr, 2);
 
     // 3. trailing columns [j1, j1 + C) in chunks of kPCH
     const int nr = R - w;
     for (int cb = 0; cb < C; cb += kPCH) {
       const int nc = min(kPCH, C - cb);
       // U12 = Li P A12 and Y = Mi P A12: one thread per column, the column in registers
-      if (tid < nc) {
-        const int64_t col = j1 + cb + tid;
+      for (int c = tid; c < nc; c += kPT) {
+        const int64_t col = j1 + cb + c;
         float* dst = ab + bix(L, j0, col);  // A(j0 + r, col) = dst[r]
         float a[32];
 #pragma unroll
@@ -156,55 +188,99 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
               y = fmaf(m.w, a[4 * k + 3], y);
             }
             dst[r] = u;  // U12
-            Ys[r * kPCH + tid] = y;
+            Ys[r * kYS + c] = y;
           }
         }
       }
       __syncthreads();
-      // A22 -= A21 Y: warp tasks of 128 rows x 16 columns; lane owns rows
-      // lane + 32 q (q < 4), so every load and store instruction of the warp
-      // covers 32 consecutive rows of one column; per k: 4 A21 values and 4
-      // float4 broadcasts of Y for 64 FMAs
-      const int nrb = (nr + 127) >> 7, ncb = (nc + 15) >> 4;
-      for (int t = warp; t < nrb * ncb; t += kPT / 32) {
-        const int rb = t / ncb, c0 = (t - rb * ncb) * 16;
-        const int i0 = w + rb * 128 + lane;
-        float acc[4][16];
+      if (cb == 0) stamp(tr, 3);
+      // A22 -= A21 Y on the tensor cores, 3xTF32 (a b ~ ah bh + ah bl + al bh:
+      // FP32-level accuracy): warp tiles of 32 rows x 32 columns, two 16-row
+      // by four 8-column MMA tiles; the accumulators start as the A22 tile
+      // and A21 enters negated, so D = A22 - A21 Y is stored directly.
+      // Fragment layouts (m16n8k8, g = lane / 4, t = lane % 4): A a0 (g, t),
+      // a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4); B b0 (t, g),
+      // b1 (t + 4, g); C c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1).
+      {
+        const int g = lane >> 2, t4 = lane & 3;
+        const int nrt = (nr + 31) >> 5, nct = (nc + 31) >> 5;
+        const int ksteps = (w + 7) >> 3;
+        for (int tt = warp; tt < nrt * nct; tt += kPT / 32) {
+          const int rt = tt / nct, ct = tt - rt * nct;
+          const int r0 = w + rt * 32, c0 = ct * 32;
+          float acc[2][4][4];
+          float* cp[2][2];  // rows r0 + 16 mt + g (+ 8), column c0 + 2 t
+          bool rok[2][2];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = i0 + 32 * q;
-          const float* a0 = ab + bix(L, j0 + i, j1 + cb + c0);
+          for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-          for (int m = 0; m < 16; ++m) acc[q][m] = (i < R && c0 + m < nc) ? a0[m * ldm] : 0.0f;
-        }
-        for (int k = 0; k < w; ++k) {
-          float a[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) a[q] = Lp[k * Rp + min(i0 + 32 * q, R - 1)];
-          const float4* y4 = reinterpret_cast<const float4*>(Ys + k * kPCH + c0);
-#pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            const float4 y = y4[m];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              acc[q][4 * m + 0] = fmaf(-a[q], y.x, acc[q][4 * m + 0]);
-              acc[q][4 * m + 1] = fmaf(-a[q], y.y, acc[q][4 * m + 1]);
-              acc[q][4 * m + 2] = fmaf(-a[q], y.z, acc[q][4 * m + 2]);
-              acc[q][4 * m + 3] = fmaf(-a[q], y.w, acc[q][4 * m + 3]);
+            for (int h = 0; h < 2; ++h) {
+              const int r = r0 + 16 * mt + g + 8 * h;
+              rok[mt][h] = r < R;
+              cp[mt][h] = ab + bix(L, j0 + r, j1 + cb + c0 + 2 * t4);
             }
+#pragma unroll
+          for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const int h = e >> 1, cc = nt * 8 + (e & 1);  // column offset from c0 + 2 t
+                acc[mt][nt][e] = (rok[mt][h] && c0 + 2 * t4 + cc < nc) ? cp[mt][h][cc * ldm] : 0.0f;
+              }
+          for (int ks = 0; ks < ksteps; ++ks) {
+            const int k0 = ks * 8 + t4, k1 = k0 + 4;
+            unsigned ah[2][4], al[2][4], bh[4][2], bl[4][2];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+              const int ra = min(r0 + 16 * mt + g, R - 1), rb = min(r0 + 16 * mt + g + 8, R - 1);
+              const float x0 = k0 < w ? -Lp[k0 * Rp + ra] : 0.0f;
+              const float x1 = k0 < w ? -Lp[k0 * Rp + rb] : 0.0f;
+              const float x2 = k1 < w ? -Lp[k1 * Rp + ra] : 0.0f;
+              const float x3 = k1 < w ? -Lp[k1 * Rp + rb] : 0.0f;
+              split_tf32(x0, ah[mt][0], al[mt][0]);
+              split_tf32(x1, ah[mt][1], al[mt][1]);
+              split_tf32(x2, ah[mt][2], al[mt][2]);
+              split_tf32(x3, ah[mt][3], al[mt][3]);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+              const int c = c0 + nt * 8 + g;
+              const float y0 = k0 < w ? Ys[k0 * kYS + c] : 0.0f;
+              const float y1 = k1 < w ? Ys[k1 * kYS + c] : 0.0f;
+              split_tf32(y0, bh[nt][0], bl[nt][0]);
+              split_tf32(y1, bh[nt][1], bl[nt][1]);
+            }
+            // the three terms in separate passes over the 8 tiles, so
+            // consecutive MMAs never wait on each other's accumulator
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+              for (int nt = 0; nt < 4; ++nt) mma_tf32(acc[mt][nt], al[mt], bh[nt]);
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+              for (int nt = 0; nt < 4; ++nt) mma_tf32(acc[mt][nt], ah[mt], bl[nt]);
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+              for (int nt = 0; nt < 4; ++nt) mma_tf32(acc[mt][nt], ah[mt], bh[nt]);
           }
-        }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = i0 + 32 * q;
-          float* a0 = ab + bix(L, j0 + i, j1 + cb + c0);
+          for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-          for (int m = 0; m < 16; ++m)
-            if (i < R && c0 + m < nc) a0[m * ldm] = acc[q][m];
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const int h = e >> 1, cc = nt * 8 + (e & 1);
+                if (rok[mt][h] && c0 + 2 * t4 + cc < nc) cp[mt][h][cc * ldm] = acc[mt][nt][e];
+              }
         }
       }
       __syncthreads();
+      if (cb == 0) stamp(tr, 4);
     }
+    stamp(tr, 5);
   }
 }
 
@@ -387,8 +463,13 @@ __global__ void __launch_bounds__(kPT, 1) patch_refine_kernel(const PatchJob* __
     ss = fma(r, r, ss);
   }
   const double r0 = sqrt(block_sum(ss, red));
+  // Stop when the last correction is small against x: |d| <= tol |x| bounds
+  // the forward error of x (about rho |d| with rho < 1 the sweep's
+  // contraction) whatever the conditioning, where a residual test would
+  // accept a large error in x on an ill-conditioned tangent.  The residual
+  // after the final sweep is then never needed.
   int status = MAFEM_OK, sweeps = 0;
-  double rn = r0, prev = r0;
+  double rn = r0, prev_dn = INFINITY;
   if (r0 > 0.0) {
     status = MAFEM_REFINE_STALLED;
     for (int k = 0; k < max_sweeps; ++k) {
@@ -396,25 +477,38 @@ __global__ void __launch_bounds__(kPT, 1) patch_refine_kernel(const PatchJob* __
       for (int64_t i = tid; i < n; i += kPT) v[i] = (float)(J.res[i] * sc);
       __syncthreads();
       patch_lu_solve(J, v, bz, part);
+      double dd = 0.0, xx = 0.0;
       for (int64_t i = tid; i < n; i += kPT) {
-        const double x = fma(rn, (double)v[i], J.x[i]);
+        const double d = rn * (double)v[i];
+        const double x = J.x[i] + d;
         J.x[i] = x;
         const float xh = (float)x;
         xs[i] = make_float2(xh, (float)(x - (double)xh));
+        dd = fma(d, d, dd);
+        xx = fma(x, x, xx);
       }
-      __syncthreads();
-      rn = patch_residual(J, xs, red);
+      const double dn = sqrt(block_sum(dd, red));
+      const double xn = sqrt(block_sum(xx, red));
       sweeps = k + 1;
+      if (!isfinite(dn) || !isfinite(xn)) {
+        status = MAFEM_NAN_DETECTED;
+        break;
+      }
+      if (dn <= tol * xn) {
+        status = MAFEM_OK;
+        break;
+      }
+      if (k >= 3 && dn > 0.5 * prev_dn) break;  // stalled
+      prev_dn = dn;
+      rn = patch_residual(J, xs, red);  // block_sum orders the x / xs writes before it
       if (!isfinite(rn)) {
         status = MAFEM_NAN_DETECTED;
         break;
       }
-      if (rn <= tol * r0) {
+      if (rn == 0.0) {
         status = MAFEM_OK;
         break;
       }
-      if (k >= 3 && rn > 0.5 * prev) break;  // stalled
-      prev = rn;
     }
   }
   if (tid == 0) {
@@ -432,6 +526,14 @@ int patch_solve_setup() {
       cudaFuncSetAttribute(patch_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
     return 0;
   return dyn;
+}
+
+cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int njobs, size_t smem_factor,
+                              size_t smem_refine, int max_sweeps, double tol, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  if (smem_factor) patch_factor_kernel<<<njobs, kPT, smem_factor, st>>>(d_jobs, d_order);
+  if (smem_refine) patch_refine_kernel<<<njobs, kPT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
+  return cudaGetLastError();
 }
 
 cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int njobs, size_t smem_factor, size_t smem_refine,

@@ -219,12 +219,16 @@ struct PatchJob {
   float2* xs;           // [n] x as two floats (workspace)
   BandLayout L;
   int kuf, npan;
+  long long* trace;     // optional: 6 globaltimer stamps per panel (patch_factor_kernel)
 };
 size_t patch_factor_smem(int kl);
 size_t patch_refine_smem(int64_t n);
 // Sets the kernels' shared-memory limits; returns the dynamic bytes available (0: unusable).
 int patch_solve_setup();
 // Factor and solve every job listed in d_order[0 .. njobs): one CTA per job.
+// The factor kernel alone (smem_refine == 0) or the refine kernel alone (smem_factor == 0).
+cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int njobs, size_t smem_factor,
+                              size_t smem_refine, int max_sweeps, double tol, cudaStream_t st);
 cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int njobs, size_t smem_factor, size_t smem_refine,
                         int max_sweeps, double tol, cudaStream_t st);
 }  // namespace mafem

@@ -150,6 +150,7 @@ def lib():
         L.mafem_launch_count.restype = C.c_int64
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
         L.mafem_set_refinement.argtypes = [vp, C.c_int32, C.c_double]
+        L.mafem_trace_patch_solve.argtypes = [vp, C.c_double, C.c_double, C.POINTER(C.c_int64), C.c_int64]
         L.mafem_pull_force.argtypes = [vp, _PD]
         L.mafem_pull_position.argtypes = [vp, _PD]
         L.mafem_format_double.argtypes = [C.c_double, C.c_char_p, C.c_int32]
@@ -438,6 +439,17 @@ class Solver:
     def set_refinement(self, max_sweeps: int = 30, tol: float = 1e-10) -> None:
         """FP32 form: refinement stops at |r - A x| <= tol |r| or after max_sweeps sweeps."""
         _raise(lib().mafem_set_refinement(self.h, max_sweeps, tol), self.h)
+
+    def trace_patch_solve(self, time: float, dt: float):
+        """FP32 form: per-panel phase stamps (ns) of the batched one-CTA factorisation
+        of the resident state, as an (npan, 6) array, and the factor / refine kernel
+        times in ms."""
+        cap = 6 * 4096 + 2
+        buf = (C.c_int64 * cap)()
+        npan = lib().mafem_trace_patch_solve(self.h, time, dt, buf, cap)
+        _raise(0 if npan >= 0 else npan, self.h)
+        a = np.ctypeslib.as_array(buf)[: 6 * npan + 2].copy()
+        return a[: 6 * npan].reshape(npan, 6), a[6 * npan] / 1e6, a[6 * npan + 1] / 1e6
 
     def set_lu_path(self, path: int) -> None:
         """Select the banded LU: LU_AUTO (default), LU_PANELS or LU_FULL."""
