@@ -392,6 +392,29 @@ def run_batched(steps, warmup, wl=BATCH):
     finally:
         for s in fsolvers:
             s.close()
+    # (d) the same FP32 form under continuous batching (mafem_server): every
+    # patch advances through its steps on its own, no barrier between steps
+    with M.Server() as srv:
+        ids = [srv.submit(patches[i][1], patches[i][0], patches[i][2], patches[i][3], warmup + steps, dt,
+                          precision=M.FP32_REFINE, refine_tol=FP32_REFINE_TOL) for i in ok]
+        cu.sync()
+        h0 = time.perf_counter()
+        got, c_err, c_fail = {}, 0.0, 0
+        while len(got) < len(ids):
+            srv.round()
+            for k, rid in enumerate(ids):
+                if k not in got:
+                    res = srv.result(rid)
+                    if res is not None:
+                        got[k] = res
+        cu.sync()
+        c_wall = time.perf_counter() - h0
+        c_stats = srv.stats()
+    for k, i in enumerate(ok):
+        stt, xc, cc = got[k]
+        c_fail += stt != M.OK
+        xs, cs = seq_state[i]
+        c_err = max(c_err, _relmax(xc, xs), _relmax(cc, cs))
     n = len(ok)
     bat_ms = sum(bat_lat)
     lat = sorted(bat_lat)
@@ -420,7 +443,120 @@ def run_batched(steps, warmup, wl=BATCH):
                                    "max_rel_diff_vs_one_at_a_time": err, "failed_patch_steps": fails,
                                    "form": "plain FP64, mafem_batch_step: every patch's Newton iteration enqueued "
                                            "on its own stream before any is waited for"},
+            "continuous": {"value": n * (warmup + steps) / c_wall, "unit": "patch time-steps/s",
+                           "speedup_vs_plain_fp64_one_at_a_time": (n * (warmup + steps) / c_wall)
+                           / (n * steps / (seq_ms / 1e3)),
+                           "p50_step_ms": c_stats["p50_step_ms"], "p99_step_ms": c_stats["p99_step_ms"],
+                           "max_rel_err_vs_plain_fp64": c_err, "failed_patches": c_fail,
+                           "form": "the FP32 form under continuous batching (mafem_server): all patches "
+                                   "submitted at once, each advancing %d steps on its own; wall clock from the "
+                                   "first round to the last result" % (warmup + steps)},
             "size_histogram": {str(k): v for k, v in sorted(sizes.items())}}
+
+
+SERVE = dict(name="serving: Poisson arrivals of tether-pull solves, n in {8,16,32,64} elements per side with "
+                  "probabilities {0.4,0.3,0.2,0.1} (seed 2), half LAG / half ALEVB, kb log-uniform [0.5, 2], "
+                  "pull speed 0.01 f/6 with f ~ U[2, 10], dt 0.005",
+             rates=(50, 200, 800), requests=48, sizes=(8, 16, 32, 64), probs=(0.4, 0.3, 0.2, 0.1), seed=2,
+             steps=(20, 100), step_scale=0.1, dt=0.005)
+
+
+def serve_requests(M, wl=SERVE):
+    """The request sample: (Params, Mesh, xms, cps, steps, arrival offset at rate 1/s)."""
+    rng = np.random.default_rng(wl["seed"])
+    out = []
+    t = 0.0
+    for k in range(wl["requests"]):
+        n = int(rng.choice(wl["sizes"], p=wl["probs"]))
+        kb = float(np.exp(rng.uniform(np.log(0.5), np.log(2.0))))
+        f = float(rng.uniform(2.0, 10.0))
+        steps = int(rng.integers(wl["steps"][0], wl["steps"][1] + 1))
+        steps = max(2, int(round(steps * wl["step_scale"])))
+        t += float(rng.exponential(1.0))
+        motion = M.LAG if k % 2 == 0 else M.ALEVB
+        p = M.Params(motion=motion, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, kb=kb,
+                     pull_speed=0.01 * f / 6.0)
+        mesh = M.Mesh(p)
+        _, xms, cps = M.prepare_input(p, mesh)
+        M.perturb_interior_z(mesh, xms, seed=1000 + k, amp=1e-4)
+        out.append((p, mesh, xms, cps, steps, t))
+    return out
+
+
+def run_serving(wl=SERVE):
+    """Continuous batching (mafem_server) of a Poisson stream of requests at each
+    rate, against the same requests solved one at a time with the plain FP64
+    path.  Requests whose FP32 band does not fit one CTA (the 64 x 64 patches)
+    are served in the plain FP64 form, which the server interleaves without
+    host waits; the others in the FP32 form with batched solves.  Per-step
+    latency is the wall time from a step's first Newton iteration to its
+    convergence; throughput is time steps per wall second from the first
+    arrival to the last result."""
+    import mafem as M
+    cu = Cudart()
+    reqs = serve_requests(M, wl)
+    dt = wl["dt"]
+    # plain FP64, one at a time
+    seq_s, ref, total_steps = 0.0, [], 0
+    for p, mesh, x0, c0, steps, _ in reqs:
+        with M.Solver(mesh, p, M.PLAIN_FP64) as s:
+            s.upload(x0, c0)
+            cu.sync()
+            h0 = time.perf_counter()
+            try:
+                s.run_analysis([dt] * steps)
+                ok = True
+            except M.NewtonNotConverged:
+                ok = False
+            cu.sync()
+            seq_s += time.perf_counter() - h0
+            ref.append(s.download() if ok else None)
+        total_steps += steps
+    out = {"workload": wl["name"], "requests": len(reqs),
+           "steps_per_request": "U{%d..%d} scaled by %g (bounded sample)" % (wl["steps"][0], wl["steps"][1],
+                                                                               wl["step_scale"]),
+           "time_steps": total_steps,
+           "plain_fp64_one_at_a_time": {"value": total_steps / seq_s, "unit": "time-steps/s"}, "rates": {}}
+    for rate in wl["rates"]:
+        with M.Server() as srv:
+            ids, got = {}, {}
+            cu.sync()
+            t0 = time.perf_counter()
+            nxt = 0
+            while len(got) < len(reqs):
+                now = time.perf_counter() - t0
+                while nxt < len(reqs) and reqs[nxt][5] / rate <= now:
+                    p, mesh, x0, c0, steps, _ = reqs[nxt]
+                    fits = mesh.half_bw <= 600  # the one-CTA FP32 solve's shared-memory limit, with margin
+                    ids[nxt] = srv.submit(mesh, p, x0, c0, steps, dt,
+                                          precision=M.FP32_REFINE if fits else M.PLAIN_FP64,
+                                          refine_tol=FP32_REFINE_TOL)
+                    nxt += 1
+                active, pending = srv.round()
+                for k, rid in ids.items():
+                    if k not in got:
+                        res = srv.result(rid)
+                        if res is not None:
+                            got[k] = res
+                if active == 0 and pending == 0 and nxt < len(reqs):
+                    time.sleep(max(0.0, reqs[nxt][5] / rate - (time.perf_counter() - t0)))
+            cu.sync()
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        err, fails = 0.0, 0
+        for k, (stt, xc, cc) in got.items():
+            if stt != M.OK:
+                fails += 1
+                continue
+            if ref[k] is not None:
+                err = max(err, _relmax(xc, ref[k][0]), _relmax(cc, ref[k][1]))
+        out["rates"][str(rate)] = {"value": total_steps / wall, "unit": "time-steps/s",
+                                   "speedup_vs_plain_fp64_one_at_a_time": (total_steps / wall) / (total_steps / seq_s),
+                                   "p50_step_ms": st["p50_step_ms"], "p99_step_ms": st["p99_step_ms"],
+                                   "max_step_ms": st["max_step_ms"], "rounds": st["rounds"],
+                                   "arrival_span_s": reqs[-1][5] / rate, "wall_s": wall,
+                                   "max_rel_err_vs_plain_fp64": err, "failed_requests": fails}
+    return out
 
 
 def cpu_baseline(wl=WORKLOAD, max_seconds=20.0, max_steps=3):
@@ -457,6 +593,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -524,6 +661,8 @@ def main():
     }
     if rank == 0 and not args.no_batch:
         line["batched"] = run_batched(args.batch_steps, 1)
+    if rank == 0 and not args.no_serve:
+        line["serving"] = run_serving()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline()
     if rank == 0:

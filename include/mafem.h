@@ -243,6 +243,49 @@ int mafem_batch_set_patch_solve(mafem_batch* b, int32_t on);
  * SMs); clamped to what the band needs.  Returns the CTAs the factorisation uses. */
 int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas);
 
+/* ---- serving: continuous batching (no reference counterpart) -------------------------
+ * A request is one solve: a patch (the mesh view, Params and args of
+ * mafem_create), its initial state and a number of time steps.  The server
+ * admits requests first come first served while their device footprint fits
+ * its HBM budget and runs the admitted ones as one continuous batch: each
+ * mafem_server_round starts a time step (predictor + time_step!) for every
+ * admitted request between steps and runs one Newton iteration of every
+ * admitted request, FP32-form requests through the batched one-CTA solve.  A
+ * finished request's state is kept on the host and its device memory freed at
+ * once.  Each request's results are those of mafem_time_step on its own handle,
+ * whatever else runs beside it. */
+typedef struct mafem_server mafem_server;
+typedef struct mafem_request {
+  const mafem_mesh_desc* mesh;  /* must stay valid until the request is admitted */
+  const mafem_params* params;   /* likewise */
+  const mafem_args* args;       /* likewise */
+  int32_t precision;            /* enum mafem_precision */
+  int32_t nsteps;               /* time steps to run */
+  double t0, dt;                /* step k ends at t0 + (k + 1) dt */
+  const double* xms0;           /* initial state, copied at submit */
+  const double* cps0;
+  double refine_tol;            /* FP32 form: mafem_set_refinement's tol; 0 = default */
+} mafem_request;
+typedef struct mafem_server_stats {
+  int64_t steps_done, rounds;
+  double p50_step_ms, p99_step_ms, max_step_ms; /* wall time of each completed step */
+  int64_t bytes_in_use, budget_bytes;
+  int32_t active, pending;
+} mafem_server_stats;
+/* hbm_budget_bytes 0: 80 % of the device memory free now; max_active 0: 1024. */
+int mafem_server_create(int64_t hbm_budget_bytes, int32_t max_active, mafem_server** out);
+int mafem_server_destroy(mafem_server* s);
+/* Queue a request; MAFEM_ERR_ADMISSION if it can never fit the budget. */
+int mafem_server_submit(mafem_server* s, const mafem_request* r, int64_t* id);
+/* Admit what fits, then one Newton iteration of every admitted request. */
+int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n_pending);
+/* A finished request's final state (xms, cps as in mafem_download_state; either
+ * may be NULL) and status; the server then forgets it.  Returns 1 while it is
+ * still queued or running. */
+int mafem_server_result(mafem_server* s, int64_t id, double* xms, double* cps, int32_t* status,
+                        int32_t* steps_done);
+int mafem_server_get_stats(const mafem_server* s, mafem_server_stats* out);
+
 /* ---- diagnostics --------------------------------------------------------------- */
 
 /* FP32 form: assemble the resident state and run the batched one-CTA solve on

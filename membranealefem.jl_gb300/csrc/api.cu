@@ -10,8 +10,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -1207,6 +1210,303 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
     }
   }
   return first;
+}
+
+// ---- serving: continuous batching of many solves ------------------------------------
+// Requests (a patch, its initial state, a number of time steps) are admitted
+// while their device footprint fits the server's HBM budget and run as one
+// continuous batch: every round starts a step for each admitted request that is
+// between steps and runs one Newton iteration of every admitted request -- the
+// FP32 ones through one batched factor/solve launch pair -- so requests at
+// different steps, and requests that arrived while others were running, share
+// the GPU.  A finished request's state is copied out and its memory freed at
+// once, which admits the next.  Each request computes exactly what
+// mafem_time_step computes on its handle: results do not depend on the mix.
+
+namespace {
+struct ServerReq {
+  int64_t id = 0;
+  mafem_request r{};
+  std::vector<double> xms, cps;  // initial state, then the result
+  int64_t est = 0, bytes = 0;
+  mafem_handle* h = nullptr;
+  int slot = -1;
+  int step = 0;
+  double t = 0.0;
+  bool in_step = false;
+  double t_start = 0.0;  // host seconds at the step's first iteration
+  int status = MAFEM_OK;
+  bool done = false;
+  mafem_step_stats last{};
+};
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+struct mafem_server {
+  int64_t budget = 0, used = 0;
+  int max_active = 0;
+  int64_t next_id = 1;
+  std::deque<ServerReq*> pending;
+  std::vector<ServerReq*> active;
+  std::map<int64_t, ServerReq*> finished;
+  std::vector<int> free_slots;
+  PatchJob* d_jobs = nullptr;
+  PatchJob* h_jobs = nullptr;  // pinned staging of the job table
+  int* d_order = nullptr;
+  int* h_order = nullptr;  // pinned
+  cudaStream_t bst = nullptr;
+  cudaEvent_t bev = nullptr;
+  size_t smem_dyn = 0;
+  std::vector<double> step_ms;  // wall latency of every completed step
+  int64_t steps_done = 0, rounds = 0;
+  ~mafem_server() {
+    if (bst) cudaStreamSynchronize(bst);
+    for (ServerReq* q : pending) delete q;
+    for (ServerReq* q : active) {
+      if (q->h) mafem_destroy(q->h);
+      delete q;
+    }
+    for (auto& kv : finished) delete kv.second;
+    if (d_jobs) cudaFree(d_jobs);
+    if (d_order) cudaFree(d_order);
+    if (h_jobs) cudaFreeHost(h_jobs);
+    if (h_order) cudaFreeHost(h_order);
+    if (bev) cudaEventDestroy(bev);
+    if (bst) cudaStreamDestroy(bst);
+  }
+};
+
+extern "C" int mafem_server_create(int64_t hbm_budget_bytes, int32_t max_active, mafem_server** out) {
+  if (!out || hbm_budget_bytes < 0 || max_active < 0) return MAFEM_ERR_ARG;
+  auto s = std::make_unique<mafem_server>();
+  size_t fr = 0, tot = 0;
+  cudaError_t e = cudaMemGetInfo(&fr, &tot);
+  if (e != cudaSuccess) {
+    set_global_error(std::string("mafem_server_create: ") + cudaGetErrorString(e));
+    return MAFEM_ERR_CUDA;
+  }
+  s->budget = hbm_budget_bytes > 0 ? hbm_budget_bytes : (int64_t)(0.8 * (double)fr);
+  s->max_active = max_active > 0 ? max_active : 1024;
+  const size_t m = (size_t)s->max_active;
+  e = cudaMalloc(&s->d_jobs, m * sizeof(PatchJob));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_order, m * sizeof(int));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_jobs, m * sizeof(PatchJob));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_order, m * sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->bst, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->bev, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    set_global_error(std::string("mafem_server_create: ") + cudaGetErrorString(e));
+    return MAFEM_ERR_CUDA;
+  }
+  const int dyn = patch_solve_setup();
+  cudaGetLastError();
+  s->smem_dyn = dyn > 0 ? (size_t)dyn : 0;
+  for (int k = s->max_active - 1; k >= 0; --k) s->free_slots.push_back(k);
+  *out = s.release();
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_server_destroy(mafem_server* s) {
+  delete s;
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_server_submit(mafem_server* s, const mafem_request* r, int64_t* id) {
+  if (!s || !r || !id || !r->mesh || !r->params || !r->args || !r->xms0 || !r->cps0 || r->nsteps < 1 ||
+      !(r->dt > 0.0))
+    return MAFEM_ERR_ARG;
+  const int64_t fp = mafem_footprint_bytes(r->mesh, r->precision);
+  if (fp < 0) return MAFEM_ERR_ARG;
+  // the footprint estimate plus the FP32 form's per-panel inverses and slack
+  const int64_t est = fp + fp / 8 + (16LL << 20);
+  if (est > s->budget) {
+    set_global_error("request needs about " + std::to_string(est) + " device bytes, more than the server's budget of " +
+                     std::to_string(s->budget));
+    return MAFEM_ERR_ADMISSION;
+  }
+  auto q = std::make_unique<ServerReq>();
+  q->id = s->next_id++;
+  q->r = *r;
+  q->xms.assign(r->xms0, r->xms0 + 3 * r->mesh->numnp);
+  q->cps.assign(r->cps0, r->cps0 + r->mesh->ndf * r->mesh->numnp);
+  q->est = est;
+  q->t = r->t0;
+  *id = q->id;
+  s->pending.push_back(q.release());
+  return MAFEM_OK;
+}
+
+static void server_retire(mafem_server* s, ServerReq* q) {
+  mafem_handle* h = q->h;
+  if (q->status == MAFEM_OK || q->status == MAFEM_NEWTON_NOT_CONVERGED)
+    mafem_download_state(h, q->xms.data(), q->cps.data());
+  s->used -= q->bytes;
+  mafem_destroy(h);
+  q->h = nullptr;
+  if (q->slot >= 0) s->free_slots.push_back(q->slot);
+  q->slot = -1;
+  q->done = true;
+  s->finished[q->id] = q;
+}
+
+extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n_pending) {
+  if (!s) return MAFEM_ERR_ARG;
+  // 1. admission, first come first served, while the footprint fits
+  while (!s->pending.empty() && (int)s->active.size() < s->max_active) {
+    ServerReq* q = s->pending.front();
+    if (s->used + q->est > s->budget) break;
+    mafem_handle* h = nullptr;
+    int rc = mafem_create(q->r.mesh, q->r.params, q->r.args, q->r.precision, &h);
+    if (rc == MAFEM_ERR_OOM) break;  // try again when memory frees up
+    s->pending.pop_front();
+    if (rc == MAFEM_OK) rc = mafem_upload_state(h, q->xms.data(), q->cps.data());
+    if (rc == MAFEM_OK && q->r.refine_tol > 0.0) rc = mafem_set_refinement(h, 30, q->r.refine_tol);
+    if (rc != MAFEM_OK) {
+      q->status = rc;
+      q->done = true;
+      if (h) mafem_destroy(h);
+      s->finished[q->id] = q;
+      continue;
+    }
+    q->h = h;
+    q->bytes = h->bytes;
+    s->used += h->bytes;
+    if (h->patch_ok && s->smem_dyn >= patch_factor_smem(h->L.kl) && s->smem_dyn >= patch_refine_smem(h->L.n) &&
+        !s->free_slots.empty()) {
+      q->slot = s->free_slots.back();
+      s->free_slots.pop_back();
+      s->h_jobs[q->slot] = h->job;
+      cudaMemcpyAsync(s->d_jobs + q->slot, s->h_jobs + q->slot, sizeof(PatchJob), cudaMemcpyHostToDevice, s->bst);
+    }
+    s->active.push_back(q);
+  }
+  // 2. a step for every request between steps: predictor (Analysis.jl:193) + step_begin
+  const double t_round = now_s();
+  for (ServerReq* q : s->active)
+    if (!q->in_step) {
+      launch_predictor(q->h->P, q->h->pp, q->r.dt, q->h->st);
+      q->h->launches += 1;
+      step_begin(q->h, q->t + q->r.dt, q->r.dt);
+      q->in_step = true;
+      q->t_start = t_round;
+    }
+  // 3. one Newton iteration of every active request
+  std::vector<int> st(s->active.size(), MAFEM_OK);
+  std::vector<int> pj;
+  for (size_t k = 0; k < s->active.size(); ++k) {
+    ServerReq* q = s->active[k];
+    const bool patch = q->slot >= 0;
+    const int rc = patch ? iter_enqueue_patch_begin(q->h) : iter_enqueue(q->h);
+    if (rc != MAFEM_OK)
+      st[k] = rc;
+    else if (patch)
+      pj.push_back((int)k);
+  }
+  if (!pj.empty()) {
+    std::vector<double> cost(pj.size());
+    std::sort(pj.begin(), pj.end(), [&](int a, int b) {
+      const mafem_handle* x = s->active[a]->h;
+      const mafem_handle* y = s->active[b]->h;
+      return (double)x->blk.npan() * x->L.kl * x->blk.kuf > (double)y->blk.npan() * y->L.kl * y->blk.kuf;
+    });
+    size_t smf = 0, smr = 0;
+    int max_sw = 1;
+    double tol = 1.0;
+    for (size_t k = 0; k < pj.size(); ++k) {
+      mafem_handle* h = s->active[pj[k]]->h;
+      s->h_order[k] = s->active[pj[k]]->slot;
+      smf = std::max(smf, patch_factor_smem(h->L.kl));
+      smr = std::max(smr, patch_refine_smem(h->L.n));
+      max_sw = std::max(max_sw, h->max_refine);
+      tol = std::min(tol, h->refine_tol);
+      cudaStreamWaitEvent(s->bst, h->ev[1], 0);
+    }
+    cudaError_t e = cudaMemcpyAsync(s->d_order, s->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice, s->bst);
+    if (e == cudaSuccess) e = patch_solve(s->d_jobs, s->d_order, (int)pj.size(), smf, smr, max_sw, tol, s->bst);
+    if (e == cudaSuccess) e = cudaEventRecord(s->bev, s->bst);
+    for (int k : pj) {
+      mafem_handle* h = s->active[k]->h;
+      if (e != cudaSuccess) {
+        h->err = std::string("batched FP32 solve: ") + cudaGetErrorString(e);
+        st[k] = MAFEM_ERR_CUDA;
+        continue;
+      }
+      if (k == pj[0]) h->launches += 2;
+      const int rc = iter_enqueue_patch_end(h, s->bev);
+      if (rc != MAFEM_OK) st[k] = rc;
+    }
+  }
+  std::vector<ServerReq*> keep;
+  for (size_t k = 0; k < s->active.size(); ++k) {
+    ServerReq* q = s->active[k];
+    int rc = st[k];
+    if (rc == MAFEM_OK) {
+      rc = iter_finish(q->h);
+      if (rc == kIterAgain) {
+        keep.push_back(q);
+        continue;
+      }
+      if (rc == kIterDone) {
+        step_stats(q->h, &q->last);
+        s->step_ms.push_back((now_s() - q->t_start) * 1e3);
+        ++s->steps_done;
+        q->t += q->r.dt;
+        q->in_step = false;
+        if (++q->step < q->r.nsteps) {
+          keep.push_back(q);
+          continue;
+        }
+        rc = MAFEM_OK;
+      }
+    }
+    q->status = rc;
+    server_retire(s, q);
+  }
+  s->active.swap(keep);
+  ++s->rounds;
+  if (n_active) *n_active = (int32_t)s->active.size();
+  if (n_pending) *n_pending = (int32_t)s->pending.size();
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_server_result(mafem_server* s, int64_t id, double* xms, double* cps, int32_t* status,
+                                   int32_t* steps_done) {
+  if (!s) return MAFEM_ERR_ARG;
+  auto it = s->finished.find(id);
+  if (it == s->finished.end()) {
+    for (ServerReq* q : s->pending)
+      if (q->id == id) return 1;
+    for (ServerReq* q : s->active)
+      if (q->id == id) return 1;
+    return MAFEM_ERR_ARG;  // unknown id, or its result was already taken
+  }
+  ServerReq* q = it->second;
+  if (xms) std::memcpy(xms, q->xms.data(), q->xms.size() * sizeof(double));
+  if (cps) std::memcpy(cps, q->cps.data(), q->cps.size() * sizeof(double));
+  if (status) *status = q->status;
+  if (steps_done) *steps_done = q->step;
+  s->finished.erase(it);
+  delete q;
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_server_get_stats(const mafem_server* s, mafem_server_stats* out) {
+  if (!s || !out) return MAFEM_ERR_ARG;
+  std::vector<double> v = s->step_ms;
+  std::sort(v.begin(), v.end());
+  auto pct = [&](double q) { return v.empty() ? 0.0 : v[std::min(v.size() - 1, (size_t)(q * (double)v.size()))]; };
+  out->steps_done = s->steps_done;
+  out->rounds = s->rounds;
+  out->p50_step_ms = pct(0.50);
+  out->p99_step_ms = pct(0.99);
+  out->max_step_ms = v.empty() ? 0.0 : v.back();
+  out->bytes_in_use = s->used;
+  out->budget_bytes = s->budget;
+  out->active = (int32_t)s->active.size();
+  out->pending = (int32_t)s->pending.size();
+  return MAFEM_OK;
 }
 
 extern "C" int mafem_time_step_host(mafem_handle* h, double* xms, double* cps, double time, double dt,

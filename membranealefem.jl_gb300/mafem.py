@@ -99,6 +99,21 @@ class StepStats(C.Structure):
                 "ms_solve": self.ms_solve, "ms_total": self.ms_total}
 
 
+class _CRequest(C.Structure):
+    _fields_ = [("mesh", C.c_void_p), ("params", C.c_void_p), ("args", C.c_void_p), ("precision", C.c_int32),
+                ("nsteps", C.c_int32), ("t0", C.c_double), ("dt", C.c_double), ("xms0", C.c_void_p),
+                ("cps0", C.c_void_p), ("refine_tol", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("steps_done", C.c_int64), ("rounds", C.c_int64), ("p50_step_ms", C.c_double),
+                ("p99_step_ms", C.c_double), ("max_step_ms", C.c_double), ("bytes_in_use", C.c_int64),
+                ("budget_bytes", C.c_int64), ("active", C.c_int32), ("pending", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class KernelTimes(C.Structure):
     _fields_ = [("ms_assemble", C.c_double), ("ms_panel", C.c_double), ("ms_apply", C.c_double),
                 ("n_panel", C.c_int64), ("n_apply", C.c_int64), ("n", C.c_int64), ("kl", C.c_int64),
@@ -168,6 +183,12 @@ def lib():
         L.mafem_batch_step.argtypes = [vp, _PD, _PD, C.POINTER(C.c_int32), C.POINTER(StepStats)]
         L.mafem_batch_destroy.argtypes = [vp]
         L.mafem_batch_set_patch_solve.argtypes = [vp, C.c_int32]
+        L.mafem_server_create.argtypes = [C.c_int64, C.c_int32, C.POINTER(vp)]
+        L.mafem_server_destroy.argtypes = [vp]
+        L.mafem_server_submit.argtypes = [vp, C.POINTER(_CRequest), C.POINTER(C.c_int64)]
+        L.mafem_server_round.argtypes = [vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.mafem_server_result.argtypes = [vp, C.c_int64, _PD, _PD, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.mafem_server_get_stats.argtypes = [vp, C.POINTER(ServerStats)]
         L.mafem_profile_factor.argtypes = [vp, C.c_double, C.c_double, C.POINTER(KernelTimes)]
         L.mafem_probe_fp64_tflops.argtypes = [C.POINTER(C.c_double)]
         _lib = L
@@ -596,3 +617,68 @@ def perturb_interior_z(mesh: Mesh, xms: np.ndarray, seed: int = 0, amp: float = 
     interior = (s1 > 0) & (s1 < mesh.num1np - 1) & (s2 > 0) & (s2 < mesh.num2np - 1)
     xms[:, 2] += np.where(interior, amp * (2.0 * u - 1.0), 0.0)
     return xms
+
+
+class Server:
+    """Continuous batching of many solves (mafem_server_*): submit requests
+    (patch, initial state, number of steps), call round() repeatedly; each round
+    admits what fits the HBM budget and runs one Newton iteration of every
+    admitted request.  result(id) returns (status, xms, cps) once a request has
+    finished, None while it is queued or running."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0):
+        self.s = C.c_void_p()
+        _raise(lib().mafem_server_create(int(hbm_budget_bytes), int(max_active), C.byref(self.s)))
+        self._keep = {}  # id -> objects the library reads until the request is admitted
+
+    def submit(self, mesh, p, xms, cps, nsteps: int, dt: float, t0: float = 0.0,
+               precision: int = FP32_REFINE, refine_tol: float = 0.0) -> int:
+        xms = np.asfortranarray(xms, dtype=np.float64)
+        cps = np.asfortranarray(cps, dtype=np.float64)
+        cp, ca = p.c_params(), p.c_args()
+        req = _CRequest(C.addressof(mesh.desc), C.addressof(cp), C.addressof(ca), precision, int(nsteps),
+                        float(t0), float(dt), xms.ctypes.data, cps.ctypes.data, float(refine_tol))
+        rid = C.c_int64()
+        _raise(lib().mafem_server_submit(self.s, C.byref(req), C.byref(rid)))
+        self._keep[rid.value] = (mesh, cp, ca, (mesh.numnp, mesh.ndf))
+        return rid.value
+
+    def round(self):
+        """One round; returns (active, pending)."""
+        a, q = C.c_int32(), C.c_int32()
+        _raise(lib().mafem_server_round(self.s, C.byref(a), C.byref(q)))
+        return a.value, q.value
+
+    def result(self, rid: int):
+        mesh, _, _, (numnp, ndf) = self._keep[rid]
+        xms = np.zeros((numnp, 3), order="F")
+        cps = np.zeros((numnp, ndf), order="F")
+        st, steps = C.c_int32(), C.c_int32()
+        rc = lib().mafem_server_result(self.s, rid, _dp(xms), _dp(cps), C.byref(st), C.byref(steps))
+        if rc == 1:
+            return None
+        _raise(rc)
+        del self._keep[rid]
+        return st.value, xms, cps
+
+    def stats(self) -> dict:
+        out = ServerStats()
+        _raise(lib().mafem_server_get_stats(self.s, C.byref(out)))
+        return out.as_dict()
+
+    def close(self):
+        if self.s:
+            lib().mafem_server_destroy(self.s)
+            self.s = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
