@@ -35,15 +35,15 @@
 namespace mafem {
 
 constexpr int kPT = 512;   // threads per CTA (16 warps)
-constexpr int kPCH = 576;  // trailing columns per chunk (kuf of a 32 x 32 patch fits one chunk)
-constexpr int kYS = kPCH + 8;  // row stride of Y in shared memory (== 8 mod 32: conflict-free fragments)
+constexpr int kPCH = 288;      // trailing columns per chunk (a 32 x 32 patch's ~550 in two)
+constexpr int kYS = kPCH + 8;  // row stride of Y (uint2 hi/lo pairs) in shared memory
 constexpr int kIS = 36;    // shared-memory row stride of the 32 x 32 inverses (16-byte rows)
 
 // panel column stride in shared memory: >= 32 + kl, == 8 mod 32 (conflict-free MMA fragments)
 __host__ __device__ inline int patch_rp(int kl) { return ((kBlkW + kl + 23) & ~31) + 8; }
 
 size_t patch_factor_smem(int kl) {
-  return sizeof(float) * ((size_t)kBlkW * patch_rp(kl) + (size_t)kBlkW * kYS + 3 * (size_t)kBlkW * kIS);
+  return sizeof(float) * ((size_t)kBlkW * patch_rp(kl) + 2 * (size_t)kBlkW * kYS + 3 * (size_t)kBlkW * kIS);
 }
 
 // D += A B on the tensor cores: A 16 x 8 (row), B 8 x 8 (col), TF32 in, FP32 accumulate
@@ -81,8 +81,8 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
   const int Rp = patch_rp(L.kl);
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* Lp = reinterpret_cast<float*>(smem_raw);  // [32][Rp]: A(j0 + r, j0 + c) at Lp[c * Rp + r]
-  float* Ys = Lp + (size_t)kBlkW * Rp;              // [32][kYS]: Y = Mi P A12 (row k at Ys + k * kYS)
-  float* Li = Ys + kBlkW * kYS;                     // [32][kIS]
+  uint2* Ys = reinterpret_cast<uint2*>(Lp + (size_t)kBlkW * Rp);  // [32][kYS]: Y = Mi P A12 split hi/lo (TF32)
+  float* Li = reinterpret_cast<float*>(Ys + kBlkW * kYS);          // [32][kIS]
   float* Ui = Li + kBlkW * kIS;
   float* Mi = Ui + kBlkW * kIS;
   __shared__ float s_l[2][32];
@@ -188,93 +188,96 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
               y = fmaf(m.w, a[4 * k + 3], y);
             }
             dst[r] = u;  // U12
-            Ys[r * kYS + c] = y;
+            uint2 yy;
+            split_tf32(y, yy.x, yy.y);
+            Ys[r * kYS + c] = yy;
           }
         }
       }
       __syncthreads();
       if (cb == 0) stamp(tr, 3);
       // A22 -= A21 Y on the tensor cores, 3xTF32 (a b ~ ah bh + ah bl + al bh:
-      // FP32-level accuracy): warp tiles of 32 rows x 32 columns, two 16-row
-      // by four 8-column MMA tiles; the accumulators start as the A22 tile
-      // and A21 enters negated, so D = A22 - A21 Y is stored directly.
-      // Fragment layouts (m16n8k8, g = lane / 4, t = lane % 4): A a0 (g, t),
-      // a1 (g + 8, t), a2 (g, t + 4), a3 (g + 8, t + 4); B b0 (t, g),
-      // b1 (t + 4, g); C c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1).
+      // FP32-level accuracy).  A warp task is a 16-row strip of A22 over half
+      // of the chunk's column tiles: the strip's A21 fragments (negated, so the
+      // MMAs accumulate A22 - A21 Y) are split once into registers; Y comes
+      // pre-split from shared memory; the next column tile's A22 values are
+      // loaded while the current tile's MMAs run.  Fragment layouts
+      // (m16n8k8, g = lane / 4, t = lane % 4): A a0 (g, t), a1 (g + 8, t),
+      // a2 (g, t + 4), a3 (g + 8, t + 4); B b0 (t, g), b1 (t + 4, g);
+      // C c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1).
       {
         const int g = lane >> 2, t4 = lane & 3;
-        const int nrt = (nr + 31) >> 5, nct = (nc + 31) >> 5;
+        const int nrs = (nr + 15) >> 4, nct = (nc + 31) >> 5;
+        const int nhalf = nct > 1 ? 2 : 1;
         const int ksteps = (w + 7) >> 3;
-        for (int tt = warp; tt < nrt * nct; tt += kPT / 32) {
-          const int rt = tt / nct, ct = tt - rt * nct;
-          const int r0 = w + rt * 32, c0 = ct * 32;
-          float acc[2][4][4];
-          float* cp[2][2];  // rows r0 + 16 mt + g (+ 8), column c0 + 2 t
-          bool rok[2][2];
+        for (int task = warp; task < nrs * nhalf; task += kPT / 32) {
+          const int rs = task / nhalf, hf = task - rs * nhalf;
+          const int ct0 = hf * ((nct + 1) >> 1), ct1 = hf + 1 == nhalf ? nct : (nct + 1) >> 1;
+          const int r0 = w + rs * 16;
+          const int ra = r0 + g, rb = r0 + g + 8;
+          const bool oka = ra < R, okb = rb < R;
+          unsigned ah[4][4], al[4][4];
 #pragma unroll
-          for (int mt = 0; mt < 2; ++mt)
+          for (int ks = 0; ks < 4; ++ks) {
+            const int k0 = ks * 8 + t4, k1 = k0 + 4;
+            const int ca = min(ra, R - 1), cbr = min(rb, R - 1);
+            const float x0 = k0 < w ? -Lp[k0 * Rp + ca] : 0.0f;
+            const float x1 = k0 < w ? -Lp[k0 * Rp + cbr] : 0.0f;
+            const float x2 = k1 < w ? -Lp[k1 * Rp + ca] : 0.0f;
+            const float x3 = k1 < w ? -Lp[k1 * Rp + cbr] : 0.0f;
+            split_tf32(x0, ah[ks][0], al[ks][0]);
+            split_tf32(x1, ah[ks][1], al[ks][1]);
+            split_tf32(x2, ah[ks][2], al[ks][2]);
+            split_tf32(x3, ah[ks][3], al[ks][3]);
+          }
+          // rows ra / rb of the chunk's first column: A(j0 + r, j1 + cb) = row pointer
+          float* pa = ab + bix(L, j0 + ra, j1 + cb);
+          float* pb = ab + bix(L, j0 + rb, j1 + cb);
+          auto load_c = [&](int ct, float (&c)[4][4]) {
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-              const int r = r0 + 16 * mt + g + 8 * h;
-              rok[mt][h] = r < R;
-              cp[mt][h] = ab + bix(L, j0 + r, j1 + cb + c0 + 2 * t4);
+            for (int nt = 0; nt < 4; ++nt) {
+              const int cc = ct * 32 + nt * 8 + 2 * t4;
+              const bool c0k = cc < nc, c1k = cc + 1 < nc;
+              c[nt][0] = oka && c0k ? pa[(int64_t)cc * ldm] : 0.0f;
+              c[nt][1] = oka && c1k ? pa[(int64_t)(cc + 1) * ldm] : 0.0f;
+              c[nt][2] = okb && c0k ? pb[(int64_t)cc * ldm] : 0.0f;
+              c[nt][3] = okb && c1k ? pb[(int64_t)(cc + 1) * ldm] : 0.0f;
             }
-#pragma unroll
-          for (int mt = 0; mt < 2; ++mt)
+          };
+          float acc[4][4], nxt[4][4];
+          if (ct0 < ct1) load_c(ct0, nxt);
+          for (int ct = ct0; ct < ct1; ++ct) {
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                const int h = e >> 1, cc = nt * 8 + (e & 1);  // column offset from c0 + 2 t
-                acc[mt][nt][e] = (rok[mt][h] && c0 + 2 * t4 + cc < nc) ? cp[mt][h][cc * ldm] : 0.0f;
-              }
-          for (int ks = 0; ks < ksteps; ++ks) {
-            const int k0 = ks * 8 + t4, k1 = k0 + 4;
-            unsigned ah[2][4], al[2][4], bh[4][2], bl[4][2];
+              for (int e = 0; e < 4; ++e) acc[nt][e] = nxt[nt][e];
+            if (ct + 1 < ct1) load_c(ct + 1, nxt);
 #pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-              const int ra = min(r0 + 16 * mt + g, R - 1), rb = min(r0 + 16 * mt + g + 8, R - 1);
-              const float x0 = k0 < w ? -Lp[k0 * Rp + ra] : 0.0f;
-              const float x1 = k0 < w ? -Lp[k0 * Rp + rb] : 0.0f;
-              const float x2 = k1 < w ? -Lp[k1 * Rp + ra] : 0.0f;
-              const float x3 = k1 < w ? -Lp[k1 * Rp + rb] : 0.0f;
-              split_tf32(x0, ah[mt][0], al[mt][0]);
-              split_tf32(x1, ah[mt][1], al[mt][1]);
-              split_tf32(x2, ah[mt][2], al[mt][2]);
-              split_tf32(x3, ah[mt][3], al[mt][3]);
+            for (int ks = 0; ks < 4; ++ks) {
+              if (ks >= ksteps) break;  // warp-uniform; the unrolled index keeps ah / al in registers
+              const int k0 = ks * 8 + t4;
+#pragma unroll
+              for (int nt = 0; nt < 4; ++nt) {
+                const int c = ct * 32 + nt * 8 + g;
+                // rows k >= w of Y are stale shared memory: mask them (0 * NaN would not vanish)
+                const uint2 y0 = k0 < w ? Ys[k0 * kYS + c] : make_uint2(0u, 0u);
+                const uint2 y1 = k0 + 4 < w ? Ys[(k0 + 4) * kYS + c] : make_uint2(0u, 0u);
+                const unsigned bh[2] = {y0.x, y1.x}, bl[2] = {y0.y, y1.y};
+                mma_tf32(acc[nt], al[ks], bh);
+                mma_tf32(acc[nt], ah[ks], bl);
+                mma_tf32(acc[nt], ah[ks], bh);
+              }
             }
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt) {
-              const int c = c0 + nt * 8 + g;
-              const float y0 = k0 < w ? Ys[k0 * kYS + c] : 0.0f;
-              const float y1 = k1 < w ? Ys[k1 * kYS + c] : 0.0f;
-              split_tf32(y0, bh[nt][0], bl[nt][0]);
-              split_tf32(y1, bh[nt][1], bl[nt][1]);
+              const int cc = ct * 32 + nt * 8 + 2 * t4;
+              const bool c0k = cc < nc, c1k = cc + 1 < nc;
+              if (oka && c0k) pa[(int64_t)cc * ldm] = acc[nt][0];
+              if (oka && c1k) pa[(int64_t)(cc + 1) * ldm] = acc[nt][1];
+              if (okb && c0k) pb[(int64_t)cc * ldm] = acc[nt][2];
+              if (okb && c1k) pb[(int64_t)(cc + 1) * ldm] = acc[nt][3];
             }
-            // the three terms in separate passes over the 8 tiles, so
-            // consecutive MMAs never wait on each other's accumulator
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-              for (int nt = 0; nt < 4; ++nt) mma_tf32(acc[mt][nt], al[mt], bh[nt]);
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-              for (int nt = 0; nt < 4; ++nt) mma_tf32(acc[mt][nt], ah[mt], bl[nt]);
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-              for (int nt = 0; nt < 4; ++nt) mma_tf32(acc[mt][nt], ah[mt], bh[nt]);
           }
-#pragma unroll
-          for (int mt = 0; mt < 2; ++mt)
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                const int h = e >> 1, cc = nt * 8 + (e & 1);
-                if (rok[mt][h] && c0 + 2 * t4 + cc < nc) cp[mt][h][cc * ldm] = acc[mt][nt][e];
-              }
         }
       }
       __syncthreads();
