@@ -559,6 +559,44 @@ def run_serving(wl=SERVE):
     return out
 
 
+def run_case(case):
+    """Small fixed cases for ncu captures (no bench line): `fp32-patch32` is one
+    batched FP32-form step of the bench's 32 x 32 ALEVB patch alone;
+    `fp32-batch16` two batched FP32-form steps of the first 16 patches of the
+    batched set.  Prints a short JSON summary."""
+    import mafem as M
+    if case == "fp32-patch32":
+        p = make_params(M)
+        mesh = M.Mesh(p)
+        x0, c0 = initial_state(M, p, mesh)
+        items = [(p, mesh, x0, c0)]
+        nsteps = 1
+    else:
+        items = batch_patches(M, dict(BATCH, patches=16))
+        nsteps = 2
+    solvers = [M.Solver(mesh, p, M.FP32_REFINE) for p, mesh, _, _ in items]
+    out = []
+    try:
+        for s, (_, _, x0, c0) in zip(solvers, items):
+            s.upload(x0, c0)
+            s.set_refinement(30, FP32_REFINE_TOL)
+        dt = BATCH["dt"] if case != "fp32-patch32" else WORKLOAD["dt"]
+        with M.Batch(solvers) as b:
+            t = 0.0
+            for _ in range(nsteps):
+                t += dt
+                h0 = time.perf_counter()
+                status, st = b.step(t, dt)
+                out.append({"ms": (time.perf_counter() - h0) * 1e3, "status": status,
+                            "newton": [x["newton_iters"] for x in st], "sweeps": [x["refine_iters"] for x in st]})
+    finally:
+        for s in solvers:
+            s.close()
+    print(json.dumps({"case": case, "steps": out}))
+    if any(x != M.OK for o in out for x in o["status"]):
+        raise SystemExit(1)
+
+
 def cpu_baseline(wl=WORKLOAD, max_seconds=20.0, max_steps=3):
     """The oracle's threaded complex-step assembly + scipy SuperLU (the stand-in for
     the reference's Julia calc_r_K + UMFPACK) on a bounded sample of the workload."""
@@ -594,7 +632,12 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--case", choices=["fp32-patch32", "fp32-batch16"],
+                    help="run a small profiling case instead of the bench (prints no bench line)")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local, dist = dist_init()
