@@ -1044,6 +1044,21 @@ extern "C" int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas) {
   return h->pers.max_grid > 0 ? h->pers.grid : h->bwd_grid;
 }
 
+// Order of a round's batched solves: the patches factored on two-CTA clusters
+// (more trailing columns than one chunk) first, then the single-CTA ones, each
+// group largest first.  Returns the number of cluster patches.
+static int order_patch_jobs(std::vector<mafem_handle*>& hv, std::vector<int>& idx) {
+  auto big = [&](int k) { return hv[k]->blk.kuf > patch_chunk_cols(); };
+  auto cost = [&](int k) { return (double)hv[k]->blk.npan() * hv[k]->L.kl * hv[k]->blk.kuf; };
+  std::sort(idx.begin(), idx.end(), [&](int a, int b) {
+    if (big(a) != big(b)) return big(a);
+    return cost(a) > cost(b);
+  });
+  int nbig = 0;
+  for (int k : idx) nbig += big(k) ? 1 : 0;
+  return nbig;
+}
+
 struct mafem_batch {
   std::vector<mafem_handle*> hs;
   // batched FP32 solve: the handles whose band fits one CTA (patch_ok)
@@ -1053,13 +1068,17 @@ struct mafem_batch {
   PatchJob* d_jobs = nullptr;
   int* d_order = nullptr;
   int* h_order = nullptr;  // pinned
-  cudaStream_t bst = nullptr;
-  cudaEvent_t bev = nullptr;
+  cudaStream_t bst = nullptr, bst2 = nullptr;  // clusters / single CTAs
+  cudaEvent_t bev = nullptr, efork = nullptr, ejoin = nullptr;
   size_t smem_f = 0, smem_r = 0;
   int max_sweeps = 30;
   double tol = 1e-10;
   ~mafem_batch() {
     if (bst) cudaStreamSynchronize(bst);
+    if (bst2) cudaStreamSynchronize(bst2);
+    if (efork) cudaEventDestroy(efork);
+    if (ejoin) cudaEventDestroy(ejoin);
+    if (bst2) cudaStreamDestroy(bst2);
     if (d_jobs) cudaFree(d_jobs);
     if (d_order) cudaFree(d_order);
     if (h_order) cudaFreeHost(h_order);
@@ -1107,7 +1126,10 @@ extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ct
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_order, nj * sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(b->d_jobs, jobs.data(), nj * sizeof(PatchJob), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->bst, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->bst2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->bev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->efork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ejoin, cudaEventDisableTiming);
     if (e != cudaSuccess) {
       set_global_error(std::string("mafem_batch_create: ") + cudaGetErrorString(e));
       return MAFEM_ERR_CUDA;
@@ -1161,7 +1183,7 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
         pj.push_back(i);
     }
     if (!pj.empty()) {
-      std::sort(pj.begin(), pj.end(), [&](int x, int y) { return b->cost[b->slot[x]] > b->cost[b->slot[y]]; });
+      const int nbig = order_patch_jobs(b->hs, pj);
       // one launch serves every patch: the strictest tolerance and the largest sweep cap among them
       b->max_sweeps = 1;
       b->tol = 1.0;
@@ -1175,7 +1197,8 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
       }
       cudaError_t e = cudaMemcpyAsync(b->d_order, b->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice, b->bst);
       if (e == cudaSuccess)
-        e = patch_solve(b->d_jobs, b->d_order, (int)pj.size(), b->smem_f, b->smem_r, b->max_sweeps, b->tol, b->bst);
+        e = patch_solve(b->d_jobs, b->d_order, nbig, (int)pj.size(), b->smem_f, b->smem_r, b->max_sweeps, b->tol,
+                        b->bst, b->bst2, b->efork, b->ejoin);
       if (e == cudaSuccess) e = cudaEventRecord(b->bev, b->bst);
       for (int i : pj) {
         mafem_handle* h = b->hs[i];
@@ -1256,8 +1279,8 @@ struct mafem_server {
   PatchJob* h_jobs = nullptr;  // pinned staging of the job table
   int* d_order = nullptr;
   int* h_order = nullptr;  // pinned
-  cudaStream_t bst = nullptr;
-  cudaEvent_t bev = nullptr;
+  cudaStream_t bst = nullptr, bst2 = nullptr;
+  cudaEvent_t bev = nullptr, efork = nullptr, ejoin = nullptr;
   size_t smem_dyn = 0;
   std::vector<double> step_ms;  // wall latency of every completed step
   int64_t steps_done = 0, rounds = 0;
@@ -1274,6 +1297,10 @@ struct mafem_server {
     if (h_jobs) cudaFreeHost(h_jobs);
     if (h_order) cudaFreeHost(h_order);
     if (bev) cudaEventDestroy(bev);
+    if (efork) cudaEventDestroy(efork);
+    if (ejoin) cudaEventDestroy(ejoin);
+    if (bst2) cudaStreamSynchronize(bst2);
+    if (bst2) cudaStreamDestroy(bst2);
     if (bst) cudaStreamDestroy(bst);
   }
 };
@@ -1295,7 +1322,10 @@ extern "C" int mafem_server_create(int64_t hbm_budget_bytes, int32_t max_active,
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_jobs, m * sizeof(PatchJob));
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_order, m * sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->bst, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->bst2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->bev, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->efork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ejoin, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     set_global_error(std::string("mafem_server_create: ") + cudaGetErrorString(e));
     return MAFEM_ERR_CUDA;
@@ -1405,12 +1435,9 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
       pj.push_back((int)k);
   }
   if (!pj.empty()) {
-    std::vector<double> cost(pj.size());
-    std::sort(pj.begin(), pj.end(), [&](int a, int b) {
-      const mafem_handle* x = s->active[a]->h;
-      const mafem_handle* y = s->active[b]->h;
-      return (double)x->blk.npan() * x->L.kl * x->blk.kuf > (double)y->blk.npan() * y->L.kl * y->blk.kuf;
-    });
+    std::vector<mafem_handle*> hv(s->active.size());
+    for (size_t k = 0; k < s->active.size(); ++k) hv[k] = s->active[k]->h;
+    const int nbig = order_patch_jobs(hv, pj);
     size_t smf = 0, smr = 0;
     int max_sw = 1;
     double tol = 1.0;
@@ -1424,7 +1451,9 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
       cudaStreamWaitEvent(s->bst, h->ev[1], 0);
     }
     cudaError_t e = cudaMemcpyAsync(s->d_order, s->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice, s->bst);
-    if (e == cudaSuccess) e = patch_solve(s->d_jobs, s->d_order, (int)pj.size(), smf, smr, max_sw, tol, s->bst);
+    if (e == cudaSuccess)
+      e = patch_solve(s->d_jobs, s->d_order, nbig, (int)pj.size(), smf, smr, max_sw, tol, s->bst, s->bst2, s->efork,
+                      s->ejoin);
     if (e == cudaSuccess) e = cudaEventRecord(s->bev, s->bst);
     for (int k : pj) {
       mafem_handle* h = s->active[k]->h;
@@ -1626,9 +1655,10 @@ extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, 
   cudaEventCreate(&e2);
   const int dyn = patch_solve_setup();
   cudaEventRecord(e0, h->st);
-  patch_solve_stage(d_job, d_ord, 1, patch_factor_smem(h->L.kl), 0, 0, 0.0, h->st);
+  const int nr = h->blk.kuf > patch_chunk_cols() ? 2 : 1;  // as a batch would run it
+  patch_solve_stage(d_job, d_ord, 1, nr, patch_factor_smem(h->L.kl), 0, 0, 0.0, h->st);
   cudaEventRecord(e1, h->st);
-  patch_solve_stage(d_job, d_ord, 1, 0, patch_refine_smem(h->L.n), h->max_refine, h->refine_tol, h->st);
+  patch_solve_stage(d_job, d_ord, 1, 1, 0, patch_refine_smem(h->L.n), h->max_refine, h->refine_tol, h->st);
   cudaEventRecord(e2, h->st);
   std::vector<long long> tr((size_t)6 * npan);
   CK(cudaMemcpyAsync(tr.data(), d_tr, tr.size() * sizeof(long long), cudaMemcpyDeviceToHost, h->st));

@@ -70,12 +70,30 @@ __device__ __forceinline__ void stamp(long long* tr, int slot) {
   }
 }
 
+// all threads of every CTA of the cluster; orders each CTA's prior memory
+// accesses (global included) before the others' later ones
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // trace (J.trace, optional): per panel 6 globaltimer stamps -- [0] start,
 // [1] diagonal block factored, [2] panel staged and inverses formed,
 // [3] U12 / Y of the first chunk, [4] its trailing update, [5] panel done
+//
+// NR = 2: a patch on a cluster of two CTAs (launched with cluster dims (2,1,1)).
+// Rank 0 factors the diagonal block; both ranks stage the panel and form the
+// inverses; rank r updates the trailing chunks r, r + 2, ... .  A column moves
+// from rank 1's chunks to rank 0's as the panels advance, so every band read
+// goes to L2 (ld.global.cg) and each panel ends at a cluster barrier; the
+// factored block is published by another after the panel factorisation.  Both
+// ranks run the same panel loop, so every barrier is reached by all threads of
+// both CTAs.
+template <int NR>
 __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __restrict__ jobs,
                                                              const int* __restrict__ order) {
-  const PatchJob& J = jobs[order[blockIdx.x]];
+  constexpr bool CG = NR > 1;
+  const int rank = (int)(blockIdx.x % NR);
+  const PatchJob& J = jobs[order[blockIdx.x / NR]];
   const BandLayout L = J.L;
   float* __restrict__ ab = J.band;
   const int Rp = patch_rp(L.kl);
@@ -102,21 +120,27 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
     stamp(tr, 0);
 
     // 1. the diagonal block
-    if (warp < kPanelWarps) blk_panel_factor<float, false>(ab, L, j0, w, J.blk_end, perm, J.rdiag, J.info, s_l, s_p);
+    if (rank == 0 && warp < kPanelWarps)
+      blk_panel_factor<float, CG>(ab, L, j0, w, J.blk_end, perm, J.rdiag, J.info, s_l, s_p);
     __syncthreads();
+    if (NR > 1) cluster_sync();
     stamp(tr, 1);
 
     // 2. panel columns (all copies in flight at once), then the inverses of
     //    L11 and U11 by column, each lane's column in registers
     for (int c = 0; c < w; ++c) {
       const float* src = ab + bix(L, j0, j0 + c);
-      for (int r = tid; r < R; r += kPT) cp_async(Lp + c * Rp + r, src + r);
+      if (CG) {
+        for (int r = tid; r < R; r += kPT) Lp[c * Rp + r] = __ldcg(src + r);
+      } else {
+        for (int r = tid; r < R; r += kPT) cp_async(Lp + c * Rp + r, src + r);
+      }
     }
     if (tid < kBlkW) {
-      sp[tid] = tid < w ? perm[tid] : 0;
-      rd[tid] = tid < w ? J.rdiag[j0 + tid] : 0.0f;
+      sp[tid] = tid < w ? ldx<CG>(perm + tid) : 0;
+      rd[tid] = tid < w ? ldx<CG>(J.rdiag + j0 + tid) : 0.0f;
     }
-    cp_async_wait_all();
+    if (!CG) cp_async_wait_all();
     __syncthreads();
     if (warp < 2) {
       float x[32];
@@ -152,15 +176,17 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
       float s = 0.0f;
       for (int k = max(i, c); k < w; ++k) s = fmaf(Ui[i * kIS + k], Li[k * kIS + c], s);
       Mi[i * kIS + c] = s;
-      inv[idx] = Li[i * kIS + c];
-      inv[kBlkW * kBlkW + idx] = Ui[i * kIS + c];
+      if (rank == 0) {
+        inv[idx] = Li[i * kIS + c];
+        inv[kBlkW * kBlkW + idx] = Ui[i * kIS + c];
+      }
     }
     __syncthreads();
     stamp(tr, 2);
 
     // 3. trailing columns [j1, j1 + C) in chunks of kPCH
     const int nr = R - w;
-    for (int cb = 0; cb < C; cb += kPCH) {
+    for (int cb = rank * kPCH; cb < C; cb += NR * kPCH) {
       const int nc = min(kPCH, C - cb);
       // U12 = Li P A12 and Y = Mi P A12: one thread per column, the column in registers
       for (int c = tid; c < nc; c += kPT) {
@@ -168,7 +194,7 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
         float* dst = ab + bix(L, j0, col);  // A(j0 + r, col) = dst[r]
         float a[32];
 #pragma unroll
-        for (int k = 0; k < 32; ++k) a[k] = k < w ? dst[sp[k]] : 0.0f;
+        for (int k = 0; k < 32; ++k) a[k] = k < w ? ldx<CG>(dst + sp[k]) : 0.0f;
 #pragma unroll 2
         for (int r = 0; r < 32; ++r) {
           if (r < w) {  // block-uniform
@@ -238,10 +264,10 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
             for (int nt = 0; nt < 4; ++nt) {
               const int cc = ct * 32 + nt * 8 + 2 * t4;
               const bool c0k = cc < nc, c1k = cc + 1 < nc;
-              c[nt][0] = oka && c0k ? pa[(int64_t)cc * ldm] : 0.0f;
-              c[nt][1] = oka && c1k ? pa[(int64_t)(cc + 1) * ldm] : 0.0f;
-              c[nt][2] = okb && c0k ? pb[(int64_t)cc * ldm] : 0.0f;
-              c[nt][3] = okb && c1k ? pb[(int64_t)(cc + 1) * ldm] : 0.0f;
+              c[nt][0] = oka && c0k ? ldx<CG>(pa + (int64_t)cc * ldm) : 0.0f;
+              c[nt][1] = oka && c1k ? ldx<CG>(pa + (int64_t)(cc + 1) * ldm) : 0.0f;
+              c[nt][2] = okb && c0k ? ldx<CG>(pb + (int64_t)cc * ldm) : 0.0f;
+              c[nt][3] = okb && c1k ? ldx<CG>(pb + (int64_t)(cc + 1) * ldm) : 0.0f;
             }
           };
           float acc[4][4], nxt[4][4];
@@ -283,6 +309,7 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
       __syncthreads();
       if (cb == 0) stamp(tr, 4);
     }
+    if (NR > 1) cluster_sync();
     stamp(tr, 5);
   }
 }
@@ -520,29 +547,70 @@ __global__ void __launch_bounds__(kPT, 1) patch_refine_kernel(const PatchJob* __
   }
 }
 
+int patch_chunk_cols() { return kPCH; }
+
 int patch_solve_setup() {
   int dev = 0, cap = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
   const int dyn = cap - 12 * 1024;  // room for the kernels' static shared memory
-  if (cudaFuncSetAttribute(patch_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
+  if (cudaFuncSetAttribute(patch_factor_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
+      cudaFuncSetAttribute(patch_factor_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(patch_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
     return 0;
   return dyn;
 }
 
-cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int njobs, size_t smem_factor,
+static cudaError_t launch_factor(const PatchJob* d_jobs, const int* d_order, int njobs, int nr, size_t smem,
+                                 cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  if (nr == 1) {
+    patch_factor_kernel<1><<<njobs, kPT, smem, st>>>(d_jobs, d_order);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(2 * njobs));
+  cfg.blockDim = dim3(kPT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, patch_factor_kernel<2>, d_jobs, d_order);
+}
+
+cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int njobs, int nr, size_t smem_factor,
                               size_t smem_refine, int max_sweeps, double tol, cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
-  if (smem_factor) patch_factor_kernel<<<njobs, kPT, smem_factor, st>>>(d_jobs, d_order);
+  if (smem_factor) {
+    const cudaError_t e = launch_factor(d_jobs, d_order, njobs, nr, smem_factor, st);
+    if (e != cudaSuccess) return e;
+  }
   if (smem_refine) patch_refine_kernel<<<njobs, kPT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
   return cudaGetLastError();
 }
 
-cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int njobs, size_t smem_factor, size_t smem_refine,
-                        int max_sweeps, double tol, cudaStream_t st) {
+cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int nbig, int njobs, size_t smem_factor,
+                        size_t smem_refine, int max_sweeps, double tol, cudaStream_t st, cudaStream_t st2,
+                        cudaEvent_t ev_fork, cudaEvent_t ev_join) {
   if (njobs <= 0) return cudaSuccess;
-  patch_factor_kernel<<<njobs, kPT, smem_factor, st>>>(d_jobs, d_order);
+  cudaError_t e = cudaSuccess;
+  const int nsmall = njobs - nbig;
+  if (nsmall > 0 && nbig > 0) {  // the single-CTA patches beside the clusters, on the second stream
+    e = cudaEventRecord(ev_fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st2, ev_fork, 0);
+    if (e == cudaSuccess) e = launch_factor(d_jobs, d_order, nbig, 2, smem_factor, st);
+    if (e == cudaSuccess) e = launch_factor(d_jobs, d_order + nbig, nsmall, 1, smem_factor, st2);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_join, st2);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_join, 0);
+  } else {
+    e = launch_factor(d_jobs, d_order, njobs, nbig > 0 ? 2 : 1, smem_factor, st);
+  }
+  if (e != cudaSuccess) return e;
   patch_refine_kernel<<<njobs, kPT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
   return cudaGetLastError();
 }
