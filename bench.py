@@ -543,10 +543,11 @@ def run_serving(wl=SERVE):
             cu.sync()
             wall = time.perf_counter() - t0
             st = srv.stats()
-        err, fails = 0.0, 0
+        err, fails, fails_both = 0.0, 0, 0
         for k, (stt, xc, cc) in got.items():
             if stt != M.OK:
                 fails += 1
+                fails_both += ref[k] is None
                 continue
             if ref[k] is not None:
                 err = max(err, _relmax(xc, ref[k][0]), _relmax(cc, ref[k][1]))
@@ -555,7 +556,8 @@ def run_serving(wl=SERVE):
                                    "p50_step_ms": st["p50_step_ms"], "p99_step_ms": st["p99_step_ms"],
                                    "max_step_ms": st["max_step_ms"], "rounds": st["rounds"],
                                    "arrival_span_s": reqs[-1][5] / rate, "wall_s": wall,
-                                   "max_rel_err_vs_plain_fp64": err, "failed_requests": fails}
+                                   "max_rel_err_vs_plain_fp64": err, "failed_requests": fails,
+                                   "failed_requests_also_failing_plain_fp64_alone": fails_both}
     return out
 
 

@@ -18,6 +18,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "mafem.h"
@@ -1248,6 +1249,7 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
 
 namespace {
 struct ServerReq {
+  enum State { IDLE, WAIT_SOLVE, FLIGHT };
   int64_t id = 0;
   mafem_request r{};
   std::vector<double> xms, cps;  // initial state, then the result
@@ -1257,11 +1259,22 @@ struct ServerReq {
   int step = 0;
   double t = 0.0;
   bool in_step = false;
+  State state = IDLE;
   double t_start = 0.0;  // host seconds at the step's first iteration
   int status = MAFEM_OK;
   bool done = false;
   mafem_step_stats last{};
 };
+// One batched FP32 solve in flight: its streams (cluster and single-CTA
+// factorisations), completion event and job order.
+struct SolveLane {
+  cudaStream_t st = nullptr, st2 = nullptr;
+  cudaEvent_t done = nullptr, efork = nullptr, ejoin = nullptr;
+  int* d_order = nullptr;
+  int* h_order = nullptr;  // pinned
+  bool busy = false;
+};
+constexpr int kLanes = 4;
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -1277,31 +1290,33 @@ struct mafem_server {
   std::vector<int> free_slots;
   PatchJob* d_jobs = nullptr;
   PatchJob* h_jobs = nullptr;  // pinned staging of the job table
-  int* d_order = nullptr;
-  int* h_order = nullptr;  // pinned
-  cudaStream_t bst = nullptr, bst2 = nullptr;
-  cudaEvent_t bev = nullptr, efork = nullptr, ejoin = nullptr;
+  cudaStream_t admin = nullptr;  // job-table uploads
+  SolveLane lanes[kLanes];
   size_t smem_dyn = 0;
   std::vector<double> step_ms;  // wall latency of every completed step
   int64_t steps_done = 0, rounds = 0;
   ~mafem_server() {
-    if (bst) cudaStreamSynchronize(bst);
+    for (SolveLane& l : lanes) {
+      if (l.st) cudaStreamSynchronize(l.st);
+      if (l.st2) cudaStreamSynchronize(l.st2);
+    }
     for (ServerReq* q : pending) delete q;
     for (ServerReq* q : active) {
       if (q->h) mafem_destroy(q->h);
       delete q;
     }
     for (auto& kv : finished) delete kv.second;
+    for (SolveLane& l : lanes) {
+      if (l.d_order) cudaFree(l.d_order);
+      if (l.h_order) cudaFreeHost(l.h_order);
+      for (cudaEvent_t e : {l.done, l.efork, l.ejoin})
+        if (e) cudaEventDestroy(e);
+      if (l.st2) cudaStreamDestroy(l.st2);
+      if (l.st) cudaStreamDestroy(l.st);
+    }
     if (d_jobs) cudaFree(d_jobs);
-    if (d_order) cudaFree(d_order);
     if (h_jobs) cudaFreeHost(h_jobs);
-    if (h_order) cudaFreeHost(h_order);
-    if (bev) cudaEventDestroy(bev);
-    if (efork) cudaEventDestroy(efork);
-    if (ejoin) cudaEventDestroy(ejoin);
-    if (bst2) cudaStreamSynchronize(bst2);
-    if (bst2) cudaStreamDestroy(bst2);
-    if (bst) cudaStreamDestroy(bst);
+    if (admin) cudaStreamDestroy(admin);
   }
 };
 
@@ -1318,14 +1333,17 @@ extern "C" int mafem_server_create(int64_t hbm_budget_bytes, int32_t max_active,
   s->max_active = max_active > 0 ? max_active : 1024;
   const size_t m = (size_t)s->max_active;
   e = cudaMalloc(&s->d_jobs, m * sizeof(PatchJob));
-  if (e == cudaSuccess) e = cudaMalloc(&s->d_order, m * sizeof(int));
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_jobs, m * sizeof(PatchJob));
-  if (e == cudaSuccess) e = cudaMallocHost(&s->h_order, m * sizeof(int));
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->bst, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->bst2, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->bev, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->efork, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ejoin, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->admin, cudaStreamNonBlocking);
+  for (SolveLane& l : s->lanes) {
+    if (e == cudaSuccess) e = cudaMalloc(&l.d_order, m * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&l.h_order, m * sizeof(int));
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&l.st2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.efork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.ejoin, cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     set_global_error(std::string("mafem_server_create: ") + cudaGetErrorString(e));
     return MAFEM_ERR_CUDA;
@@ -1381,9 +1399,15 @@ static void server_retire(mafem_server* s, ServerReq* q) {
   s->finished[q->id] = q;
 }
 
+// One pass of the event-driven loop: admit what fits; enqueue the next Newton
+// iteration of every request that is not waiting on the GPU (starting a time
+// step first if it is between steps); hand the FP32 requests whose assembly is
+// enqueued to a free solve lane as one batched launch; collect every request
+// whose iteration has completed.  Requests advance at their own pace: a small
+// patch runs several iterations while a large one runs one.
 extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n_pending) {
   if (!s) return MAFEM_ERR_ARG;
-  // 1. admission, first come first served, while the footprint fits
+  // admission, first come first served, while the footprint fits
   while (!s->pending.empty() && (int)s->active.size() < s->max_active) {
     ServerReq* q = s->pending.front();
     if (s->used + q->est > s->budget) break;
@@ -1408,33 +1432,44 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
       q->slot = s->free_slots.back();
       s->free_slots.pop_back();
       s->h_jobs[q->slot] = h->job;
-      cudaMemcpyAsync(s->d_jobs + q->slot, s->h_jobs + q->slot, sizeof(PatchJob), cudaMemcpyHostToDevice, s->bst);
+      cudaMemcpyAsync(s->d_jobs + q->slot, s->h_jobs + q->slot, sizeof(PatchJob), cudaMemcpyHostToDevice, s->admin);
+      cudaStreamSynchronize(s->admin);
     }
     s->active.push_back(q);
   }
-  // 2. a step for every request between steps: predictor (Analysis.jl:193) + step_begin
-  const double t_round = now_s();
-  for (ServerReq* q : s->active)
-    if (!q->in_step) {
+  std::vector<ServerReq*> retire;
+  // the next iteration of every request not waiting on the GPU
+  const double t_now = now_s();
+  for (ServerReq* q : s->active) {
+    if (q->state != ServerReq::IDLE) continue;
+    if (!q->in_step) {  // predictor (Analysis.jl:193) + step_begin
       launch_predictor(q->h->P, q->h->pp, q->r.dt, q->h->st);
       q->h->launches += 1;
       step_begin(q->h, q->t + q->r.dt, q->r.dt);
       q->in_step = true;
-      q->t_start = t_round;
+      q->t_start = t_now;
     }
-  // 3. one Newton iteration of every active request
-  std::vector<int> st(s->active.size(), MAFEM_OK);
-  std::vector<int> pj;
-  for (size_t k = 0; k < s->active.size(); ++k) {
-    ServerReq* q = s->active[k];
-    const bool patch = q->slot >= 0;
-    const int rc = patch ? iter_enqueue_patch_begin(q->h) : iter_enqueue(q->h);
-    if (rc != MAFEM_OK)
-      st[k] = rc;
-    else if (patch)
-      pj.push_back((int)k);
+    const int rc = q->slot >= 0 ? iter_enqueue_patch_begin(q->h) : iter_enqueue(q->h);
+    if (rc != MAFEM_OK) {
+      q->status = rc;
+      retire.push_back(q);
+      continue;
+    }
+    q->state = q->slot >= 0 ? ServerReq::WAIT_SOLVE : ServerReq::FLIGHT;
   }
-  if (!pj.empty()) {
+  // the waiting FP32 requests as one batched solve on a free lane
+  for (SolveLane& l : s->lanes)
+    if (l.busy && cudaEventQuery(l.done) == cudaSuccess) l.busy = false;
+  std::vector<int> pj;
+  for (size_t k = 0; k < s->active.size(); ++k)
+    if (s->active[k]->state == ServerReq::WAIT_SOLVE && s->active[k]->status == MAFEM_OK) pj.push_back((int)k);
+  SolveLane* lane = nullptr;
+  for (SolveLane& l : s->lanes)
+    if (!l.busy) {
+      lane = &l;
+      break;
+    }
+  if (!pj.empty() && lane) {
     std::vector<mafem_handle*> hv(s->active.size());
     for (size_t k = 0; k < s->active.size(); ++k) hv[k] = s->active[k]->h;
     const int nbig = order_patch_jobs(hv, pj);
@@ -1443,57 +1478,84 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
     double tol = 1.0;
     for (size_t k = 0; k < pj.size(); ++k) {
       mafem_handle* h = s->active[pj[k]]->h;
-      s->h_order[k] = s->active[pj[k]]->slot;
+      lane->h_order[k] = s->active[pj[k]]->slot;
       smf = std::max(smf, patch_factor_smem(h->L.kl));
       smr = std::max(smr, patch_refine_smem(h->L.n));
       max_sw = std::max(max_sw, h->max_refine);
       tol = std::min(tol, h->refine_tol);
-      cudaStreamWaitEvent(s->bst, h->ev[1], 0);
+      cudaStreamWaitEvent(lane->st, h->ev[1], 0);
     }
-    cudaError_t e = cudaMemcpyAsync(s->d_order, s->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice, s->bst);
+    cudaError_t e = cudaMemcpyAsync(lane->d_order, lane->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                    lane->st);
     if (e == cudaSuccess)
-      e = patch_solve(s->d_jobs, s->d_order, nbig, (int)pj.size(), smf, smr, max_sw, tol, s->bst, s->bst2, s->efork,
-                      s->ejoin);
-    if (e == cudaSuccess) e = cudaEventRecord(s->bev, s->bst);
+      e = patch_solve(s->d_jobs, lane->d_order, nbig, (int)pj.size(), smf, smr, max_sw, tol, lane->st, lane->st2,
+                      lane->efork, lane->ejoin);
+    if (e == cudaSuccess) e = cudaEventRecord(lane->done, lane->st);
+    lane->busy = true;
     for (int k : pj) {
-      mafem_handle* h = s->active[k]->h;
+      ServerReq* q = s->active[k];
       if (e != cudaSuccess) {
-        h->err = std::string("batched FP32 solve: ") + cudaGetErrorString(e);
-        st[k] = MAFEM_ERR_CUDA;
+        q->h->err = std::string("batched FP32 solve: ") + cudaGetErrorString(e);
+        q->status = MAFEM_ERR_CUDA;
+        retire.push_back(q);
         continue;
       }
-      if (k == pj[0]) h->launches += 2;
-      const int rc = iter_enqueue_patch_end(h, s->bev);
-      if (rc != MAFEM_OK) st[k] = rc;
+      if (k == pj[0]) q->h->launches += 2;
+      const int rc = iter_enqueue_patch_end(q->h, lane->done);
+      if (rc != MAFEM_OK) {
+        q->status = rc;
+        retire.push_back(q);
+        continue;
+      }
+      q->state = ServerReq::FLIGHT;
     }
   }
-  std::vector<ServerReq*> keep;
-  for (size_t k = 0; k < s->active.size(); ++k) {
-    ServerReq* q = s->active[k];
-    int rc = st[k];
-    if (rc == MAFEM_OK) {
-      rc = iter_finish(q->h);
-      if (rc == kIterAgain) {
-        keep.push_back(q);
-        continue;
-      }
-      if (rc == kIterDone) {
-        step_stats(q->h, &q->last);
-        s->step_ms.push_back((now_s() - q->t_start) * 1e3);
-        ++s->steps_done;
-        q->t += q->r.dt;
-        q->in_step = false;
-        if (++q->step < q->r.nsteps) {
-          keep.push_back(q);
-          continue;
-        }
-        rc = MAFEM_OK;
-      }
+  // collect finished iterations
+  bool progressed = false;
+  for (ServerReq* q : s->active) {
+    if (q->state != ServerReq::FLIGHT || q->status != MAFEM_OK) continue;
+    const cudaError_t qe = cudaEventQuery(q->h->ev[4]);
+    if (qe == cudaErrorNotReady) continue;
+    progressed = true;
+    q->state = ServerReq::IDLE;
+    int rc = qe == cudaSuccess ? iter_finish(q->h) : MAFEM_ERR_CUDA;
+    if (qe != cudaSuccess) q->h->err = std::string("iteration: ") + cudaGetErrorString(qe);
+    if (rc == kIterAgain) continue;
+    if (rc == kIterDone) {
+      step_stats(q->h, &q->last);
+      s->step_ms.push_back((now_s() - q->t_start) * 1e3);
+      ++s->steps_done;
+      q->t += q->r.dt;
+      q->in_step = false;
+      if (++q->step < q->r.nsteps) continue;
+      rc = MAFEM_OK;
     }
     q->status = rc;
-    server_retire(s, q);
+    retire.push_back(q);
   }
-  s->active.swap(keep);
+  if (!retire.empty()) {
+    std::vector<ServerReq*> keep;
+    for (ServerReq* q : s->active)
+      if (std::find(retire.begin(), retire.end(), q) == retire.end()) keep.push_back(q);
+    // A request retired on an error path may still be read by a batched solve
+    // in flight on some lane: wait for the lanes before its memory is freed.
+    // (A request whose iteration completed normally is past its lane's solve:
+    // its update waited on it.)
+    bool drain = false;
+    for (ServerReq* q : retire) drain |= q->status != MAFEM_OK && q->status != MAFEM_NEWTON_NOT_CONVERGED;
+    if (drain)
+      for (SolveLane& l : s->lanes) {
+        cudaStreamSynchronize(l.st);
+        cudaStreamSynchronize(l.st2);
+        l.busy = false;
+      }
+    for (ServerReq* q : retire) {
+      if (q->h) cudaStreamSynchronize(q->h->st);
+      server_retire(s, q);
+    }
+    s->active.swap(keep);
+  }
+  if (!progressed && !s->active.empty()) std::this_thread::sleep_for(std::chrono::microseconds(20));
   ++s->rounds;
   if (n_active) *n_active = (int32_t)s->active.size();
   if (n_pending) *n_pending = (int32_t)s->pending.size();
