@@ -292,7 +292,10 @@ int mafem_server_get_stats(const mafem_server* s, mafem_server_stats* out);
  * this handle alone, its factorisation traced -- 6 globaltimer stamps (ns) per
  * panel in out[6p .. 6p+5] (start, diagonal block factored, panel staged and
  * inverses formed, first chunk's U12/Y, its trailing update, panel done), then
- * the factor and refine kernels' event times in ns.  cap >= 6 npan + 2.
+ * the factor and refine kernels' event times in ns, then 4 stamps per
+ * refinement sweep for up to 32 sweeps (start, substitutions done, x updated,
+ * residual done; 0 where not reached), then 16 phase sums (ns) of the first
+ * sweep's substitutions (see patch_lu_solve).  cap >= 6 npan + 146.
  * Returns npan, or MAFEM_ERR_UNSUPPORTED if the handle cannot use that solve. */
 int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap);
 

@@ -494,7 +494,9 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     mafem_destroy(hp.release());
     return MAFEM_ERR_OOM;
   }
-  if (precision != MAFEM_PLAIN_FP64 && h->use_blk) {
+  // (the refinement residual reads every band window without bounds checks:
+  // it needs nb >= 32 rows of padding)
+  if (precision != MAFEM_PLAIN_FP64 && h->use_blk && h->L.nb >= 32) {
     const int dyn = patch_solve_setup();
     cudaGetLastError();
     if (dyn > 0 && patch_factor_smem(h->L.kl) <= (size_t)dyn && patch_refine_smem(n) <= (size_t)dyn) {
@@ -1696,18 +1698,19 @@ extern "C" int mafem_trace_factor(mafem_handle* h, double time, double dt, int64
 extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap) {
   if (!h || !out || !h->patch_ok) return MAFEM_ERR_UNSUPPORTED;
   const int npan = h->blk.npan();
-  if (cap < 6LL * npan + 2) return MAFEM_ERR_ARG;
+  const int64_t ntr = 6LL * npan + 4 * 32 + 16;  // factor stamps, 4 per refinement sweep (up to 32), 16 phase sums
+  if (cap < ntr + 2) return MAFEM_ERR_ARG;  // 6 npan + 146
   long long* d_tr = nullptr;
   PatchJob* d_job = nullptr;
   int* d_ord = nullptr;
-  CK(cudaMalloc(&d_tr, sizeof(long long) * 6 * npan));
+  CK(cudaMalloc(&d_tr, sizeof(long long) * ntr));
   CK(cudaMalloc(&d_job, sizeof(PatchJob)));
   CK(cudaMalloc(&d_ord, sizeof(int)));
   PatchJob J = h->job;
   J.trace = d_tr;
   CK(cudaMemcpyAsync(d_job, &J, sizeof J, cudaMemcpyHostToDevice, h->st));
   CK(cudaMemsetAsync(d_ord, 0, sizeof(int), h->st));
-  CK(cudaMemsetAsync(d_tr, 0, sizeof(long long) * 6 * npan, h->st));
+  CK(cudaMemsetAsync(d_tr, 0, sizeof(long long) * ntr, h->st));
   int rc = assemble(h, time, dt, true);
   if (rc) return rc;
   CK(cudaMemsetAsync(h->d_info, 0, 4 * sizeof(int), h->st));
@@ -1722,15 +1725,16 @@ extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, 
   cudaEventRecord(e1, h->st);
   patch_solve_stage(d_job, d_ord, 1, 1, 0, patch_refine_smem(h->L.n), h->max_refine, h->refine_tol, h->st);
   cudaEventRecord(e2, h->st);
-  std::vector<long long> tr((size_t)6 * npan);
+  std::vector<long long> tr((size_t)ntr);
   CK(cudaMemcpyAsync(tr.data(), d_tr, tr.size() * sizeof(long long), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
   float mf = 0, mr = 0;
   cudaEventElapsedTime(&mf, e0, e1);
   cudaEventElapsedTime(&mr, e1, e2);
-  for (size_t k = 0; k < tr.size(); ++k) out[k] = tr[k];
+  for (int64_t k = 0; k < 6LL * npan; ++k) out[k] = tr[(size_t)k];
   out[6 * npan] = (int64_t)(mf * 1e6);
   out[6 * npan + 1] = (int64_t)(mr * 1e6);
+  for (int64_t k = 0; k < 4 * 32 + 16; ++k) out[6 * npan + 2 + k] = tr[(size_t)(6 * npan + k)];
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaEventDestroy(e2);

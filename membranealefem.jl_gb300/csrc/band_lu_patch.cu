@@ -34,7 +34,8 @@
 
 namespace mafem {
 
-constexpr int kPT = 512;   // threads per CTA (16 warps)
+constexpr int kPT = 512;   // threads per CTA of the factorisation (16 warps)
+constexpr int kRT = 768;   // threads per CTA of the refinement (24 warps)
 constexpr int kPCH = 288;      // trailing columns per chunk (a 32 x 32 patch's ~550 in two)
 constexpr int kYS = kPCH + 8;  // row stride of Y (uint2 hi/lo pairs) in shared memory
 constexpr int kIS = 36;    // shared-memory row stride of the 32 x 32 inverses (16-byte rows)
@@ -170,15 +171,15 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
       for (int i = 0; i < 32; ++i) X[i * kIS + lane] = (lane < w && i < w) ? x[i] : 0.0f;
     }
     __syncthreads();
-    float* inv = J.inv + (size_t)p * 2 * kBlkW * kBlkW;  // Li then Ui, row-major 32 x 32
+    float* inv = J.inv + (size_t)p * 2 * kBlkW * kBlkW;  // Li then Ui, 32 x 32, column-major
     for (int idx = tid; idx < kBlkW * kBlkW; idx += kPT) {
       const int i = idx >> 5, c = idx & 31;
       float s = 0.0f;
       for (int k = max(i, c); k < w; ++k) s = fmaf(Ui[i * kIS + k], Li[k * kIS + c], s);
       Mi[i * kIS + c] = s;
-      if (rank == 0) {
-        inv[idx] = Li[i * kIS + c];
-        inv[kBlkW * kBlkW + idx] = Ui[i * kIS + c];
+      if (rank == 0) {  // stored transposed: element (i, c) at c * 32 + i
+        inv[c * kBlkW + i] = Li[i * kIS + c];
+        inv[kBlkW * kBlkW + c * kBlkW + i] = Ui[i * kIS + c];
       }
     }
     __syncthreads();
@@ -324,96 +325,181 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   double s = 0.0;
-  for (int q = 0; q < kPT / 32; ++q) s += red[q];  // same order in every thread
+  for (int q = 0; q < kRT / 32; ++q) s += red[q];  // same order in every thread
   return s;
 }
 
-// row `lane` of a 32 x 32 row-major matrix in global memory, as registers
-__device__ __forceinline__ void load_row32(const float* m, int lane, float r[32]) {
-  const float4* q = reinterpret_cast<const float4*>(m + lane * 32);
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const float4 t = q[k];
-    r[4 * k] = t.x;
-    r[4 * k + 1] = t.y;
-    r[4 * k + 2] = t.z;
-    r[4 * k + 3] = t.w;
-  }
+// 16-byte global -> shared copy, L2 only (16-byte aligned addresses)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
 }
 
-// v <- (L U)^-1 v with the stored factors and inverses
-__device__ void patch_lu_solve(const PatchJob& J, float* v, float* bz, float (*part)[33]) {
+constexpr int kTraceSweeps = 32;  // sweeps the refinement trace records
+constexpr int kFwdRows = 1;       // A21 rows per thread (warps 1..31) whose loads run ahead
+constexpr int kBwdCols = 24;      // U12 columns per warp whose loads run ahead
+
+// v <- (L U)^-1 v with the stored factors and inverses.  Every panel step
+// waits for one round trip at most: the next panel's inverses are copied into
+// a second shared buffer while the current panel is processed, and each
+// thread loads its next A21 rows (forward) or U12 columns (backward) into
+// registers as soon as it has used the current ones.
+// inv_s: 2 x (2 x 32 x 32) floats of shared memory, 16-byte aligned.
+// prof (trace mode, optional): thread 0 and thread 32 add the globaltimer
+// time of each phase -- [0..3] thread 0 forward: wait + barrier, warp-0 work,
+// barrier, row update; [4..7] thread 32 the same; [8..11] thread 0 backward:
+// partial sums + prefetch, wait + barrier, warp-0 work, barrier; [12..15] thread 32
+__device__ __forceinline__ long long gtime() {
+  unsigned long long v;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
+  return (long long)v;
+}
+__device__ void patch_lu_solve(const PatchJob& J, float* v, float* bz, float (*part)[33], float* inv_s,
+                               long long* prof) {
+  const bool pt = prof && (threadIdx.x == 0 || threadIdx.x == 32);
+  const int po = threadIdx.x == 32 ? 4 : 0;
+  long long tk = pt ? gtime() : 0;
+  auto lap = [&](int slot) {
+    if (pt) {
+      const long long t1 = gtime();
+      prof[slot] += t1 - tk;
+      tk = t1;
+    }
+  };
   const BandLayout L = J.L;
   const float* __restrict__ ab = J.band;
   const int64_t ldm = L.ldb - 1;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // forward: per panel y1 = Li P b1, z = Ui y1, b2 -= A21 z
-  for (int p = 0; p < J.npan; ++p) {
+  const int npan = J.npan;
+  constexpr int kInv = 2 * kBlkW * kBlkW;  // floats per panel: Li then Ui, column-major
+  auto inv_copy = [&](int p, int buf) {  // 512 threads x 16 bytes = one panel's Li and Ui
+    if (p >= 0 && p < npan && tid < kInv / 4)
+      cp_async16(inv_s + buf * kInv + tid * 4, J.inv + (size_t)p * kInv + tid * 4);
+    cp_async_commit();
+  };
+  // ---- forward: per panel y1 = Li P b1, z = Ui y1, b2 -= A21 z
+  const int rt = tid - 32;  // row slot of warps 1..15
+  float t[kFwdRows][32];
+  auto fwd_load = [&](int p) {  // this thread's A21 rows of panel p
+    if (rt < 0 || p >= npan) return;
     const int64_t j0 = J.ps[p], j1 = J.ps[p + 1];
     const int w = (int)(j1 - j0);
-    const int R = (int)min64b(L.n - j0, (int64_t)w + L.kl);
+    const int64_t rend = j0 + min64b(L.n - j0, (int64_t)w + L.kl);
+#pragma unroll
+    for (int q = 0; q < kFwdRows; ++q) {
+      const int64_t i = j1 + rt + (int64_t)q * (kRT - 32);
+      const float* a = ab + bix(L, i, j0);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) t[q][k] = (i < rend && k < w) ? a[k * ldm] : 0.0f;
+    }
+  };
+  inv_copy(0, 0);
+  fwd_load(0);
+  int pnext = warp == 0 && lane < J.ps[1] - J.ps[0] ? J.perm[lane] : 0;  // panel 0's permutation
+  for (int p = 0; p < npan; ++p) {
+    const int64_t j0 = J.ps[p], j1 = J.ps[p + 1];
+    const int w = (int)(j1 - j0);
+    const int64_t rend = j0 + min64b(L.n - j0, (int64_t)w + L.kl);
+    inv_copy(p + 1, (p + 1) & 1);
+    cp_async_wait_group<1>();  // this panel's inverses (this thread's part)
+    __syncthreads();
+    lap(po + 0);
+    const float* Li = inv_s + (p & 1) * kInv;
+    const float* Ui = Li + kBlkW * kBlkW;
     if (warp == 0) {
-      const float* inv = J.inv + (size_t)p * 2 * kBlkW * kBlkW;
-      float li[32], ui[32];
-      load_row32(inv, lane, li);
-      load_row32(inv + kBlkW * kBlkW, lane, ui);
-      const float b = lane < w ? v[j0 + J.perm[(size_t)p * kBlkW + lane]] : 0.0f;
+      const int pm = pnext;
+      if (p + 1 < npan && lane < J.ps[p + 2] - j1) pnext = J.perm[(size_t)(p + 1) * kBlkW + lane];
+      const float b = lane < w ? v[j0 + pm] : 0.0f;
       float y = 0.0f;
 #pragma unroll
-      for (int k = 0; k < 32; ++k) y = fmaf(li[k], __shfl_sync(kFull, b, k), y);
+      for (int k = 0; k < 32; ++k) y = fmaf(Li[k * 32 + lane], __shfl_sync(kFull, b, k), y);
       float z = 0.0f;
 #pragma unroll
-      for (int k = 0; k < 32; ++k) z = fmaf(ui[k], __shfl_sync(kFull, y, k), z);
+      for (int k = 0; k < 32; ++k) z = fmaf(Ui[k * 32 + lane], __shfl_sync(kFull, y, k), z);
       if (lane < w) v[j0 + lane] = y;
       bz[lane] = lane < w ? z : 0.0f;
     }
+    lap(po + 1);
     __syncthreads();
-    for (int64_t i = j1 + tid; i < j0 + R; i += kPT) {
-      const float* a = ab + bix(L, i, j0);
-      float t[32];
+    lap(po + 2);
+    if (rt >= 0) {
 #pragma unroll
-      for (int k = 0; k < 32; ++k) t[k] = k < w ? a[k * ldm] : 0.0f;  // all loads in flight
-      float s = 0.0f;
+      for (int q = 0; q < kFwdRows; ++q) {
+        const int64_t i = j1 + rt + (int64_t)q * (kRT - 32);
+        if (i < rend) {
+          float sacc = 0.0f;
 #pragma unroll
-      for (int k = 0; k < 32; ++k) s = fmaf(t[k], bz[k], s);
-      v[i] -= s;
+          for (int k = 0; k < 32; ++k) sacc = fmaf(t[q][k], bz[k], sacc);
+          v[i] -= sacc;
+        }
+      }
+      // rows beyond kFwdRows slots (very wide bands): loaded on the spot
+      for (int64_t i = j1 + rt + (int64_t)kFwdRows * (kRT - 32); i < rend; i += kRT - 32) {
+        const float* a = ab + bix(L, i, j0);
+        float sacc = 0.0f;
+        for (int k = 0; k < w; ++k) sacc = fmaf(a[k * ldm], bz[k], sacc);
+        v[i] -= sacc;
+      }
+      fwd_load(p + 1);
     }
-    __syncthreads();
+    lap(po + 3);
   }
-  // backward: per panel x1 = Ui (y1 - U12 x2)
-  for (int p = J.npan - 1; p >= 0; --p) {
+  cp_async_wait_group<0>();
+  __syncthreads();
+  tk = pt ? gtime() : 0;
+  // ---- backward: per panel x1 = Ui (y1 - U12 x2)
+  float u[kBwdCols];
+  auto bwd_load = [&](int p) {  // this lane's row of U12 in this warp's columns, panel p
+    if (p < 0) return;
     const int64_t j0 = J.ps[p], j1 = J.ps[p + 1];
     const int w = (int)(j1 - j0);
     const int C = (int)(min64b(L.n, j1 + J.kuf) - j1);
+    const float* ur = ab + bix(L, j0 + lane, j1);  // U(j0 + lane, j1 + c) = ur[c * ldm]
+#pragma unroll
+    for (int m = 0; m < kBwdCols; ++m) {
+      const int c = warp + m * (kRT / 32);
+      u[m] = (lane < w && c < C) ? ur[(int64_t)c * ldm] : 0.0f;
+    }
+  };
+  inv_copy(npan - 1, (npan - 1) & 1);
+  bwd_load(npan - 1);
+  for (int p = npan - 1; p >= 0; --p) {
+    const int64_t j0 = J.ps[p], j1 = J.ps[p + 1];
+    const int w = (int)(j1 - j0);
+    const int C = (int)(min64b(L.n, j1 + J.kuf) - j1);
+    inv_copy(p - 1, (p - 1) & 1);
     float acc = 0.0f;
-    if (lane < w) {
-      const float* u = ab + bix(L, j0 + lane, j1);  // U(j0 + lane, j1 + c) = u[c * ldm]
-      for (int c = warp; c < C; c += 8 * (kPT / 32)) {
-        float t[8];
 #pragma unroll
-        for (int m = 0; m < 8; ++m) {
-          const int cc = c + m * (kPT / 32);
-          t[m] = cc < C ? u[(int64_t)cc * ldm] * v[j1 + cc] : 0.0f;
-        }
-#pragma unroll
-        for (int m = 0; m < 8; ++m) acc += t[m];
-      }
+    for (int m = 0; m < kBwdCols; ++m) {
+      const int c = warp + m * (kRT / 32);
+      if (c < C) acc = fmaf(u[m], v[j1 + c], acc);
+    }
+    if (lane < w) {  // columns beyond kBwdCols slots (very wide bands): loaded on the spot
+      const float* ur = ab + bix(L, j0 + lane, j1);
+      for (int c = warp + kBwdCols * (kRT / 32); c < C; c += kRT / 32) acc = fmaf(ur[(int64_t)c * ldm], v[j1 + c], acc);
     }
     part[warp][lane] = acc;
+    bwd_load(p - 1);
+    lap(8 + po);
+    cp_async_wait_group<1>();  // this panel's inverses
     __syncthreads();
+    lap(9 + po);
     if (warp == 0) {
-      float ui[32];
-      load_row32(J.inv + (size_t)p * 2 * kBlkW * kBlkW + kBlkW * kBlkW, lane, ui);
-      float s = 0.0f;
-      for (int q = 0; q < kPT / 32; ++q) s += part[q][lane];
-      const float t = lane < w ? v[j0 + lane] - s : 0.0f;
+      const float* Ui = inv_s + (p & 1) * kInv + kBlkW * kBlkW;
+      float sum = 0.0f;
+      for (int q = 0; q < kRT / 32; ++q) sum += part[q][lane];
+      const float tv = lane < w ? v[j0 + lane] - sum : 0.0f;
       float x = 0.0f;
 #pragma unroll
-      for (int k = 0; k < 32; ++k) x = fmaf(ui[k], __shfl_sync(kFull, t, k), x);
+      for (int k = 0; k < 32; ++k) x = fmaf(Ui[k * 32 + lane], __shfl_sync(kFull, tv, k), x);
       if (lane < w) v[j0 + lane] = x;
     }
+    lap(10 + po);
     __syncthreads();
+    lap(11 + po);
   }
+  cp_async_wait_group<0>();
+  __syncthreads();
 }
 
 // res = rhs - A0 x (A0: the unfactored FP32 band); returns |res|.  The
@@ -424,39 +510,51 @@ __device__ void patch_lu_solve(const PatchJob& J, float* v, float* bz, float (*p
 // refinement tolerance, at a sixth of the cost of FP64 FMAs on this GPU.
 __device__ double patch_residual(const PatchJob& J, const float2* xs, double* red) {
   const BandLayout L = J.L;
-  const float* __restrict__ a0 = J.band0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t ldm = L.ldb - 1;
   double ss = 0.0;
-  for (int64_t rb = (int64_t)warp * 32; rb < L.n; rb += kPT) {
+  // A warp takes 32 rows and walks the columns j of their band window; with
+  // nb >= 32 every (i, j) it visits lies inside the band's storage, where the
+  // entries outside the band are stored zeros, so A0(i, j) = a[j * ldm + lane]
+  // with a at row rb of column 0 needs no guard but i < n.
+  for (int64_t rb = (int64_t)warp * 32; rb < L.n; rb += kRT) {
     const int64_t i = rb + lane;
+    const bool live = i < L.n;
     const int64_t jlo = rb - L.ku > 0 ? rb - L.ku : 0;
     const int64_t jhi = min64b(L.n, rb + 32 + L.kl);
+    const float* a = J.band0 + L.off + (live ? i : rb);  // + j * ldm: A0(i, j)
     float sh = 0.0f, sl = 0.0f;
-    if (i < L.n)
-      for (int64_t jb = jlo; jb < jhi; jb += 8) {
-        float av[8];
-        float2 xv[8];
+    int64_t j = jlo;
+    for (; j + 8 <= jhi; j += 8) {
+      float av[8];
+      float2 xv[8];
 #pragma unroll
-        for (int m = 0; m < 8; ++m) {  // all loads in flight
-          const int64_t j = jb + m;
-          const bool in = j < jhi && i - j <= L.kl && j - i <= L.ku;
-          av[m] = in ? a0[bix(L, i, j)] : 0.0f;
-          xv[m] = in ? xs[j] : make_float2(0.0f, 0.0f);
-        }
-#pragma unroll
-        for (int m = 0; m < 8; ++m) {
-          const float a = av[m];
-          const float2 x = xv[m];
-          // explicit roundings: a contraction of p into t would break TwoSum
-          const float p = __fmul_rn(a, x.x);
-          const float e = fmaf(a, x.y, fmaf(a, x.x, -p));
-          const float t = __fadd_rn(sh, p);
-          const float z = __fsub_rn(t, sh);
-          sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
-          sh = t;
-        }
+      for (int m = 0; m < 8; ++m) {  // all loads in flight
+        av[m] = a[(j + m) * ldm];
+        xv[m] = xs[j + m];
       }
-    if (i < L.n) {
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        // explicit roundings: a contraction of p into t would break TwoSum
+        const float p = __fmul_rn(av[m], xv[m].x);
+        const float e = fmaf(av[m], xv[m].y, fmaf(av[m], xv[m].x, -p));
+        const float t = __fadd_rn(sh, p);
+        const float z = __fsub_rn(t, sh);
+        sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+        sh = t;
+      }
+    }
+    for (; j < jhi; ++j) {
+      const float av = a[j * ldm];
+      const float2 xv = xs[j];
+      const float p = __fmul_rn(av, xv.x);
+      const float e = fmaf(av, xv.y, fmaf(av, xv.x, -p));
+      const float t = __fadd_rn(sh, p);
+      const float z = __fsub_rn(t, sh);
+      sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+      sh = t;
+    }
+    if (live) {
       const double r = J.rhs[i] - ((double)sh + (double)sl);
       J.res[i] = r;
       ss = fma(r, r, ss);
@@ -465,15 +563,16 @@ __device__ double patch_residual(const PatchJob& J, const float2* xs, double* re
   return sqrt(block_sum(ss, red));
 }
 
-__global__ void __launch_bounds__(kPT, 1) patch_refine_kernel(const PatchJob* __restrict__ jobs,
+__global__ void __launch_bounds__(kRT, 1) patch_refine_kernel(const PatchJob* __restrict__ jobs,
                                                              const int* __restrict__ order, int max_sweeps,
                                                              double tol) {
   const PatchJob& J = jobs[order[blockIdx.x]];
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* v = reinterpret_cast<float*>(smem_raw);  // [n]
   __shared__ float bz[32];  // zero beyond the panel width
-  __shared__ float part[kPT / 32][33];
-  __shared__ double red[kPT / 32];
+  __shared__ float part[kRT / 32][33];
+  __shared__ __align__(16) float inv_s[2 * 2 * kBlkW * kBlkW];  // double-buffered panel inverses
+  __shared__ double red[kRT / 32];
   const int tid = threadIdx.x;
   const int64_t n = J.L.n;
   int* stat = J.stat;  // [0] status, [1] sweeps
@@ -486,13 +585,16 @@ __global__ void __launch_bounds__(kPT, 1) patch_refine_kernel(const PatchJob* __
     return;
   }
   double ss = 0.0;
-  for (int64_t i = tid; i < n; i += kPT) {
+  for (int64_t i = tid; i < n; i += kRT) {
     const double r = J.rhs[i];
     J.res[i] = r;
     J.x[i] = 0.0;
     ss = fma(r, r, ss);
   }
   const double r0 = sqrt(block_sum(ss, red));
+  // trace: per sweep 4 stamps after J.trace's 6 per panel -- [0] sweep start,
+  // [1] substitutions done, [2] x updated and norms formed, [3] residual done
+  long long* tr = J.trace ? J.trace + (size_t)J.npan * 6 : nullptr;
   // Stop when the last correction is small against x: |d| <= tol |x| bounds
   // the forward error of x (about rho |d| with rho < 1 the sweep's
   // contraction) whatever the conditioning, where a residual test would
@@ -503,12 +605,15 @@ __global__ void __launch_bounds__(kPT, 1) patch_refine_kernel(const PatchJob* __
   if (r0 > 0.0) {
     status = MAFEM_REFINE_STALLED;
     for (int k = 0; k < max_sweeps; ++k) {
+      long long* trk = tr && k < kTraceSweeps ? tr + 4 * k : nullptr;
+      stamp(trk, 0);
       const double sc = 1.0 / rn;
-      for (int64_t i = tid; i < n; i += kPT) v[i] = (float)(J.res[i] * sc);
+      for (int64_t i = tid; i < n; i += kRT) v[i] = (float)(J.res[i] * sc);
       __syncthreads();
-      patch_lu_solve(J, v, bz, part);
+      patch_lu_solve(J, v, bz, part, inv_s, tr && k == 0 ? tr + 4 * kTraceSweeps : nullptr);
+      stamp(trk, 1);
       double dd = 0.0, xx = 0.0;
-      for (int64_t i = tid; i < n; i += kPT) {
+      for (int64_t i = tid; i < n; i += kRT) {
         const double d = rn * (double)v[i];
         const double x = J.x[i] + d;
         J.x[i] = x;
@@ -519,6 +624,7 @@ __global__ void __launch_bounds__(kPT, 1) patch_refine_kernel(const PatchJob* __
       }
       const double dn = sqrt(block_sum(dd, red));
       const double xn = sqrt(block_sum(xx, red));
+      stamp(trk, 2);
       sweeps = k + 1;
       if (!isfinite(dn) || !isfinite(xn)) {
         status = MAFEM_NAN_DETECTED;
@@ -531,6 +637,7 @@ __global__ void __launch_bounds__(kPT, 1) patch_refine_kernel(const PatchJob* __
       if (k >= 3 && dn > 0.5 * prev_dn) break;  // stalled
       prev_dn = dn;
       rn = patch_residual(J, xs, red);  // block_sum orders the x / xs writes before it
+      stamp(trk, 3);
       if (!isfinite(rn)) {
         status = MAFEM_NAN_DETECTED;
         break;
@@ -553,7 +660,7 @@ int patch_solve_setup() {
   int dev = 0, cap = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   if (cudaDeviceGetAttribute(&cap, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
-  const int dyn = cap - 12 * 1024;  // room for the kernels' static shared memory
+  const int dyn = cap - 20 * 1024;  // room for the kernels' static shared memory (refine: ~19 KB)
   if (cudaFuncSetAttribute(patch_factor_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(patch_factor_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(patch_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
@@ -590,7 +697,7 @@ cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int nj
     const cudaError_t e = launch_factor(d_jobs, d_order, njobs, nr, smem_factor, st);
     if (e != cudaSuccess) return e;
   }
-  if (smem_refine) patch_refine_kernel<<<njobs, kPT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
+  if (smem_refine) patch_refine_kernel<<<njobs, kRT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
   return cudaGetLastError();
 }
 
@@ -611,7 +718,7 @@ cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int nbig, in
     e = launch_factor(d_jobs, d_order, njobs, nbig > 0 ? 2 : 1, smem_factor, st);
   }
   if (e != cudaSuccess) return e;
-  patch_refine_kernel<<<njobs, kPT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
+  patch_refine_kernel<<<njobs, kRT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
   return cudaGetLastError();
 }
 

@@ -206,7 +206,7 @@ namespace mafem {
 struct PatchJob {
   float* band;          // factored in place
   const float* band0;   // the unfactored band (refinement residual)
-  float* inv;           // [npan][2][32][32]: L11^-1, U11^-1 per panel
+  float* inv;           // [npan][2][32][32]: L11^-1, U11^-1 per panel, column-major
   const int* ps;        // panel starts [npan + 1]
   const int* blk_end;   // [n]
   int* perm;            // [npan][32]
