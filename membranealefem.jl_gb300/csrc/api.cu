@@ -122,6 +122,7 @@ struct mafem_handle {
   int64_t fallbacks = 0;
   // batched FP32 form (band_lu_patch.cu): the handle's job, usable when its band fits
   float* d_inv = nullptr;
+  double* d_zbuf = nullptr;  // npan x 32: z = U11^-1 y1 per panel (cooperative forward substitution)
   bool patch_ok = false;
   bool ss_patch = false;  // the iteration in progress ran through a batch's patch solve
   PatchJob job{};
@@ -449,6 +450,7 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
       h->blk.d_blk_end = h->d_blk_end;
       h->use_blk = true;
       AL(h->d_flags, (size_t)h->blk.npan());
+      AL(h->d_zbuf, (size_t)h->blk.npan() * kBlkW);
       cudaMemsetAsync(h->d_flags, 0, (size_t)h->blk.npan() * sizeof(int), h->st);
       h->bwd_grid = precision == MAFEM_PLAIN_FP64 ? blk_backward_grid<double, double>() : blk_backward_grid<double, float>();
       h->bwd_max = h->bwd_grid;
@@ -748,6 +750,23 @@ static void blk_back_solve(mafem_handle* h, double* y) {
   h->launches += 1;
 }
 
+// Forward substitution with the node-block factors, in place on y (device):
+// the cooperative multi-CTA kernel where the device allows it.
+template <class T>
+static void blk_fwd_solve(mafem_handle* h, double* y) {
+  if (h->bwd_grid > 0) {
+    ++h->epoch;
+    if (blk_forward_coop<double, T>((const T*)h->d_band, h->L, h->blk, h->d_perm, (const T*)h->d_rdiag, y, h->d_zbuf,
+                                    h->d_flags, h->epoch, h->d_info + 1, h->bwd_grid, h->st) == 0) {
+      h->launches += 1;
+      return;
+    }
+    cudaGetLastError();
+  }
+  blk_forward<double, T>((const T*)h->d_band, h->L, h->blk, h->d_perm, (const T*)h->d_rdiag, y, h->st);
+  h->launches += 1;
+}
+
 // info[0]: zero-pivot column, info[1]: a bounded device wait ran out (h_out + 5 holds both)
 static int check_info(mafem_handle* h) {
   int info[2] = {0, 0};
@@ -774,9 +793,7 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
       int rc = factor(h, h->d_x, rhs_dev);
       if (rc) return rc;
     } else if (h->last_blk) {
-      blk_forward<double, double>((const double*)h->d_band, h->L, h->blk, h->d_perm, (const double*)h->d_rdiag,
-                                  h->d_x, h->st);
-      h->launches += 1;
+      blk_fwd_solve<double>(h, h->d_x);
     } else {
       band_forward<double, double>((const double*)h->d_band, h->L, h->d_perm, h->rmax, h->d_x, h->st);
       h->launches += 1;
@@ -812,17 +829,17 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   for (int k = 0; k < h->max_refine; ++k) {
     CK(cudaMemcpyAsync(h->d_dx, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     if (h->last_blk) {
-      blk_forward<double, float>((const float*)h->d_band, h->L, h->blk, h->d_perm, (const float*)h->d_rdiag, h->d_dx,
-                                 h->st);
+      blk_fwd_solve<float>(h, h->d_dx);
       blk_back_solve<float>(h, h->d_dx);
     } else {
       band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
       band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
+      h->launches += 2;
     }
     launch_axpy(n, h->d_dx, h->d_x, h->st);
     launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part,
                                 h->d_out + 3, h->st);
-    h->launches += 5;
+    h->launches += 3;
     CK(cudaMemcpyAsync(h->h_out + 3, h->d_out + 3, sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     *sweeps = k + 1;

@@ -383,6 +383,78 @@ __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restr
 }
 
 // ---------------------------------------------------------------------------
+// Forward substitution on many SMs: one cooperative launch, panel p handled by
+// CTA p mod gridDim.x in increasing order.  For its panel's rows a CTA gathers
+// the contributions A21(q) z(q) of the earlier panels q whose rows reach them
+// (rows of panel q end at ps[q + 1] + kl), each as soon as q's flag appears,
+// then applies the panel's interchanges and triangles like blk_forward_kernel:
+// y1 = L11^-1 P b1 replaces b1 in place, z = U11^-1 y1 goes to zbuf[p] with a
+// release store of the flag.  A panel waits only for lower-numbered panels,
+// which CTAs take in increasing order, so the chain always progresses; waits
+// are bounded (kSpinLimit polls, then *err and every CTA returns).
+template <class T, class V>
+__global__ void __launch_bounds__(256) blk_forward_coop_kernel(const T* __restrict__ ab, BandLayout L,
+                                                               const int* __restrict__ ps, int npan,
+                                                               const int* __restrict__ perm_all,
+                                                               const T* __restrict__ rdiag, V* b, V* zbuf,
+                                                               int* flags, int epoch, int* err) {
+  __shared__ V part[8][33];
+  __shared__ V Ls[32][33];
+  __shared__ V accs[32];
+  __shared__ int s_ok;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int p = blockIdx.x; p < npan; p += gridDim.x) {
+    const int64_t j0 = ps[p], j1 = ps[p + 1];
+    const int w = (int)(j1 - j0);
+    for (int k = tid; k < w * w; k += 256) {
+      const int c = k / w, i = k - c * w;
+      Ls[c][i] = V(ab[bix(L, j0 + i, j0 + c)]);
+    }
+    int pf = p;  // earliest panel whose rows reach j0
+    while (pf > 0 && ps[pf] + L.kl > j0) --pf;
+    V acc = V(0);
+    for (int q = pf; q < p; ++q) {
+      if (!wait_flag(flags, q, epoch, err, &s_ok)) return;
+      const int64_t q0 = ps[q];
+      const int wq = ps[q + 1] - ps[q];
+      if (lane < w)
+        for (int k = warp; k < wq; k += 8)
+          if (j0 + lane - (q0 + k) <= L.kl)  // inside panel q's band rows
+            acc += V(ab[bix(L, j0 + lane, q0 + k)]) * __ldcg(zbuf + (size_t)q * kBlkW + k);
+    }
+    part[warp][lane] = acc;
+    __syncthreads();
+    if (warp == 0) {
+      accs[lane] = ((part[0][lane] + part[1][lane]) + (part[2][lane] + part[3][lane])) +
+                   ((part[4][lane] + part[5][lane]) + (part[6][lane] + part[7][lane]));
+      __syncwarp();
+      const int pr = lane < w ? perm_all[(size_t)p * kBlkW + lane] : 0;
+      V x = lane < w ? __ldcg(b + j0 + pr) - accs[pr] : V(0);
+      for (int k = 0; k < w; ++k) {  // L11 (unit lower)
+        const V xk = __shfl_sync(kFull, x, k);
+        if (lane > k && lane < w) x -= Ls[k][lane] * xk;
+      }
+      const V y1 = x;
+      V v = x;
+      for (int k = w - 1; k >= 0; --k) {  // U11, 1 / U(k, k) from rdiag
+        V yk = lane == k ? v * V(rdiag[j0 + k]) : V(0);
+        yk = __shfl_sync(kFull, yk, k);
+        if (lane == k) v = yk;
+        if (lane < k) v -= Ls[k][lane] * yk;
+      }
+      if (lane < w) {
+        __stcg(b + j0 + lane, y1);
+        __stcg(zbuf + (size_t)p * kBlkW + lane, v);
+      }
+      __threadfence();
+      __syncwarp();
+      if (lane == 0) st_release(flags + p, epoch);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host side
 constexpr int kApplyNR = 9;     // 32-row chunks per warp per pass of the bulk update (two warps per column)
 constexpr int kColNR = 6;       // rows per thread per pass of the critical-path update
@@ -538,6 +610,18 @@ template <class V, class T>
 void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, cudaStream_t st) {
   blk_backward_kernel<T, V><<<1, 1024, 0, st>>>(ab, L, B.kuf, B.d_ps, B.npan(), rdiag, y);
 }
+// cooperative forward substitution; returns 0, or -1 if the launch was refused
+template <class V, class T>
+int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
+                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st) {
+  const int npan = B.npan();
+  const int* ps = B.d_ps;
+  void* args[] = {(void*)&ab,    (void*)&L,    (void*)&ps,    (void*)&npan,  (void*)&perm_all, (void*)&rdiag,
+                  (void*)&b,     (void*)&zbuf, (void*)&flags, (void*)&epoch, (void*)&err};
+  const cudaError_t e = cudaLaunchCooperativeKernel((const void*)blk_forward_coop_kernel<T, V>,
+                                                    dim3(std::min(grid, npan)), dim3(256), args, 0, st);
+  return e == cudaSuccess ? 0 : -1;
+}
 // CTAs of the cooperative back substitution that can be resident at once
 template <class V, class T>
 int blk_backward_grid() {
@@ -568,5 +652,9 @@ template void blk_backward_1cta<double, float>(const float*, const BandLayout&, 
                                                cudaStream_t);
 template int blk_backward_grid<double, double>();
 template int blk_backward_grid<double, float>();
+template int blk_forward_coop<double, double>(const double*, const BandLayout&, const BlkPlan&, const int*,
+                                              const double*, double*, double*, int*, int, int*, int, cudaStream_t);
+template int blk_forward_coop<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*, const float*,
+                                             double*, double*, int*, int, int*, int, cudaStream_t);
 
 }  // namespace mafem

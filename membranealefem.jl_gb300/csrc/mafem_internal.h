@@ -171,6 +171,12 @@ int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rd
                  int* err, int grid, cudaStream_t st);
 template <class V, class T>
 int blk_backward_grid();
+// Forward substitution (P, L11, A21 of the stored panels) on `grid` CTAs of one
+// cooperative launch, in place on b; zbuf: npan x 32 scratch; flags/epoch as
+// for blk_backward.  Returns 0, or -1 if the cooperative launch was refused.
+template <class V, class T>
+int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
+                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st);
 // Persistent cooperative factorisation (band_lu_persist.cu): launch shape and
 // per-panel flags.  Flags are zeroed once; epochs make them reusable.
 struct BlkPersist {
