@@ -95,7 +95,7 @@ struct mafem_handle {
   cudaEvent_t ev[6] = {};
   bool factored = false;
   int max_refine = 30;
-  double refine_tol = 1e-10;
+  double refine_tol = 1e-6;  // refinement stops when the last correction is <= refine_tol |x|
   int64_t launches = 0;  // kernels enqueued by this handle
   // node-block pivoting (band_lu_blk.cu): the default; full partial pivoting
   // (band_lu.cu) is the fallback for a block without a usable pivot
@@ -825,7 +825,10 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
   CK(cudaStreamSynchronize(h->st));
   const double r0 = h->h_out[4];
   if (!(r0 > 0.0)) return MAFEM_OK;
-  double prev = r0;
+  // stop when the last correction is small against x (|d| <= tol |x|): a bound
+  // on the forward error of x whatever the conditioning (a residual test at a
+  // loose tolerance can accept a large error in x on an ill-conditioned tangent)
+  double prev = INFINITY;
   for (int k = 0; k < h->max_refine; ++k) {
     CK(cudaMemcpyAsync(h->d_dx, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     if (h->last_blk) {
@@ -836,24 +839,25 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
       band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
       h->launches += 2;
     }
-    launch_axpy(n, h->d_dx, h->d_x, h->st);
+    launch_axpy_norms(n, h->d_dx, h->d_x, h->d_part, h->d_out + 8, h->st);
     launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part,
                                 h->d_out + 3, h->st);
-    h->launches += 3;
+    h->launches += 4;
     CK(cudaMemcpyAsync(h->h_out + 3, h->d_out + 3, sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->h_out + 8, h->d_out + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     *sweeps = k + 1;
-    const double rn = h->h_out[3];
-    if (!std::isfinite(rn)) {
-      h->err = "non-finite refinement residual";
+    const double rn = h->h_out[3], dn = h->h_out[8], xn = h->h_out[9];
+    if (!std::isfinite(rn) || !std::isfinite(dn) || !std::isfinite(xn)) {
+      h->err = "non-finite refinement residual or correction";
       return MAFEM_NAN_DETECTED;
     }
-    if (rn <= h->refine_tol * r0) return MAFEM_OK;
-    if (rn > 0.5 * prev && k >= 3) {
-      h->err = "iterative refinement stalled at relative residual " + std::to_string(rn / r0);
+    if (dn <= h->refine_tol * xn || rn == 0.0) return MAFEM_OK;
+    if (dn > 0.5 * prev && k >= 3) {
+      h->err = "iterative refinement stalled at relative correction " + std::to_string(dn / xn);
       return MAFEM_REFINE_STALLED;
     }
-    prev = rn;
+    prev = dn;
   }
   h->err = "iterative refinement did not reach its tolerance";
   return MAFEM_REFINE_STALLED;

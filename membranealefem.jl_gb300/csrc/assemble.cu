@@ -187,6 +187,50 @@ __global__ void axpy_kernel(int64_t n, const double* __restrict__ dx, double* __
     x[i] += dx[i];
 }
 
+// x += dx with the partial sums of |dx|^2 and |x|^2 per block (part[2 b], part[2 b + 1])
+__global__ void axpy_norms_kernel(int64_t n, const double* __restrict__ dx, double* __restrict__ x,
+                                  double* __restrict__ part) {
+  double dd = 0.0, xx = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double d = dx[i];
+    const double v = x[i] + d;
+    x[i] = v;
+    dd = fma(d, d, dd);
+    xx = fma(v, v, xx);
+  }
+  __shared__ double s[2][8];
+  for (int o = 16; o > 0; o >>= 1) {
+    dd += __shfl_xor_sync(0xffffffffu, dd, o);
+    xx += __shfl_xor_sync(0xffffffffu, xx, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s[0][threadIdx.x >> 5] = dd;
+    s[1][threadIdx.x >> 5] = xx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      a += s[0][w];
+      b += s[1][w];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+// out[0] = |dx|, out[1] = |x| from the block partial sums, in a fixed order
+__global__ void sqrt_pair_kernel(const double* __restrict__ part, int nblk, double* __restrict__ out) {
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int k = 0; k < nblk; ++k) {
+      a += part[2 * k];
+      b += part[2 * k + 1];
+    }
+    out[0] = sqrt(a);
+    out[1] = sqrt(b);
+  }
+}
+
 // ---- launchers -------------------------------------------------------------------
 template <class T>
 void launch_band_gather(const DevPatch& P, int ndf, int nq, const BandLayout& L, const T* K_el, T* ab,
@@ -216,6 +260,11 @@ void launch_band_residual(const T* a0, const BandLayout& L, const double* x, con
   const int blocks = band_residual_blocks(L.n);
   band_residual_kernel<T><<<blocks, 256, 0, st>>>(a0, L, x, r, res, part);
   sqrt_sum_kernel<<<1, 32, 0, st>>>(part, blocks, out);
+}
+void launch_axpy_norms(int64_t n, const double* dx, double* x, double* part, double* out, cudaStream_t st) {
+  const int blocks = (int)min64(1024, (n + 255) / 256);  // part holds 2048 doubles
+  axpy_norms_kernel<<<blocks, 256, 0, st>>>(n, dx, x, part);
+  sqrt_pair_kernel<<<1, 32, 0, st>>>(part, blocks, out);
 }
 void launch_axpy(int64_t n, const double* dx, double* x, cudaStream_t st) {
   const int blocks = (int)min64(1024, (n + 255) / 256);

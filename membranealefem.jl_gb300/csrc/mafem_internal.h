@@ -119,6 +119,8 @@ template <class T>
 void launch_band_residual(const T* a0, const BandLayout& L, const double* x, const double* r, double* res,
                           double* part, double* out, cudaStream_t st);
 void launch_axpy(int64_t n, const double* dx, double* x, cudaStream_t st);
+// x += dx; out[0] = |dx|, out[1] = |x| (part: 2048 doubles of scratch)
+void launch_axpy_norms(int64_t n, const double* dx, double* x, double* part, double* out, cudaStream_t st);
 
 template <class T>
 size_t apply_smem_bytes(const BandLayout& L, int threads);
