@@ -302,11 +302,13 @@ int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, int64_t* ou
 /* Number of kernels this handle has enqueued since mafem_create. */
 int64_t mafem_launch_count(const mafem_handle* h);
 
-/* FP32 form: FP64 iterative refinement of each linear solve stops when its
- * last correction is at most tol |x| (default 1e-6) -- a bound on the forward
- * error of x that holds on ill-conditioned tangents too -- or fails after
- * max_sweeps sweeps (default 30) or when the corrections stop shrinking
- * (MAFEM_REFINE_STALLED).  A looser tol trades refinement sweeps for Newton
+/* FP32 form: FP64 iterative refinement of each linear solve stops at tol
+ * (default 1e-10) or fails after max_sweeps sweeps (default 30) or when it stops
+ * converging (MAFEM_REFINE_STALLED).  A handle stepped on its own stops when
+ * |r - A x| <= tol |r|; the batched solve of mafem_batch_step stops when its
+ * last correction is at most tol |x| (a bound on the forward error of x that
+ * holds on ill-conditioned tangents too) and hands a stalled solve to the
+ * handle's own solver.  A looser tol trades refinement sweeps for Newton
  * iterations: the Newton criterion (FiniteElement.jl:48) on the FP64 residual
  * still decides convergence, so the converged state does not depend on tol. */
 int mafem_set_refinement(mafem_handle* h, int32_t max_sweeps, double tol);

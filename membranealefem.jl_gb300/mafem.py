@@ -457,9 +457,9 @@ class Solver:
         """CTAs of the persistent factorisation (0: all SMs); returns the value in use."""
         return int(lib().mafem_set_launch_ctas(self.h, ctas))
 
-    def set_refinement(self, max_sweeps: int = 30, tol: float = 1e-6) -> None:
-        """FP32 form: refinement stops when its last correction is <= tol |x| (or fails
-        after max_sweeps sweeps)."""
+    def set_refinement(self, max_sweeps: int = 30, tol: float = 1e-10) -> None:
+        """FP32 form: refinement tolerance (|r - A x| <= tol |r| alone; last correction
+        <= tol |x| in the batched solve) and sweep cap."""
         _raise(lib().mafem_set_refinement(self.h, max_sweeps, tol), self.h)
 
     def trace_patch_solve(self, time: float, dt: float):
