@@ -142,14 +142,11 @@ struct mafem_handle {
 
 template <class X>
 static int dalloc(mafem_handle* h, X** p, size_t count) {
-  // stream-ordered allocation from the device's memory pool, which keeps freed
-  // blocks (pool_keep_memory): creating a handle after another was destroyed
-  // reuses its memory without a device-wide cudaMalloc
   void* v = nullptr;
   size_t bytes = std::max<size_t>(count, 1) * sizeof(X);
-  cudaError_t e = cudaMallocAsync(&v, bytes, h->st);
+  cudaError_t e = cudaMalloc(&v, bytes);
   if (e != cudaSuccess) {
-    h->err = std::string("cudaMallocAsync of ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e);
+    h->err = std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? MAFEM_ERR_OOM : MAFEM_ERR_CUDA;
   }
   h->allocs.push_back(v);
@@ -161,25 +158,8 @@ template <class X>
 static int dupload(mafem_handle* h, X** p, const std::vector<X>& v) {
   int rc = dalloc(h, p, v.size());
   if (rc) return rc;
-  // from pageable memory: returns once v has been staged, so v may go away
-  CK(cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(X), cudaMemcpyHostToDevice));
   return MAFEM_OK;
-}
-
-// The default memory pool of the device keeps what is freed into it instead of
-// returning it at the next synchronisation, so handles created and destroyed
-// in turn (a server admitting requests) reuse device memory cheaply.
-static void pool_keep_memory() {
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int dev = 0;
-    cudaMemPool_t pool;
-    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
-      uint64_t thr = UINT64_MAX;
-      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
-    }
-    cudaGetLastError();
-  });
 }
 
 // Gᵀ H⁻¹ G of the Dohrmann-Bochev projection (FiniteElement.jl:279-323) for one
@@ -379,7 +359,6 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
   h->npan = (n + nb - 1) / nb;
   h->rmax = nb + (int)kl;
 
-  pool_keep_memory();
   cudaError_t ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (ce != cudaSuccess) {
     set_global_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(ce));
@@ -451,7 +430,7 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
       h->use_blk = true;
       AL(h->d_flags, (size_t)h->blk.npan());
       AL(h->d_zbuf, (size_t)h->blk.npan() * kBlkW);
-      cudaMemsetAsync(h->d_flags, 0, (size_t)h->blk.npan() * sizeof(int), h->st);
+      cudaMemset(h->d_flags, 0, (size_t)h->blk.npan() * sizeof(int));
       h->bwd_grid = precision == MAFEM_PLAIN_FP64 ? blk_backward_grid<double, double>() : blk_backward_grid<double, float>();
       h->bwd_max = h->bwd_grid;
       cudaGetLastError();
@@ -463,9 +442,9 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
         AL(h->pers.d_pdone, np);
         AL(h->pers.d_critcnt, np);
         AL(h->pers.d_a21cnt, np);
-        cudaMemsetAsync(h->pers.d_pdone, 0, np * sizeof(int), h->st);
-        cudaMemsetAsync(h->pers.d_critcnt, 0, np * sizeof(int), h->st);
-        cudaMemsetAsync(h->pers.d_a21cnt, 0, np * sizeof(int), h->st);
+        cudaMemset(h->pers.d_pdone, 0, np * sizeof(int));
+        cudaMemset(h->pers.d_critcnt, 0, np * sizeof(int));
+        cudaMemset(h->pers.d_a21cnt, 0, np * sizeof(int));
       } else {
         h->pers.grid = 0;
       }
@@ -490,7 +469,7 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
   AL(h->d_ipiv, n);
   AL(h->d_perm, std::max((size_t)h->npan * h->rmax, (size_t)h->blk.npan() * kBlkW));
   AL(h->d_info, 4);  // [0] zero-pivot column (1-based), [1] nonzero: a bounded device wait ran out
-  cudaMemsetAsync(h->d_info, 0, 4 * sizeof(int), h->st);
+  cudaMemset(h->d_info, 0, 4 * sizeof(int));
   const size_t band_elems = (size_t)h->L.ldb * n;
   if (precision == MAFEM_PLAIN_FP64) {
     double *kel, *band, *rd;
@@ -564,13 +543,6 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     mafem_destroy(hp.release());
     return MAFEM_ERR_CUDA;
   }
-  // every allocation, upload and clear done: the buffers are usable from any stream
-  ce = cudaStreamSynchronize(h->st);
-  if (ce != cudaSuccess) {
-    set_global_error(std::string("handle set-up: ") + cudaGetErrorString(ce));
-    mafem_destroy(hp.release());
-    return MAFEM_ERR_CUDA;
-  }
   *out = hp.release();
   return MAFEM_OK;
 }
@@ -579,8 +551,7 @@ extern "C" int mafem_destroy(mafem_handle* h) {
   if (!h) return MAFEM_OK;
   if (h->st) cudaStreamSynchronize(h->st);
   h->writer.reset();  // finishes the pending state files
-  for (void* p : h->allocs) cudaFreeAsync(p, h->st);
-  if (h->st) cudaStreamSynchronize(h->st);
+  for (void* p : h->allocs) cudaFree(p);
   if (h->h_out) cudaFreeHost(h->h_out);
   if (h->st2) cudaStreamSynchronize(h->st2);
   for (auto& e : h->ev)
@@ -1924,7 +1895,6 @@ extern "C" int mafem_snapshot_reserve(mafem_handle* h, int32_t nslots) {
   }
   const int rc = dalloc(h, &h->d_snap, (size_t)nslots * h->numnp * (3 + h->ndf));
   if (rc) return rc;
-  CK(cudaStreamSynchronize(h->st));
   h->nsnap = nslots;
   return MAFEM_OK;
 }
