@@ -1440,7 +1440,9 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
     if (s->used + q->est > s->budget) break;
     mafem_handle* h = nullptr;
     int rc = mafem_create(q->r.mesh, q->r.params, q->r.args, q->r.precision, &h);
-    if (rc == MAFEM_ERR_OOM) break;  // try again when memory frees up
+    // Out of device memory: try again once an active request frees its memory;
+    // with none active, nothing of this server's will free up, so fail it.
+    if (rc == MAFEM_ERR_OOM && !s->active.empty()) break;
     s->pending.pop_front();
     if (rc == MAFEM_OK) rc = mafem_upload_state(h, q->xms.data(), q->cps.data());
     if (rc == MAFEM_OK && q->r.refine_tol > 0.0) rc = mafem_set_refinement(h, 30, q->r.refine_tol);

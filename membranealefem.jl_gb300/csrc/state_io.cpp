@@ -146,11 +146,25 @@ int readdlm(const char* path, double* a, int64_t rows, int64_t cols, std::string
         err = std::string(path) + ": more than " + std::to_string(rows) + " rows";
         return MAFEM_ERR_ARG;
       }
-      // strtod would read past the line's end only through whitespace, which
-      // the separator loop above has already skipped
-      char* stop = nullptr;
-      const double v = std::strtod(q, &stop);
-      if (stop == q || stop > end) {
+      // from_chars reads '.' as the decimal point whatever the process locale
+      // (a host that set a ',' locale must still read these files); it takes
+      // "Inf", "NaN" in any case, but no leading '+', which is skipped here
+      const char* b = (*q == '+' && q + 1 < end && *(q + 1) != '-') ? q + 1 : q;
+      double v = 0.0;
+      const auto res = std::from_chars(b, end, v);
+      const char* stop = res.ptr;
+      if (res.ec == std::errc::result_out_of_range) {
+        // beyond the double range: +-0 for a negative exponent, else +-Inf,
+        // as Julia's parse gives
+        const char* ex = b;
+        while (ex < stop && *ex != 'e' && *ex != 'E') ++ex;
+        const bool tiny = ex + 1 < stop && *(ex + 1) == '-';
+        v = std::copysign(tiny ? 0.0 : HUGE_VAL, *b == '-' ? -1.0 : 1.0);
+      } else if (res.ec != std::errc() || stop == b) {
+        err = std::string(path) + ": not a number in row " + std::to_string(i + 1);
+        return MAFEM_ERR_ARG;
+      }
+      if (stop < end && *stop != ' ' && *stop != '\t' && *stop != '\r') {
         err = std::string(path) + ": not a number in row " + std::to_string(i + 1);
         return MAFEM_ERR_ARG;
       }

@@ -84,12 +84,30 @@ def test_readdlm_accepts_readdlm_whitespace(tmp_path):
     assert np.array_equal(b, [[1.0, 2.5, -3.0], [4e-3, 5e6, 6.0]])
 
 
+def test_readdlm_special_values(tmp_path):
+    """What print(::Float64) writes for the special values, a leading '+', and
+    numbers beyond the double range (Julia's parse: +-Inf on overflow, +-0 on
+    underflow)."""
+    path = str(tmp_path / "sp.txt")
+    with open(path, "w") as f:
+        f.write("+1.5\tInf\t-Inf\nNaN\t1e400\t-1e-400\n-0.0\t5.0e-324\t1.7976931348623157e308\n")
+    b = M.readdlm(path, 3, 3)
+    assert b[0, 0] == 1.5 and b[0, 1] == np.inf and b[0, 2] == -np.inf
+    assert np.isnan(b[1, 0]) and b[1, 1] == np.inf
+    assert b[1, 2] == 0.0 and np.signbit(b[1, 2])
+    assert b[2, 0] == 0.0 and np.signbit(b[2, 0])
+    assert b[2, 1] == 5e-324 and b[2, 2] == np.finfo(np.float64).max
+
+
 @pytest.mark.parametrize("text,rows,cols", [
     ("1.0\t2.0\n3.0\t4.0\n", 3, 2),   # too few rows
     ("1.0\t2.0\n3.0\t4.0\n", 1, 2),   # too many rows
     ("1.0\t2.0\n3.0\n", 2, 2),        # ragged row
     ("1.0\t2.0\t9\n3.0\t4.0\n", 2, 2),  # too many entries
     ("1.0\tx\n3.0\t4.0\n", 2, 2),     # not a number
+    ("1.0\t2.0abc\n3.0\t4.0\n", 2, 2),  # trailing garbage
+    ("1.0,2.0\n3.0\t4.0\n", 2, 2),    # not readdlm's separator
+    ("+-1.0\t2.0\n3.0\t4.0\n", 2, 2),  # two signs
 ])
 def test_readdlm_rejects_wrong_shape(tmp_path, text, rows, cols):
     path = str(tmp_path / "bad.txt")
