@@ -52,7 +52,8 @@ def dist_init():
     if ws <= 1:
         return 0, 1, 0, None
     import torch.distributed as dist
-    dist.init_process_group("gloo")
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
     return dist.get_rank(), ws, int(os.environ.get("LOCAL_RANK", "0")), dist
 
 

@@ -1,0 +1,78 @@
+"""bench.py's N > 1 path on the CPU: two ranks over gloo, as torchrun launches
+them (RANK / WORLD_SIZE / MASTER_* in the environment, 127.0.0.1).
+
+The path shards into independent replicas (each rank its own patch, no
+data-path collective): what the ranks share is the barrier around the timed
+region and the max over ranks of the timed totals, and only rank 0 prints.
+The reference arm runs on rank 0 alone; the other ranks exit without output.
+The reference arm's CPU sample is replaced by a stub here (its own timing is
+covered by the bench itself), so the test checks the plumbing, not the oracle.
+"""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+CHILD = r"""
+import contextlib, io, json, os, sys
+sys.path.insert(0, sys.argv[1])
+import bench
+rank, world, local, dist = bench.dist_init()
+assert dist is not None and world == 2 and rank == int(os.environ["RANK"])
+bench.barrier(dist)
+m = bench.allmax(dist, 10.0 * (rank + 1))
+bench.cpu_baseline = lambda **kw: {"value": 0.5, "unit": "time-steps/s", "cores": 1, "kind": "port",
+                                   "sample": "stub"}
+sys.argv = ["bench.py", "--impl", "reference", "--gpus", "2", "--steps", "2", "--warmup", "3"]
+buf = io.StringIO()
+with contextlib.redirect_stdout(buf):
+    bench.main()
+bench.barrier(dist)
+print(json.dumps({"rank": rank, "max": m, "out": buf.getvalue()}))
+"""
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_two_gloo_ranks_share_barrier_and_max_and_rank0_prints():
+    pytest.importorskip("torch.distributed")
+    port = _free_port()
+    procs = []
+    for rank in range(2):
+        env = dict(os.environ, RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE="2", LOCAL_WORLD_SIZE="2",
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, "-c", CHILD, ROOT], env=env, stdout=subprocess.PIPE,
+                                      stderr=subprocess.PIPE, text=True))
+    outs = []
+    try:
+        for p in procs:
+            out, err = p.communicate(timeout=240)
+            assert p.returncode == 0, err[-2000:]
+            outs.append(json.loads(out.strip().splitlines()[-1]))
+    finally:
+        for p in procs:
+            if p.poll() is None:
+                p.kill()
+    by_rank = {o["rank"]: o for o in outs}
+    assert sorted(by_rank) == [0, 1]
+    assert by_rank[0]["max"] == by_rank[1]["max"] == 20.0
+    assert by_rank[1]["out"] == ""
+    lines = [ln for ln in by_rank[0]["out"].splitlines() if ln.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] == 0.5
+    assert line["cpu_baseline"]["sample"] == "stub"
+    assert line["e2e"] == {"value": 0.5, "unit": "time-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    for key in ("metric", "unit", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling", "vs_baseline",
+                "dtype", "data", "config"):
+        assert key in line
+    assert line["config"]["parallelism"] == "replicas x2"
