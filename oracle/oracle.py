@@ -456,6 +456,32 @@ class Mesh:
         return eps[: it.value]
 
 
+def bend_errors(mesh: Mesh, xms, cps) -> tuple[float, float, float]:
+    """The error norms of ``analyze_output`` (src/Output.jl:128-177) for the
+    bending scenario at L = kb = 1, whose state should approach the arc of
+    radius 1 about (sin 1, ·, cos 1) with λ = 1/4 and H = 1/2.  Summed over the
+    elements and Gauss points in the reference's order, w the parametric Gauss
+    weight (get_gpw): Er = Σ w (√((x - sin 1)² + (z - cos 1)²) - 1)² (left
+    without the square root, as there), Eλ = √Σ w (λ - 1/4)²,
+    EH = √Σ w (H - 1/2)²."""
+    import math
+    ids, uf = mesh.area_tables()
+    er = el = eh = 0.0
+    for e2 in range(mesh.num2el):
+        for e1 in range(mesh.num1el):
+            e = e1 + mesh.num1el * e2
+            for g2 in range(3):
+                for g1 in range(3):
+                    g = g1 + 3 * g2
+                    w = uf[ids[e] - 1, g, 0]
+                    d = mesh.gds(xms, cps, e + 1, g + 1)
+                    x = d["x"]
+                    er += w * (math.sqrt((x[0] - math.sin(1.0)) ** 2 + (x[2] - math.cos(1.0)) ** 2) - 1.0) ** 2
+                    el += w * (d["lam"] - 0.25) ** 2
+                    eh += w * (d["H"] - 0.5) ** 2
+    return er, math.sqrt(el), math.sqrt(eh)
+
+
 def band_to_dense(ab: np.ndarray, kl: int, ku: int, n: int) -> np.ndarray:
     """Band storage (row q = column q of the matrix, offset kl+ku+i-j) -> dense."""
     A = np.zeros((n, n))

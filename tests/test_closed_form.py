@@ -25,13 +25,20 @@ One time step of the static mesh reaches the steady state (no inertia).
 Bending (F_BEND, Lagrangian).  The patch [0, L]² gets the moment kb / (2L) on
 its left and right edges, ramped up over bend_tm (src/input/Bc.jl:319-393,
 Params.jl:97-100).  It settles into a cylinder of half-angle 1/2:
-H = 1 / (2L), K = 0, and λ = kb / (4L²), the analytical tension with which
-src/Input.jl:68-69 initialises λ.  The top and bottom edges are moment-free,
-which a cylinder satisfies only with kg = -kb / 2 (the reference's defaults
-kb = 1, kg = -0.5).  The B-spline surface approximates the circle: on 8 x 2
-elements the mean of H is within 1e-3 of 1/(2L) and every point within 1e-2
-(under refinement the error of the mean falls as h², the pointwise one as h);
-K vanishes to rounding.
+H = 1 / (2L), K = 0, and λ = kb / (4L²), the analytical values with which
+src/Input.jl:68-69 initialises λ and src/Output.jl:141 measures the error.
+Both ends stay at z = 0 (v = 0 on the left edge, vz = 0 on the right,
+src/input/Bc.jl:369-386), so the section is the arc of radius L about
+(L sin 1/2, L cos 1/2) in the x-z plane.  (analyze_output's position error Er,
+src/Output.jl:160, measures the distance from (sin 1, cos 1) instead, the
+centre of an arc whose left end stays horizontal; with these boundary
+conditions it does not tend to zero, so only its Eλ and EH are checked.)  The
+top and bottom edges are moment-free, which a cylinder satisfies only with
+kg = -kb / 2 (the reference's defaults kb = 1, kg = -0.5).  The B-spline
+surface approximates the circle: on 8 x 2 elements the mean of H is within
+1e-3 of 1/(2L), every point within 1e-2 and within 2e-3 L of the arc (under
+refinement the error of the mean falls as h², the pointwise one as h); K
+vanishes to rounding.
 """
 import numpy as np
 import pytest
@@ -90,7 +97,9 @@ def _bend_setup(n1, n2, L, kb, zv):
 
 
 def _check_bend(om, L, kb, xms, cps):
-    H, K, lam = _gauss_points(om, xms, cps, [("H", 0), ("K", 0), ("lam", 0)])
+    H, K, lam, X, Z = _gauss_points(om, xms, cps, [("H", 0), ("K", 0), ("lam", 0), ("x", 0), ("x", 2)])
+    r = np.hypot(X - L * np.sin(0.5), Z - L * np.cos(0.5))
+    assert np.abs(r / L - 1.0).max() < 2e-3
     assert abs(H.mean() * 2 * L - 1.0) < 1e-3
     assert np.abs(H * 2 * L - 1.0).max() < 1e-2
     assert np.abs(K).max() * L * L < 1e-12
@@ -118,7 +127,8 @@ def test_oracle_bends_into_the_cylinder(n1, n2, L, kb, zv):
 
 
 def test_oracle_bending_error_falls_under_refinement():
-    errs = []
+    """The mean of H, and analyze_output's Eλ and EH (src/Output.jl:128-177)."""
+    errs, norms = [], []
     for n1 in (4, 8, 16):
         _, _, om, xms, cps = _bend_setup(n1, 2, 1.0, 1.0, 1.0)
         t = 0.0
@@ -128,7 +138,11 @@ def test_oracle_bending_error_falls_under_refinement():
             om.time_step(xms, cps, t, BEND_DT, nthreads=2)
         (H,) = _gauss_points(om, xms, cps, [("H", 0)])
         errs.append(abs(H.mean() * 2 - 1.0))
+        norms.append(O.bend_errors(om, xms, cps)[1:])
     assert errs[0] > 3.5 * errs[1] > 12.0 * errs[2]  # the mean's error: about h^2 each halving
+    (el4, eh4), (el8, eh8), (el16, eh16) = norms
+    assert el8 < 2e-3 and eh8 < 2e-3
+    assert el4 > 2.0 * el8 > 4.0 * el16 and eh4 > 2.0 * eh8 > 4.0 * eh16
 
 
 @pytest.mark.gpu
