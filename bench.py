@@ -302,6 +302,23 @@ def batch_patches(M, wl=BATCH):
 FP32_REFINE_TOL = 1e-4  # batched FP32 form: refinement tolerance per linear solve
 
 
+def hbm_view(traffic, launch_ms):
+    """The dominant kernel against HBM: its measured DRAM bytes per launch over
+    its average launch time, as a fraction of the measured copy bandwidth
+    (MEASURED_PEAKS.json's hbm_gbs; 6800 GB/s, one earlier GB300 measurement,
+    when that file is absent)."""
+    if not traffic or not launch_ms:
+        return None
+    peak, source = 6800.0, "fallback"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, source = float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        pass
+    gbs = traffic / (launch_ms * 1e-3) / 1e9
+    return {"achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": source}
+
+
 def _relmax(a, b):
     return float(np.abs(a - b).max() / max(float(np.abs(b).max()), 1e-300))
 
@@ -694,7 +711,8 @@ def main():
                                     "the kernel is bound by the FP64 pipe and its critical path, not by HBM "
                                     "or tensor cores",
                      "flops_per_launch": flops, "launch_ms": fac_ms,
-                     "traffic": NCU_TRAFFIC.get("blk_factor_persist_kernel<double>")},
+                     "traffic": NCU_TRAFFIC.get("blk_factor_persist_kernel<double>"),
+                     "hbm_view": hbm_view(NCU_TRAFFIC.get("blk_factor_persist_kernel<double>"), fac_ms)},
         "phase_ms_per_iter": {"assemble": sum(res["asm_ms"]) / n_fact, "factor": fac_ms,
                               "back_substitution": sum(res["sol_ms"]) / n_fact},
         "clocks": res["clocks"],
