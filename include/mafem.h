@@ -288,6 +288,12 @@ int mafem_server_get_stats(const mafem_server* s, mafem_server_stats* out);
 
 /* ---- diagnostics --------------------------------------------------------------- */
 
+/* Assemble the resident state at (time, dt), factor once with the persistent
+ * node-block LU and copy its per-panel clock stamps (12 int64 per panel) to
+ * out[0 .. 12 npan).  cap >= 12 npan.  Returns npan, or MAFEM_ERR_UNSUPPORTED if
+ * the handle does not use that factorisation. */
+int mafem_trace_factor(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap);
+
 /* FP32 form: assemble the resident state and run the batched one-CTA solve on
  * this handle alone, its factorisation traced -- 6 globaltimer stamps (ns) per
  * panel in out[6p .. 6p+5] (start, diagonal block factored, panel staged and

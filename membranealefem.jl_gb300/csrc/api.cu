@@ -1687,10 +1687,10 @@ static void lu_flops(const mafem_handle* h, double* fpanel, double* fapply) {
   *fapply = fa;
 }
 
-// Diagnostic (not in the public header): assemble at (time, dt), factor once
-// with the persistent kernel and copy its per-panel clock stamps
-// (12 int64 per panel, see blk_lu_factor_persist) to out[0 .. 12 * npan).
-// Returns npan, or a negative status.
+// Diagnostic: assemble at (time, dt), factor once with the persistent kernel
+// and copy its per-panel clock stamps (12 int64 per panel, see
+// blk_lu_factor_persist) to out[0 .. 12 * npan).  Returns npan, or a negative
+// status.
 extern "C" int mafem_trace_factor(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap) {
   if (!h || !out || !h->use_blk || h->pers.grid <= 0) return MAFEM_ERR_UNSUPPORTED;
   const int npan = h->blk.npan();
