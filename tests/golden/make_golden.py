@@ -36,12 +36,19 @@ import oracle as O  # noqa: E402
 NPZ = os.path.join(HERE, "oracle_cases.npz")
 
 _COMMON = dict(length=1.0, pull_speed=0.5, bend_mf=0.5, bend_tm=2.0)
-# (motion, scenario, num1el, num2el, seed)
+# (motion, scenario, num1el, num2el, seed[, parameter overrides])
 ASSEMBLY = [
     (O.ALEVB, O.F_PULL, 4, 5, 1), (O.ALEV, O.F_PULL, 3, 3, 2), (O.LAG, O.F_PULL, 3, 4, 3),
     (O.EUL, O.F_PULL, 3, 3, 4), (O.LAG, O.F_PULL, 1, 1, 5), (O.STATIC, O.F_CAVI, 3, 3, 6),
     (O.STATIC, O.F_COUE, 4, 3, 7), (O.STATIC, O.F_POIS, 3, 4, 8), (O.LAG, O.F_BEND, 3, 4, 9),
     (O.ALEV, O.F_BEND, 4, 3, 10),
+    # non-default moduli, viscosity and size (a normal pressure is rejected for
+    # F_PULL and F_BEND, Bc.jl:266 and Params.jl:103, and has no z unknowns to
+    # act on in the flat flows)
+    (O.ALEVB, O.F_PULL, 5, 4, 14, dict(kb=1.7, kg=-0.3, zv=0.6)),
+    (O.LAG, O.F_PULL, 4, 4, 15, dict(kb=0.6, zv=1.8)),
+    (O.EUL, O.F_PULL, 4, 3, 16, dict(kg=-0.8, length=2.0)),
+    (O.ALEV, O.F_BEND, 3, 3, 17, dict(kb=1.4, kg=-0.7, bend_mf=0.7, zv=0.5)),
 ]
 ASSEMBLY_TIME, ASSEMBLY_DT = 0.37, 0.01
 # (motion, num1el, num2el, steps, seed): tether pull at pull speed 1.0
@@ -102,8 +109,8 @@ def band_matvec(ab: np.ndarray, kl: int, v: np.ndarray, transpose: bool = False)
 def generate() -> dict:
     out, meta = {}, {"assembly": [], "steps": [], "assembly_time": ASSEMBLY_TIME,
                      "assembly_dt": ASSEMBLY_DT, "step_dt": STEP_DT}
-    for k, (motion, scen, n1, n2, seed) in enumerate(ASSEMBLY):
-        kw = case_params(motion, scen, n1, n2)
+    for k, (motion, scen, n1, n2, seed, *over) in enumerate(ASSEMBLY):
+        kw = case_params(motion, scen, n1, n2, **(over[0] if over else {}))
         mesh = O.Mesh(O.Params(**kw))
         xms, cps = initial_state(mesh, kw, seed, amp=2e-2, vel_amp=0.05)
         r, ab = mesh.calc_r_K(xms, cps, ASSEMBLY_TIME, ASSEMBLY_DT, nthreads=1)

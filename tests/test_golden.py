@@ -31,6 +31,12 @@ ARRAYS, META = G.load()
 N_ASM, N_STEP = len(META["assembly"]), len(META["steps"])
 
 
+def _product_params(kw):
+    """The fixture's Params keywords (the oracle's spelling) for the product's Params."""
+    names = {"zv": "zeta_v", "adb": "alpha_db", "am": "alpha_m"}
+    return M.Params(**{names.get(k, k): v for k, v in kw.items()})
+
+
 def _assembly_inputs(k):
     c = META["assembly"][k]
     return c, ARRAYS[f"a{k}_xms"], ARRAYS[f"a{k}_cps"], ARRAYS[f"a{k}_v"]
@@ -79,7 +85,7 @@ def test_oracle_reproduces_step_fixture(k):
 @pytest.mark.parametrize("k", range(N_ASM))
 def test_product_mesh_has_the_fixture_sizes(k):
     c = META["assembly"][k]
-    mesh = M.Mesh(M.Params(**c["params"]))
+    mesh = M.Mesh(_product_params(c["params"]))
     assert (mesh.nmdf, mesh.half_bw, mesh.numnp, mesh.ndf) == (c["nmdf"], c["half_bw"], c["numnp"], c["ndf"])
 
 
@@ -104,7 +110,7 @@ def test_state_files_byte_exact(tmp_path):
 @pytest.mark.parametrize("k", range(N_ASM))
 def test_gpu_assembly_matches_fixture(k, precision, tol):
     c, xms, cps, v = _assembly_inputs(k)
-    p = M.Params(**c["params"])
+    p = _product_params(c["params"])
     mesh = M.Mesh(p)
     with M.Solver(mesh, p, precision) as s:
         r, ab = s.calc_r_K(xms, cps, META["assembly_time"], META["assembly_dt"])
@@ -124,7 +130,7 @@ def test_gpu_assembly_matches_fixture(k, precision, tol):
 @pytest.mark.parametrize("k", range(N_STEP))
 def test_gpu_steps_match_fixture(k, precision, tol):
     c = META["steps"][k]
-    p = M.Params(**c["params"])
+    p = _product_params(c["params"])
     mesh = M.Mesh(p)
     dt, t = META["step_dt"], 0.0
     with M.Solver(mesh, p, precision) as s:
