@@ -309,6 +309,9 @@ int build_mesh(const mafem_params& p, const mafem_args& args, HostMesh& M, std::
       break;
     case MAFEM_F_BEND:  // Bc.jl:347-393
       if (p.motion == MAFEM_STATIC || p.motion == MAFEM_ALEVB) { err = "F_BEND needs LAG, EUL or ALEV motion (Params.jl:101-102)"; return MAFEM_ERR_ARG; }
+      // Params.jl:100 and 103, the same exact comparison: (kb / 2) / length
+      if (args.bend_mf != p.kb / 2 / p.length) { err = "F_BEND needs bend_mf == kb / 2 / length: the half-angle is 1/2 (Params.jl:100)"; return MAFEM_ERR_ARG; }
+      if (p.pn != 0.0) { err = "F_BEND with a normal pressure is not implemented (Params.jl:103)"; return MAFEM_ERR_ARG; }
       for (int b : {0, 2}) for (auto nd : bn[b]) { fix(VY, nd); if (ale) fix(VMY, nd); }
       for (auto nd : bn[3]) { fix(VX, nd); fix(VY, nd); fix(VZ, nd); if (ale) { fix(VMX, nd); fix(VMY, nd); fix(VMZ, nd); } }
       for (auto nd : bn[1]) { fix(VZ, nd); if (ale) fix(VMZ, nd); }

@@ -1502,6 +1502,15 @@ int orc_mesh_create(const orc_params* q, void** out) {
     ORC_ASSERT(p.nen == NEN && p.poly == POLY && p.nders == NDERS, "compile-time constants mismatch");
     Args a;
     a.pull_speed = q->pull_speed; a.bend_tm = q->bend_tm; a.bend_mf = q->bend_mf;
+    // check_params' scenario conditions (Params.jl:97-119)
+    if (p.scenario == F_BEND) {
+      ORC_ASSERT(a.bend_mf == p.kb / 2 / p.length, "α = 1/2 is the half-angle");
+      ORC_ASSERT(p.motion != STATIC, "mesh cannot be static for F_BEND scenario");
+      ORC_ASSERT(p.motion != ALEVB, "F_BEND not implemented for ALEVB motion");
+      ORC_ASSERT(p.pn == 0.0, "F_BEND with normal pressure not implemented");
+    } else if (p.scenario == F_CAVI || p.scenario == F_COUE || p.scenario == F_POIS) {
+      ORC_ASSERT(p.motion == STATIC, "need static motion for the flat flow scenarios");
+    }
     *out = generate_mesh(p, a).release();
   })
 }

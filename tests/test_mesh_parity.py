@@ -63,3 +63,17 @@ def test_errors_like_the_reference():
         M.Mesh(M.Params(scenario=M.F_PULL, pn=1.0))
     with pytest.raises(M.MafemError):  # Params.jl:108-115
         M.Mesh(M.Params(scenario=M.F_CAVI, motion=M.LAG))
+    # F_BEND's conditions (Params.jl:100-103), on the library and on the oracle
+    bad = [dict(bend_mf=0.4), dict(bend_mf=0.5, motion=M.ALEVB), dict(bend_mf=0.5, motion=M.STATIC),
+           dict(bend_mf=0.5, pn=0.1)]
+    for over in bad:
+        kw = dict(dict(motion=M.LAG), **over)
+        p, q = params_pair(kw.pop("motion"), M.F_BEND, 3, 3, **kw)
+        with pytest.raises(M.MafemError):
+            M.Mesh(p)
+        with pytest.raises(O.AssertionFailed):
+            O.Mesh(q)
+    p, q = params_pair(M.LAG, M.F_BEND, 3, 3, kb=1.4, length=2.0, bend_mf=1.4 / 2 / 2.0)
+    assert M.Mesh(p).numnp == O.Mesh(q).numnp == 25
+    with pytest.raises(O.AssertionFailed):  # Params.jl:108-115
+        O.Mesh(O.Params(scenario=O.F_POIS, motion=O.LAG, num1el=3, num2el=3))
