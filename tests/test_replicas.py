@@ -76,3 +76,14 @@ def test_two_gloo_ranks_share_barrier_and_max_and_rank0_prints():
                 "dtype", "data", "config"):
         assert key in line
     assert line["config"]["parallelism"] == "replicas x2"
+
+
+def test_cpu_baseline_times_the_oracle_on_a_small_patch():
+    """The reference arm's measurement itself (the oracle's assembly + sparse
+    LU on the host cores), on a 6 x 6 version of the workload."""
+    import bench
+    wl = dict(bench.WORKLOAD, n=6)
+    cb = bench.cpu_baseline(wl=wl, max_seconds=10.0, max_steps=2)
+    assert cb["kind"] == "port" and cb["unit"] == "time-steps/s"
+    assert cb["value"] > 0 and cb["cores"] >= 1
+    assert cb["sample"].startswith("first 2 time steps")
