@@ -558,18 +558,27 @@ class Batch:
         _raise(lib().mafem_batch_create(arr, len(self.solvers), ctas, C.byref(self.b)))
 
     def set_patch_solve(self, on: bool) -> bool:
-        """Batched one-CTA-per-patch FP32 solve for the FP32 patches (default on)."""
-        return bool(lib().mafem_batch_set_patch_solve(self.b, int(on)))
+        """Batched one-CTA-per-patch FP32 solve for the FP32 patches (default on);
+        returns whether it is in use."""
+        rc = lib().mafem_batch_set_patch_solve(self.b, int(on))
+        if rc < 0:
+            _raise(rc)
+        return rc == 1
 
     def step(self, times, dts):
-        """One time step of every patch; returns (statuses, list of step-stat dicts)."""
+        """One time step of every patch; returns (statuses, list of step-stat dicts).
+        Each patch's outcome, failures included, is its status; an error of the
+        call itself (a code no patch reports) raises."""
         n = len(self.solvers)
         times = np.ascontiguousarray(np.broadcast_to(times, (n,)), dtype=np.float64)
         dts = np.ascontiguousarray(np.broadcast_to(dts, (n,)), dtype=np.float64)
         status = (C.c_int32 * n)()
         stats = (StepStats * n)()
-        lib().mafem_batch_step(self.b, _dp(times), _dp(dts), status, stats)
-        return [int(x) for x in status], [st.as_dict() for st in stats]
+        rc = lib().mafem_batch_step(self.b, _dp(times), _dp(dts), status, stats)
+        statuses = [int(x) for x in status]
+        if rc != OK and rc not in statuses:
+            _raise(rc)
+        return statuses, [st.as_dict() for st in stats]
 
     def close(self):
         if self.b:
