@@ -9,7 +9,6 @@ patches must still equal their runs alone.  Every patch matches the oracle
 (1e-9 plain FP64, 1e-8 FP32).  A patch whose Newton iteration fails reports its
 status without disturbing the others.
 """
-import numpy as np
 import pytest
 
 from _cases import M, O, params_pair, rel, state
