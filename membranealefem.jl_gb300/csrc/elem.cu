@@ -677,7 +677,7 @@ cudaError_t launch_elem<double>(const DevPatch& Pt, const PhysParams& pp, double
 template <>
 cudaError_t launch_elem<float>(const DevPatch& Pt, const PhysParams& pp, double time, double dt, double* r_el,
                                float* K_el, cudaStream_t st, const int* elist, int nlist, int area_only) {
-  if (elist || area_only) return cudaErrorInvalidValue;
+  if (elist || nlist || area_only) return cudaErrorInvalidValue;
   cudaError_t e;
   switch (pp.motion) {
     case MAFEM_STATIC:
