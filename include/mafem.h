@@ -119,7 +119,11 @@ typedef struct mafem_step_stats {
 
 /* ---- host mesh (restates Mesh(p; args...) and prepare_input) ----------------- */
 
-/* Mesh(p; args...) -- src/input/Mesh.jl:79,94-302, src/input/Bc.jl. */
+/* Mesh(p; args...) -- src/input/Mesh.jl:79,94-302, src/input/Bc.jl.  Rejects
+ * (MAFEM_ERR_ARG / MAFEM_ERR_UNSUPPORTED) what check_params does
+ * (src/input/Params.jl:89-119): other element orders, F_BEND with a static or
+ * ALEVB mesh, bend_mf != kb / 2 / length or a normal pressure, the flat flows
+ * with a moving mesh, F_PULL with a normal pressure (Bc.jl:266). */
 int mafem_mesh_build(const mafem_params* p, const mafem_args* a, mafem_mesh** out);
 /* Fill `out` with pointers into `m` (valid until mafem_mesh_free). */
 int mafem_mesh_view(const mafem_mesh* m, mafem_mesh_desc* out);
