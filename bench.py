@@ -617,9 +617,11 @@ def run_case(case):
         raise SystemExit(1)
 
 
-def cpu_baseline(wl=WORKLOAD, max_seconds=20.0, max_steps=3):
+def cpu_baseline(wl=WORKLOAD, max_seconds=20.0, max_steps=3, state_out=None):
     """The oracle's threaded complex-step assembly + scipy SuperLU (the stand-in for
-    the reference's Julia calc_r_K + UMFPACK) on a bounded sample of the workload."""
+    the reference's Julia calc_r_K + UMFPACK) on a bounded sample of the workload.
+    If state_out is a dict it receives the oracle's state after the sample
+    (xms, cps, steps) for the accuracy report."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     q = O.Params(motion=wl["motion"], scenario=O.F_PULL, num1el=wl["n"], num2el=wl["n"], length=wl["length"],
@@ -637,9 +639,32 @@ def cpu_baseline(wl=WORKLOAD, max_seconds=20.0, max_steps=3):
         iters += len(O.time_step_sparse(om, xms, cps, t, dt, nthreads=cores))
         steps += 1
     el = time.perf_counter() - t0
+    if state_out is not None:
+        state_out.update(xms=xms, cps=cps, steps=steps)
     return {"value": steps / el, "unit": "time-steps/s", "cores": cores, "kind": "port",
             "sample": f"first {steps} time steps ({iters} Newton iterations) of the workload: oracle complex-step "
                       f"assembly on {cores} threads + scipy SuperLU, {el:.1f} s"}
+
+
+def rel_err_vs_oracle(M, ref, wl=WORKLOAD):
+    """The plain FP64 path's state after the oracle sample's time steps, from the
+    same initial state, against the oracle's: relative errors of xms, of the
+    velocity unknowns and of λ (the parity bar of the plain FP64 form is 1e-9)."""
+    p = make_params(M, wl)
+    mesh = M.Mesh(p)
+    xms, cps = initial_state(M, p, mesh, wl)
+    t = 0.0
+    with M.Solver(mesh, p, M.PLAIN_FP64) as s:
+        s.upload(xms, cps)
+        for _ in range(ref["steps"]):
+            t += wl["dt"]
+            s.predict(wl["dt"])
+            s.time_step_resident(t, wl["dt"])
+        x, c = s.download()
+    lam = mesh.dofs[6] - 1
+    vel = [d for d in range(mesh.ndf) if d != lam]
+    return {"steps": ref["steps"], "xms": _relmax(x, ref["xms"]), "velocities": _relmax(c[:, vel], ref["cps"][:, vel]),
+            "lambda": _relmax(c[:, lam], ref["cps"][:, lam]), "bar": 1e-9}
 
 
 def main():
@@ -728,7 +753,13 @@ def main():
     if rank == 0 and not args.no_serve:
         line["serving"] = run_serving()
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline()
+        ref = {}
+        line["cpu_baseline"] = cpu_baseline(state_out=ref)
+        try:
+            import mafem as M
+            line["rel_err_vs_oracle"] = rel_err_vs_oracle(M, ref)
+        except Exception as e:  # the accuracy report must not cost the bench line
+            line["rel_err_vs_oracle"] = {"error": repr(e)[:300]}
     if rank == 0:
         print(json.dumps(line))
 

@@ -87,3 +87,52 @@ def test_cpu_baseline_times_the_oracle_on_a_small_patch():
     assert cb["kind"] == "port" and cb["unit"] == "time-steps/s"
     assert cb["value"] > 0 and cb["cores"] >= 1
     assert cb["sample"].startswith("first 2 time steps")
+
+
+def test_rel_err_vs_oracle_report():
+    """The bench's accuracy report against the oracle sample: same initial state,
+    same steps.  The device solver is replaced by the oracle's own band-LU
+    stepping, so the report compares two CPU solvers and must sit far below
+    the 1e-9 bar."""
+    import dataclasses
+    import types
+
+    import bench
+    from _cases import M, O
+
+    wl = dict(bench.WORKLOAD, n=6)
+    ref = {}
+    bench.cpu_baseline(wl=wl, max_seconds=10.0, max_steps=2, state_out=ref)
+    assert ref["steps"] == 2
+
+    fields = {f.name for f in dataclasses.fields(O.Params)}
+
+    class OracleSolver:
+        def __init__(self, mesh, p, precision):
+            d = dataclasses.asdict(p)
+            d["zv"] = d.pop("zeta_v")
+            self.om = O.Mesh(O.Params(**{k: v for k, v in d.items() if k in fields}))
+
+        def __enter__(self):
+            return self
+
+        def __exit__(self, *a):
+            pass
+
+        def upload(self, x, c):
+            self.x, self.c = x.copy(order="F"), c.copy(order="F")
+
+        def predict(self, dt):
+            self.om.update_xms(self.x, self.c, dt)
+
+        def time_step_resident(self, t, dt):
+            self.om.time_step(self.x, self.c, t, dt, nthreads=2)
+
+        def download(self):
+            return self.x, self.c
+
+    fake = types.SimpleNamespace(**{k: getattr(M, k) for k in dir(M) if not k.startswith("__")})
+    fake.Solver = OracleSolver
+    rep = bench.rel_err_vs_oracle(fake, ref, wl)
+    assert rep["steps"] == 2 and rep["bar"] == 1e-9
+    assert max(rep["xms"], rep["velocities"], rep["lambda"]) < 1e-11, rep
