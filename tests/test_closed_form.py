@@ -38,7 +38,11 @@ kg = -kb / 2 (the reference's defaults kb = 1, kg = -0.5).  The B-spline
 surface approximates the circle: on 8 x 2 elements the mean of H is within
 1e-3 of 1/(2L), every point within 1e-2 and within 2e-3 L of the arc (under
 refinement the error of the mean falls as h², the pointwise one as h); K
-vanishes to rounding.
+vanishes to rounding.  The Eulerian mesh (its nodes move only along the
+normal) settles into the same cylinder.  It has the same mean H and the mean
+of λ within 2e-3, and its pointwise errors are larger: H within 5e-2, the arc
+within 1e-2 L.  The ALE mesh is still relaxing long after the membrane has
+settled and is not checked here.
 """
 import numpy as np
 import pytest
@@ -50,8 +54,9 @@ FLOWS = [  # (scenario, num1el, num2el, length, zeta_v)
     (M.F_POIS, 6, 4, 1.0, 0.7), (M.F_POIS, 5, 5, 3.0, 2.0),
 ]
 FLOW_DT = 0.01
-BENDS = [  # (num1el, num2el, length, kb, zeta_v)
-    (8, 2, 1.0, 1.0, 1.0), (8, 2, 1.0, 2.0, 1.0), (8, 2, 2.0, 4.0, 1.0), (8, 3, 1.0, 0.5, 0.5),
+BENDS = [  # (motion, num1el, num2el, length, kb, zeta_v)
+    (M.LAG, 8, 2, 1.0, 1.0, 1.0), (M.LAG, 8, 2, 1.0, 2.0, 1.0), (M.LAG, 8, 2, 2.0, 4.0, 1.0),
+    (M.LAG, 8, 3, 1.0, 0.5, 0.5), (M.EUL, 8, 2, 1.0, 1.0, 1.0), (M.EUL, 8, 2, 2.0, 3.0, 1.5),
 ]
 BEND_DT, BEND_STEPS = 0.05, 40  # the moment reaches its final value at t = 1, the state settles by t = 1.5
 
@@ -86,8 +91,8 @@ def _flow_setup(scenario, n1, n2, L, zv):
     return p, q, O.Mesh(q)
 
 
-def _bend_setup(n1, n2, L, kb, zv):
-    p, q = params_pair(M.LAG, M.F_BEND, n1, n2, length=L, kb=kb, kg=-kb / 2, zeta_v=zv,
+def _bend_setup(motion, n1, n2, L, kb, zv):
+    p, q = params_pair(motion, M.F_BEND, n1, n2, length=L, kb=kb, kg=-kb / 2, zeta_v=zv,
                        bend_mf=kb / 2 / L, bend_tm=1.0)
     om = O.Mesh(q)
     mesh = M.Mesh(p)
@@ -96,14 +101,18 @@ def _bend_setup(n1, n2, L, kb, zv):
     return p, mesh, om, xms, cps
 
 
-def _check_bend(om, L, kb, xms, cps):
+def _check_bend(om, motion, L, kb, xms, cps):
     H, K, lam, X, Z = _gauss_points(om, xms, cps, [("H", 0), ("K", 0), ("lam", 0), ("x", 0), ("x", 2)])
     r = np.hypot(X - L * np.sin(0.5), Z - L * np.cos(0.5))
-    assert np.abs(r / L - 1.0).max() < 2e-3
+    lag = motion == M.LAG
+    assert np.abs(r / L - 1.0).max() < (2e-3 if lag else 1e-2)
     assert abs(H.mean() * 2 * L - 1.0) < 1e-3
-    assert np.abs(H * 2 * L - 1.0).max() < 1e-2
+    assert np.abs(H * 2 * L - 1.0).max() < (1e-2 if lag else 5e-2)
     assert np.abs(K).max() * L * L < 1e-12
-    assert np.abs(lam * 4 * L * L / kb - 1.0).max() < 2e-2
+    lam_n = lam * 4 * L * L / kb
+    assert abs(lam_n.mean() - 1.0) < 2e-3
+    if lag:
+        assert np.abs(lam_n - 1.0).max() < 2e-2
 
 
 @pytest.mark.parametrize("scenario,n1,n2,L,zv", FLOWS)
@@ -115,22 +124,22 @@ def test_oracle_reaches_the_closed_form_flow(scenario, n1, n2, L, zv):
     _check_flow(om, scenario, L, zv, xms, cps, 1e-12)
 
 
-@pytest.mark.parametrize("n1,n2,L,kb,zv", BENDS)
-def test_oracle_bends_into_the_cylinder(n1, n2, L, kb, zv):
-    _, _, om, xms, cps = _bend_setup(n1, n2, L, kb, zv)
+@pytest.mark.parametrize("motion,n1,n2,L,kb,zv", BENDS)
+def test_oracle_bends_into_the_cylinder(motion, n1, n2, L, kb, zv):
+    _, _, om, xms, cps = _bend_setup(motion, n1, n2, L, kb, zv)
     t = 0.0
     for _ in range(BEND_STEPS):
         t += BEND_DT
         om.update_xms(xms, cps, BEND_DT)
         om.time_step(xms, cps, t, BEND_DT, nthreads=2)
-    _check_bend(om, L, kb, xms, cps)
+    _check_bend(om, motion, L, kb, xms, cps)
 
 
 def test_oracle_bending_error_falls_under_refinement():
     """The mean of H, and analyze_output's Eλ and EH (src/Output.jl:128-177)."""
     errs, norms = [], []
     for n1 in (4, 8, 16):
-        _, _, om, xms, cps = _bend_setup(n1, 2, 1.0, 1.0, 1.0)
+        _, _, om, xms, cps = _bend_setup(M.LAG, n1, 2, 1.0, 1.0, 1.0)
         t = 0.0
         for _ in range(BEND_STEPS):
             t += BEND_DT
@@ -158,9 +167,9 @@ def test_gpu_reaches_the_closed_form_flow(scenario, n1, n2, L, zv, precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n1,n2,L,kb,zv", BENDS)
-def test_gpu_bends_into_the_cylinder(n1, n2, L, kb, zv):
-    p, mesh, om, xms, cps = _bend_setup(n1, n2, L, kb, zv)
+@pytest.mark.parametrize("motion,n1,n2,L,kb,zv", BENDS)
+def test_gpu_bends_into_the_cylinder(motion, n1, n2, L, kb, zv):
+    p, mesh, om, xms, cps = _bend_setup(motion, n1, n2, L, kb, zv)
     with M.Solver(mesh, p) as s:
         s.upload(xms, cps)
         t = 0.0
@@ -169,4 +178,4 @@ def test_gpu_bends_into_the_cylinder(n1, n2, L, kb, zv):
             s.predict(BEND_DT)
             s.time_step_resident(t, BEND_DT)
         xms, cps = s.download()
-    _check_bend(om, L, kb, xms, cps)
+    _check_bend(om, motion, L, kb, xms, cps)
