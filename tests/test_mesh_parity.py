@@ -11,7 +11,8 @@ from _cases import M, O, params_pair
 CASES = [(M.LAG, M.F_PULL, 8, 8), (M.ALEVB, M.F_PULL, 32, 32), (M.ALEVB, M.F_PULL, 19, 21),
          (M.ALEVB, M.F_PULL, 64, 64), (M.EUL, M.F_PULL, 5, 6), (M.ALEV, M.F_PULL, 4, 7),
          (M.LAG, M.F_PULL, 1, 1), (M.STATIC, M.F_CAVI, 2, 3), (M.STATIC, M.F_COUE, 3, 4),
-         (M.STATIC, M.F_POIS, 5, 4), (M.LAG, M.F_BEND, 3, 3), (M.ALEV, M.F_BEND, 2, 5)]
+         (M.STATIC, M.F_POIS, 5, 4), (M.LAG, M.F_BEND, 3, 3), (M.ALEV, M.F_BEND, 2, 5),
+         (M.EUL, M.F_BEND, 8, 2)]
 
 
 @pytest.mark.parametrize("motion,scenario,n1,n2", CASES)
