@@ -49,6 +49,7 @@ ASSEMBLY = [
     (O.LAG, O.F_PULL, 4, 4, 15, dict(kb=0.6, zv=1.8)),
     (O.EUL, O.F_PULL, 4, 3, 16, dict(kg=-0.8, length=2.0)),
     (O.ALEV, O.F_BEND, 3, 3, 17, dict(kb=1.4, kg=-0.7, bend_mf=0.7, zv=0.5)),
+    (O.EUL, O.F_BEND, 4, 3, 18),
 ]
 ASSEMBLY_TIME, ASSEMBLY_DT = 0.37, 0.01
 # (motion, num1el, num2el, steps, seed): tether pull at pull speed 1.0
