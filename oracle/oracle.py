@@ -457,7 +457,7 @@ class Mesh:
 
 
 def bend_errors(mesh: Mesh, xms, cps) -> tuple[float, float, float]:
-    """The error norms of ``analyze_output`` (src/Output.jl:128-177) for the
+    """The error norms of ``analyze_output`` (src/Output.jl:129-180) for the
     bending scenario at L = kb = 1, whose state should approach the arc of
     radius 1 about (sin 1, ·, cos 1) with λ = 1/4 and H = 1/2.  Summed over the
     elements and Gauss points in the reference's order, w the parametric Gauss

@@ -11,7 +11,7 @@ back and evaluated the same way).
 Flows.  The flat static scenarios' steady solutions lie in the biquadratic
 B-spline space, so the discrete solution must equal them to rounding.  Take
 the in-plane stress σ = λ 1 + ζ (∇v + ∇vᵀ) on the square [-L/2, L/2]²
-(src/input/Bc.jl:109-153 and 273-310 give the conditions):
+(src/input/Bc.jl:110-157 and 273-316 give the conditions):
 
 * Couette (F_COUE): vx = 0 on the bottom edge, 3 on the top, vy = 0 on every
   edge, normal traction 4 on the left and right edges:
@@ -26,11 +26,11 @@ Bending (F_BEND, Lagrangian).  The patch [0, L]² gets the moment kb / (2L) on
 its left and right edges, ramped up over bend_tm (src/input/Bc.jl:319-393,
 Params.jl:97-100).  It settles into a cylinder of half-angle 1/2:
 H = 1 / (2L), K = 0, and λ = kb / (4L²), the analytical values with which
-src/Input.jl:68-69 initialises λ and src/Output.jl:141 measures the error.
+src/Input.jl:68-69 initialises λ and src/Output.jl:142 measures the error.
 Both ends stay at z = 0 (v = 0 on the left edge, vz = 0 on the right,
 src/input/Bc.jl:369-386), so the section is the arc of radius L about
 (L sin 1/2, L cos 1/2) in the x-z plane.  (analyze_output's position error Er,
-src/Output.jl:160, measures the distance from (sin 1, cos 1) instead, the
+src/Output.jl:163, measures the distance from (sin 1, cos 1) instead, the
 centre of an arc whose left end stays horizontal; with these boundary
 conditions it does not tend to zero, so only its Eλ and EH are checked.)  The
 top and bottom edges are moment-free, which a cylinder satisfies only with
@@ -136,7 +136,7 @@ def test_oracle_bends_into_the_cylinder(motion, n1, n2, L, kb, zv):
 
 
 def test_oracle_bending_error_falls_under_refinement():
-    """The mean of H, and analyze_output's Eλ and EH (src/Output.jl:128-177)."""
+    """The mean of H, and analyze_output's Eλ and EH (src/Output.jl:129-180)."""
     errs, norms = [], []
     for n1 in (4, 8, 16):
         _, _, om, xms, cps = _bend_setup(M.LAG, n1, 2, 1.0, 1.0, 1.0)
