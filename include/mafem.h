@@ -168,7 +168,8 @@ int mafem_time_step(mafem_handle* h, double time, double dt, mafem_step_stats* s
 int mafem_time_step_host(mafem_handle* h, double* xms, double* cps, double time, double dt,
                          mafem_step_stats* stats);
 /* run_analysis!'s time loop (src/Analysis.jl:183-216) on the resident state:
- * predictor + time_step! for each Δt; times[k] = t0 + sum(dts[0..k]). */
+ * predictor + time_step! for each Δt; step k ends at t0 + dts[0] + ... + dts[k],
+ * summed left to right. */
 int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, mafem_step_stats* last);
 
 /* calc_pull_force (src/analysis/PullForce.jl:61-80) on the resident state:

@@ -1642,7 +1642,10 @@ extern "C" int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, dou
   if (!h || (!dts && nsteps > 0)) return MAFEM_ERR_ARG;
   double t = t0;
   for (int k = 0; k < nsteps; ++k) {
-    t += dts[k];  // times = cumsum(Δts) + t0 (Analysis.jl:154)
+    // the step's end time, accumulated left to right from t0; the reference
+    // forms [sum(Δts[1:i]) for i] .+ t0 (Analysis.jl:30), whose summation
+    // order Julia's sum chooses: the two agree to rounding
+    t += dts[k];
     launch_predictor(h->P, h->pp, dts[k], h->st);
     h->launches += 1;
     CK(cudaGetLastError());
