@@ -1,7 +1,7 @@
 """Benchmark: membrane time-steps/s of the GB300 assemble-and-solve path.
 
 Workload (one "step" = one time step of run_analysis!: the predictor
-update_xms! and the Newton loop of time_step!, src/Analysis.jl:193-196):
+update_xms! and the Newton loop of time_step!, src/Analysis.jl:70-73):
 ALE-viscous-bending (ALEVB) tether pull on a 32x32-element graded flat patch
 (34x34 control points, 8430 unknowns, half bandwidth 543), L = 1, kb = 1,
 kg = -1/2, ζv = 1, dt = 0.005, velocity-driven pull (pull_speed = 0.02, the
@@ -212,7 +212,7 @@ def run_gb300(args, rank, world, local, dist):
         t = 0.0
 
         def host_step(t):
-            for j, d in enumerate(mmo):  # update_xms! predictor on the host (Analysis.jl:193)
+            for j, d in enumerate(mmo):  # update_xms! predictor on the host (Analysis.jl:70)
                 xms[:, j] += dt * cps[:, d]
             return s.time_step(xms, cps, t, dt)
 

@@ -159,7 +159,7 @@ int mafem_calc_r_K(mafem_handle* h, double time, double dt, double* r_out, doubl
 /* Δu = -K \ r for the K of the last mafem_calc_r_K and a host r (nmdf). */
 int mafem_solve(mafem_handle* h, const double* r, double* du_out);
 /* update_xms! (FiniteElement.jl:408-423) on the resident state: the predictor
- * xms[:, j] += Δt * cps[:, m_motion_order[j]] (Analysis.jl:193). */
+ * xms[:, j] += Δt * cps[:, m_motion_order[j]] (Analysis.jl:70). */
 int mafem_predict(mafem_handle* h, double dt);
 /* time_step! (FiniteElement.jl:11-63) on the resident state. */
 int mafem_time_step(mafem_handle* h, double time, double dt, mafem_step_stats* stats);
@@ -167,7 +167,7 @@ int mafem_time_step(mafem_handle* h, double time, double dt, mafem_step_stats* s
  * the updated xms/cps into the same arrays -- the drop-in for the reference. */
 int mafem_time_step_host(mafem_handle* h, double* xms, double* cps, double time, double dt,
                          mafem_step_stats* stats);
-/* run_analysis!'s time loop (src/Analysis.jl:183-216) on the resident state:
+/* run_analysis!'s time loop (src/Analysis.jl:60-93) on the resident state:
  * predictor + time_step! for each Δt; step k ends at t0 + dts[0] + ... + dts[k],
  * summed left to right. */
 int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, mafem_step_stats* last);

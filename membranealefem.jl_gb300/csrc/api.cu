@@ -1192,7 +1192,7 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
   std::vector<int> active, st(n, MAFEM_OK);
   for (int i = 0; i < n; ++i) {
     mafem_handle* h = b->hs[i];
-    launch_predictor(h->P, h->pp, dts[i], h->st);  // update_xms! (Analysis.jl:193)
+    launch_predictor(h->P, h->pp, dts[i], h->st);  // update_xms! (Analysis.jl:70)
     h->launches += 1;
     step_begin(h, times[i], dts[i]);
     active.push_back(i);
@@ -1471,7 +1471,7 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
   const double t_now = now_s();
   for (ServerReq* q : s->active) {
     if (q->state != ServerReq::IDLE) continue;
-    if (!q->in_step) {  // predictor (Analysis.jl:193) + step_begin
+    if (!q->in_step) {  // predictor (Analysis.jl:70) + step_begin
       launch_predictor(q->h->P, q->h->pp, q->r.dt, q->h->st);
       q->h->launches += 1;
       step_begin(q->h, q->t + q->r.dt, q->r.dt);

@@ -72,7 +72,7 @@ __global__ void resid_gather_kernel(DevPatch P, int ndf, int nq, const double* _
   }
 }
 
-// update_xms! (FiniteElement.jl:408-423) used as the predictor (Analysis.jl:193):
+// update_xms! (FiniteElement.jl:408-423) used as the predictor (Analysis.jl:70):
 // xms[:, j] += dt * cps[:, m_motion_order[j]]
 __global__ void predictor_kernel(DevPatch P, PhysParams pp, double dt) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < 3LL * P.numnp;

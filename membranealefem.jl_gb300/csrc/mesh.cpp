@@ -158,7 +158,7 @@ Line line_tables(const std::vector<double>& U) {
     if (!same) {
       ++nu;
       double lo = U[s], hi = U[s + 1];
-      for (int g = 0; g < 3; ++g) {  // GaussPointsζ (GaussPoint.jl:480-484)
+      for (int g = 0; g < 3; ++g) {  // GaussPointsζ (GaussPoint.jl:72-77)
         double u = xi[g] * (hi - lo) / 2 + (hi + lo) / 2;
         double w = wx[g] * (hi - lo) / 2;
         double N[3], dN[3], ddN[3];

@@ -536,7 +536,7 @@ class Solver:
         return self.last_stats
 
     def run_analysis(self, dts, t0: float = 0.0):
-        """``run_analysis!``'s time loop on the resident state (Analysis.jl:183-216)."""
+        """``run_analysis!``'s time loop on the resident state (Analysis.jl:60-93)."""
         dts = np.ascontiguousarray(dts, dtype=np.float64)
         st = StepStats()
         rc = lib().mafem_run(self.h, _dp(dts), len(dts), t0, C.byref(st))

@@ -40,7 +40,7 @@ namespace orc {
 
 using cd = std::complex<double>;
 
-// ---- enums (src/input/Enums.jl:203-335, src/input/Dof.jl:29-34) -------------
+// ---- enums (src/input/Enums.jl:24-157, src/input/Dof.jl:29-34) -------------
 enum Scenario { F_CAVI = 1, F_COUE = 2, F_POIS = 3, F_PULL = 4, F_BEND = 5 };
 enum Topology { FLAT = 1, CYLINDER = 2 };
 enum Motion { STATIC = 1, EUL = 2, LAG = 3, ALEV = 4, ALEVB = 5 };
@@ -460,7 +460,7 @@ std::vector<double> get_xi_weights(int ngp) {
   ORC_ASSERT(false, "weights for this number of Gauss points not implemented");
   return {};
 }
-// GaussPoint.jl:480-484: ζ = ξ (hi-lo)/2 + (hi+lo)/2,  w = ŵ (hi-lo)/2
+// GaussPoint.jl:72-77: ζ = ξ (hi-lo)/2 + (hi+lo)/2,  w = ŵ (hi-lo)/2
 void gauss_zeta(int ngp, double lo, double hi, std::vector<double>& zs, std::vector<double>& ws) {
   auto xs = get_xis(ngp);
   auto wx = get_xi_weights(ngp);
