@@ -15,8 +15,12 @@ The FP32 substitutions use the same stored quantities.  The refinement
 repeats x += LU^-1 (b - A0 x), with the residual taken in FP64 against the
 FP32 tangent A0.  It stops when the last correction is at most tol |x|.
 
+`double_float_residual` restates how the batched refinement forms that
+residual on the FP32 pipe (double-float arithmetic).
+
 The model answers numerical questions about that scheme on the oracle's
-tangents (growth, refinement contraction, sweeps per solve) without a GPU.
+tangents (growth, refinement contraction, sweeps per solve, residual
+accuracy) without a GPU.
 Dense float32 storage: meant for patches up to 32 x 32 elements.
 """
 from __future__ import annotations
@@ -153,3 +157,39 @@ def refine(lu: PatchLU, ab0: np.ndarray, kl: int, b: np.ndarray, tol: float = 1e
             break
         res = b - band_matvec(ab0, kl, x)
     return x, hist
+
+
+def _fma32(a, b, c):
+    """fmaf(a, b, c) for float32 arrays: the product is exact in float64 and the
+    sum is rounded to float32 (double rounding through float64 can differ from a
+    true FMA in the last bit, far below what the model measures)."""
+    return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(np.float32)
+
+
+def double_float_residual(ab0: np.ndarray, kl: int, b: np.ndarray, x: np.ndarray) -> np.ndarray:
+    """b - A0 x as the batched refinement forms it on the FP32 pipe: x split into
+    two floats (xh + xl), each term a xh = p + e exactly by FMA (plus a xl), and
+    the row sum kept as an unevaluated float pair (sh, sl) updated by Knuth's
+    TwoSum with explicit roundings, one column at a time from the left edge of
+    the band; the pair is added in FP64 at the end."""
+    n = ab0.shape[0]
+    f32 = np.float32
+    a0 = ab0.astype(f32)
+    xh = x.astype(f32)
+    xl = (x - xh.astype(np.float64)).astype(f32)
+    sh = np.zeros(n, f32)
+    sl = np.zeros(n, f32)
+    rows = np.arange(n)
+    for off in range(-kl, kl + 1):  # column j = i + off, left to right within each row's window
+        j = rows + off
+        ok = (j >= 0) & (j < n)
+        i, jj = rows[ok], j[ok]
+        a = a0[jj, 2 * kl + (i - jj)]
+        p = (a * xh[jj]).astype(f32)
+        e = _fma32(a, xl[jj], _fma32(a, xh[jj], -p))
+        t = (sh[i] + p).astype(f32)
+        z = (t - sh[i]).astype(f32)
+        corr = ((sh[i] - (t - z).astype(f32)).astype(f32) + (p - z).astype(f32)).astype(f32)
+        sl[i] = (sl[i] + (corr + e).astype(f32)).astype(f32)
+        sh[i] = t
+    return b - (sh.astype(np.float64) + sl.astype(np.float64))

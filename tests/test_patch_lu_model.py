@@ -35,3 +35,34 @@ def test_fp32_node_block_lu_refines_stiff_tangents(motion, n):
     assert info == 0
     x64, _ = lapack.dgbtrs(f, kl, kl, -r, piv)
     assert np.linalg.norm(x - x64) <= 1e-7 * np.linalg.norm(x64)
+
+
+def test_double_float_residual_is_fp64_accurate():
+    """The refinement's residual b - A0 x in double-float arithmetic on the FP32
+    pipe (PM.double_float_residual, as the batched refinement forms it): each
+    row within 2^-40 of its terms' magnitude sum Σ|a_ij x_j| (measured ≈ 2^-44 on
+    the batch's stiffest tangents), against an extended-precision sum."""
+    p, q = params_pair(M.ALEVB, M.F_PULL, 16, 16, kb=0.5, pull_speed=0.01)
+    mesh, om = M.Mesh(p), O.Mesh(q)
+    xms, cps = state(p, mesh, seed=4, amp=1e-4)
+    om.update_xms(xms, cps, DT)
+    r, ab = om.calc_r_K(xms, cps, DT, DT, nthreads=2)
+    kl = om.half_bw
+    ab0 = ab.astype(np.float32).astype(np.float64)
+    lu = PM.PatchLU(ab0, kl, PM.node_blocks(om.ID_inv))
+    x, _ = PM.refine(lu, ab0, kl, -r, tol=1e-6)
+    b = -r
+    df = PM.double_float_residual(ab0, kl, b, x)
+    n = len(b)
+    exact = np.zeros(n, dtype=np.longdouble)
+    mag = np.zeros(n)
+    rows = np.arange(n)
+    for off in range(-kl, kl + 1):
+        j = rows + off
+        ok = (j >= 0) & (j < n)
+        i, jj = rows[ok], j[ok]
+        a = ab0[jj, 2 * kl + (i - jj)]
+        exact[i] += a.astype(np.longdouble) * x[jj].astype(np.longdouble)
+        mag[i] += np.abs(a * x[jj])
+    err = np.abs(df.astype(np.longdouble) - (b.astype(np.longdouble) - exact)).astype(np.float64)
+    assert np.all(err <= 2.0**-40 * mag)
