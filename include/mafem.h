@@ -74,9 +74,23 @@ typedef struct mafem_params {
 
 /* The keyword arguments (`args...`) the hot path reads:
  * pull_speed (src/input/Bc.jl:234,240), bend_tm and bend_mf
- * (src/analysis/FiniteElement.jl:379, src/input/Bc.jl:389-390). */
+ * (src/analysis/FiniteElement.jl:379, src/input/Bc.jl:389-390).
+ * Two F_PULL extensions follow; the reference has no such keywords, and their
+ * zero values give the reference's behaviour:
+ *  - lambda0: the edge tension of the four STRETCH conditions and the initial
+ *    λ of every node.  The reference fixes both at kb / 4 (Bc.jl:259,
+ *    Input.jl:85); 0 keeps kb / 4.
+ *  - pull_centre: which element is pulled.  0 = element ceil(numel / 2)
+ *    (get_pull_el_id, PullForce.jl:8-13), which for an even num1el lies on the
+ *    right edge; 1 = element (floor(num1el/2) + 1, floor(num2el/2) + 1), the
+ *    centre element for any size (the same element as the reference's rule
+ *    when num1el == num2el is odd).  The pull force and x_pull use the same
+ *    element. */
 typedef struct mafem_args {
   double pull_speed, bend_tm, bend_mf;
+  double lambda0;
+  int32_t pull_centre;
+  int32_t reserved; /* 0 */
 } mafem_args;
 
 /* A view of the reference's `Mesh` struct (src/input/Mesh.jl:48-80): the fields
@@ -174,7 +188,8 @@ int mafem_run(mafem_handle* h, const double* dts, int32_t nsteps, double t0, maf
 
 /* calc_pull_force (src/analysis/PullForce.jl:61-80) on the resident state:
  * the velocity residual of calc_elem_dof_residuals over the 5x5 elements around
- * element ceil(numel/2) (get_adj_maps, PullForce.jl:25-53), summed over that
+ * the pulled element (ceil(numel/2), or the centre element with
+ * args.pull_centre; get_adj_maps, PullForce.jl:25-53), summed over that
  * element's nodes -> f_out[3].  The reference writes it to f-pull.txt after
  * each step of an F_PULL run (src/Analysis.jl:81-91). */
 int mafem_pull_force(mafem_handle* h, double* f_out);

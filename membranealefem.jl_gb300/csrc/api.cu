@@ -1777,14 +1777,15 @@ extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, 
 
 // calc_pull_force (PullForce.jl:61-80) with get_pull_el_id / get_adj_maps
 // (PullForce.jl:8-53): the velocity residual rv of calc_elem_dof_residuals
-// (area Gauss points only) of the (2·poly+1)² elements around element
-// ceil(numel/2), summed over that element's nodes.  The element rows come
+// (area Gauss points only) of the (2·poly+1)² elements around the pulled
+// element (ceil(numel/2), or the centre element with args.pull_centre),
+// summed over that element's nodes.  The element rows come
 // from the element kernel (area-only mode on the 25-element list); the sum is
 // done here in a fixed order.
 extern "C" int mafem_pull_force(mafem_handle* h, double* f_out) {
   if (!h || !f_out) return MAFEM_ERR_ARG;
   const int poly = h->p.poly, n1 = h->p.num1el, numel = h->numel, nq = h->nq, ndf = h->ndf;
-  const int pull = (numel + 1) / 2 - 1;  // ceil(numel / 2), 0-based
+  const int pull = pull_element(n1, h->p.num2el, h->a) - 1;  // get_pull_el_id (or the centre rule), 0-based
   std::vector<int> adj;
   for (int i = -poly; i <= poly; ++i)
     for (int j = -poly; j <= poly; ++j) adj.push_back(pull + i * n1 + j);
@@ -1823,7 +1824,7 @@ extern "C" int mafem_pull_force(mafem_handle* h, double* f_out) {
 // pull element's nine nodes, summed in IX order and divided by 9.
 extern "C" int mafem_pull_position(mafem_handle* h, double* x_out) {
   if (!h || !x_out) return MAFEM_ERR_ARG;
-  const int pull = (h->numel + 1) / 2 - 1;
+  const int pull = pull_element(h->p.num1el, h->p.num2el, h->a) - 1;
   std::vector<double> xms((size_t)h->numnp * 3);
   CK(cudaMemcpyAsync(xms.data(), h->P.xms, xms.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));

@@ -28,7 +28,18 @@ struct HostMesh {
   std::vector<double> neu_val;
   std::vector<int64_t> dir_unknown, dir_node;
   std::vector<double> dir_val;
+  double lambda0 = 0.0;  // F_PULL edge tension and initial λ (kb / 4 unless mafem_args.lambda0 > 0)
 };
+
+// 1-based id of the pulled element: ceil(numel / 2) (get_pull_el_id,
+// PullForce.jl:8-13), or with a.pull_centre the element
+// (floor(n1/2) + 1, floor(n2/2) + 1) numbered e1 + n1 (e2 - 1) (Mesh.jl:582-589).
+inline int pull_element(int n1, int n2, const mafem_args& a) {
+  if (a.pull_centre) return (n1 / 2 + 1) + n1 * (n2 / 2);
+  return (n1 * n2 + 1) / 2;
+}
+// F_PULL's tension value: kb / 4 (Bc.jl:259, Input.jl:85) unless a.lambda0 > 0.
+inline double pull_tension(const mafem_params& p, const mafem_args& a) { return a.lambda0 > 0 ? a.lambda0 : p.kb / 4; }
 
 // ---- state files (state_io.cpp) -------------------------------------------------
 // Julia's print(::Float64), appended to out.

@@ -204,6 +204,10 @@ int build_mesh(const mafem_params& p, const mafem_args& args, HostMesh& M, std::
   if (p.num1el < 1 || p.num2el < 1) { err = "num1el/num2el must be >= 1"; return MAFEM_ERR_ARG; }
   if (p.scenario < MAFEM_F_CAVI || p.scenario > MAFEM_F_BEND) { err = "unknown scenario"; return MAFEM_ERR_ARG; }
   if (p.motion < MAFEM_STATIC || p.motion > MAFEM_ALEVB) { err = "unknown motion"; return MAFEM_ERR_ARG; }
+  if (!(args.lambda0 >= 0.0) || !std::isfinite(args.lambda0)) { err = "lambda0 must be finite and >= 0 (0: kb / 4)"; return MAFEM_ERR_ARG; }
+  if (args.pull_centre != 0 && args.pull_centre != 1) { err = "pull_centre must be 0 or 1"; return MAFEM_ERR_ARG; }
+  if (args.lambda0 > 0.0 && p.scenario != MAFEM_F_PULL) { err = "lambda0 is an F_PULL extension"; return MAFEM_ERR_ARG; }
+  M.lambda0 = pull_tension(p, args);  // kb / 4 for every scenario but a F_PULL run given lambda0
   const int n1 = p.num1el, n2 = p.num2el, numel = n1 * n2;
   const int n1np = n1 + P, n2np = n2 + P, numnp = n1np * n2np;
   M.num1el = n1; M.num2el = n2; M.numel = numel; M.num1np = n1np; M.num2np = n2np; M.numnp = numnp;
@@ -321,7 +325,7 @@ int build_mesh(const mafem_params& p, const mafem_args& args, HostMesh& M, std::
       if (p.pn != 0.0) { err = "F_PULL with a normal pressure is not implemented (Bc.jl:266)"; return MAFEM_ERR_ARG; }
       for (int b = 0; b < 4; ++b) for (auto nd : bn[b]) { fix(VZ, nd); if (ale) { fix(VMX, nd); fix(VMY, nd); fix(VMZ, nd); } }
       for (int b = 0; b < 4; ++b) for (auto nd : bin[b]) { fix(VZ, nd); if (p.motion == MAFEM_ALEVB) fix(VMZ, nd); }
-      int ce = (numel + 1) / 2;  // get_pull_el_id = ceil(numel/2), PullForce.jl:8-13
+      const int ce = pull_element(n1, n2, args);  // get_pull_el_id (PullForce.jl:8-13), or the centre element
       for (int a = 0; a < 9; ++a) {
         int64_t nd = M.IX[(size_t)a + 9 * (size_t)(ce - 1)];
         fix(VX, nd); fix(VY, nd); fix(VZ, nd); dir(3, nd, args.pull_speed);
@@ -332,7 +336,7 @@ int build_mesh(const mafem_params& p, const mafem_args& args, HostMesh& M, std::
         fix(VX, c); fix(VY, c);
         if (p.motion != MAFEM_LAG) { fix(VMX, c); fix(VMY, c); }
       }
-      double lv = p.kb / 4;
+      const double lv = pull_tension(p, args);  // kb / 4 (Bc.jl:259) unless lambda0 is given
       neu(MAFEM_LEFT, MAFEM_STRETCH, lv); neu(MAFEM_RIGHT, MAFEM_STRETCH, lv);
       neu(MAFEM_TOP, MAFEM_STRETCH, lv); neu(MAFEM_BOTTOM, MAFEM_STRETCH, lv);
       break;
@@ -426,7 +430,7 @@ int prepare_input(const HostMesh& M, const mafem_params& p, double* xms, double*
       xms[s1 + (size_t)M.num1np * s2] = cx[s1];
       xms[(size_t)np + s1 + (size_t)M.num1np * s2] = cy[s2];
     }
-  double lv = p.kb / 4;  // Input.jl:85-86
+  const double lv = M.lambda0;  // Input.jl:85-86: kb / 4 unless lambda0 is given
   for (int i = 0; i < np; ++i) cps[i + (size_t)np * (M.dofs[6] - 1)] = lv;
   for (size_t q = 0; q < M.dir_node.size(); ++q) {  // Input.jl:103-108
     int u = (int)M.dir_unknown[q];

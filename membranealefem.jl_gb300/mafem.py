@@ -66,7 +66,8 @@ class _CParams(C.Structure):
 
 
 class _CArgs(C.Structure):
-    _fields_ = [("pull_speed", C.c_double), ("bend_tm", C.c_double), ("bend_mf", C.c_double)]
+    _fields_ = [("pull_speed", C.c_double), ("bend_tm", C.c_double), ("bend_mf", C.c_double),
+                ("lambda0", C.c_double), ("pull_centre", C.c_int32), ("reserved", C.c_int32)]
 
 
 _P64 = C.POINTER(C.c_int64)
@@ -248,7 +249,10 @@ def f_pull_line(rec) -> str:
 @dataclass
 class Params:
     """``Params`` (src/input/Params.jl:36-55) plus the keyword arguments the hot
-    path reads (``pull_speed``, ``bend_tm``, ``bend_mf``)."""
+    path reads (``pull_speed``, ``bend_tm``, ``bend_mf``) and two F_PULL
+    extensions with no reference keyword: ``lambda0`` (edge tension and initial
+    λ; 0 = the reference's kb / 4) and ``pull_centre`` (1 = pull the centre
+    element (floor(n1/2) + 1, floor(n2/2) + 1) instead of ceil(numel / 2))."""
 
     motion: int = ALEVB
     scenario: int = F_PULL
@@ -271,6 +275,8 @@ class Params:
     pull_speed: float = 0.0
     bend_tm: float = 1.0
     bend_mf: float = 0.0
+    lambda0: float = 0.0
+    pull_centre: int = 0
 
     def c_params(self) -> _CParams:
         adb = self.length ** 2 if self.alpha_db is None else self.alpha_db
@@ -279,7 +285,7 @@ class Params:
                         self.nen, adb, self.alpha_m, self.eps_k, self.eps_nr)
 
     def c_args(self) -> _CArgs:
-        return _CArgs(self.pull_speed, self.bend_tm, self.bend_mf)
+        return _CArgs(self.pull_speed, self.bend_tm, self.bend_mf, self.lambda0, self.pull_centre, 0)
 
 
 class Mesh:

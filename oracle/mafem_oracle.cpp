@@ -90,8 +90,14 @@ struct Params {
 };
 // keyword arguments used on the hot path (pull_speed: Bc.jl:234,240;
 // bend_tm / bend_mf: FiniteElement.jl:379, Bc.jl:389-390)
+// Two F_PULL extensions with no reference keyword (their zero values are the
+// reference's behaviour): lambda0 > 0 replaces the edge tension and initial λ
+// kb / 4 (Bc.jl:259, Input.jl:85); pull_centre = 1 pulls element
+// (floor(n1/2) + 1, floor(n2/2) + 1) instead of ceil(numel / 2).
 struct Args {
   double pull_speed = 0.0, bend_tm = 1.0, bend_mf = 0.0;
+  double lambda0 = 0.0;
+  int pull_centre = 0;
 };
 
 // ---- KnotVector (src/input/Spline.jl:20-96) --------------------------------
@@ -625,6 +631,14 @@ static void get_dofs(int motion, int* dofs, int& ndf) {
 
 // get_pull_el_id, src/analysis/PullForce.jl:8-13
 int get_pull_el_id(int numel) { return (int)std::ceil(numel / 2.0); }
+// the pulled element: get_pull_el_id, or with the centre extension the element
+// at (floor(n1/2) + 1, floor(n2/2) + 1), numbered e1 + n1 (e2 - 1) (Mesh.jl:582-589)
+int pull_el_id(const Params& p, const Args& a) {
+  if (a.pull_centre) return (p.num1el / 2 + 1) + p.num1el * (p.num2el / 2);
+  return get_pull_el_id(p.num1el * p.num2el);
+}
+// F_PULL's tension: kb / 4 (Bc.jl:259, Input.jl:85) unless lambda0 > 0
+double pull_lambda(const Params& p, const Args& a) { return a.lambda0 > 0 ? a.lambda0 : p.kb / 4; }
 
 // Bc.jl:15-40 and the per-scenario helpers
 static void scenario_bc_info(Mesh& M) {
@@ -700,7 +714,7 @@ static void scenario_bc_info(Mesh& M) {
         M.ID(M.dofs[vz], i) = -1;
         if (p.motion == ALEVB) M.ID(M.dofs[vmz], i) = -1;
       }
-    int ce = get_pull_el_id(M.numel);
+    int ce = pull_el_id(p, M.args);
     for (int a = 1; a <= NEN; ++a) {
       int node = M.IX(a, ce);
       M.ID(M.dofs[vx], node) = -1; M.ID(M.dofs[vy], node) = -1; M.ID(M.dofs[vz], node) = -1;
@@ -716,7 +730,7 @@ static void scenario_bc_info(Mesh& M) {
       M.ID(M.dofs[vx], c) = -1; M.ID(M.dofs[vy], c) = -1;
       if (p.motion != LAG) { M.ID(M.dofs[vmx], c) = -1; M.ID(M.dofs[vmy], c) = -1; }
     }
-    double lv = p.kb / 4;
+    double lv = pull_lambda(p, M.args);  // kb / 4 unless lambda0 is given
     M.inh_neu_bcs = {{LEFT, STRETCH, lv}, {RIGHT, STRETCH, lv}, {TOP, STRETCH, lv}, {BOTTOM, STRETCH, lv}};
     ORC_ASSERT(p.pn == 0.0, "F_PULL with a normal pressure is not implemented");
   } else {
@@ -1345,6 +1359,8 @@ typedef struct orc_params {
   int poly, gp1d, nders, nen;
   double adb, am, eps_k, eps_nr;
   double pull_speed, bend_tm, bend_mf;
+  double lambda0;
+  int pull_centre;
 } orc_params;
 
 const char* orc_last_error() { return g_err.c_str(); }
@@ -1502,6 +1518,9 @@ int orc_mesh_create(const orc_params* q, void** out) {
     ORC_ASSERT(p.nen == NEN && p.poly == POLY && p.nders == NDERS, "compile-time constants mismatch");
     Args a;
     a.pull_speed = q->pull_speed; a.bend_tm = q->bend_tm; a.bend_mf = q->bend_mf;
+    a.lambda0 = q->lambda0; a.pull_centre = q->pull_centre;
+    ORC_ASSERT(a.lambda0 >= 0.0 && std::isfinite(a.lambda0), "lambda0 must be finite and >= 0");
+    ORC_ASSERT(a.lambda0 == 0.0 || p.scenario == F_PULL, "lambda0 is an F_PULL extension");
     // check_params' scenario conditions (Params.jl:97-119)
     if (p.scenario == F_BEND) {
       ORC_ASSERT(a.bend_mf == p.kb / 2 / p.length, "α = 1/2 is the half-angle");
@@ -1591,7 +1610,7 @@ int orc_prepare_input(void* h, double* xms, double* cps) {
     auto X = get_2d_bspline_cps(m->kv1, m->kv2, [&](double z1, double) { return p.length * (z1 - 0.5); });
     auto Y = get_2d_bspline_cps(m->kv1, m->kv2, [&](double, double z2) { return p.length * (z2 - 0.5); });
     for (int i = 0; i < np; ++i) { xms[i] = X[i]; xms[i + np] = Y[i]; }
-    double lv = p.kb / 4;
+    double lv = p.scenario == F_PULL ? pull_lambda(p, m->args) : p.kb / 4;  // Input.jl:85 (kb / 4)
     for (int i = 0; i < np; ++i) cps[i + (size_t)np * (m->dofs[lam] - 1)] = lv;
     for (const auto& bc : m->inh_dir_bcs) {
       cps[(bc.node - 1) + (size_t)np * (m->dofs[bc.unknown] - 1)] = bc.value;
@@ -1679,14 +1698,14 @@ void orc_update_xms(void* h, double* xms, const double* c, double dt) { update_x
 
 // calc_pull_force (PullForce.jl:61-80) with get_pull_el_id (:8-13) and
 // get_adj_maps (:25-53): real(rv) of calc_elem_dof_residuals of each element
-// adjacent to element ceil(numel/2), at the nodes it shares with that element,
+// adjacent to the pulled element (ceil(numel/2), or the centre element), at the nodes it shares with that element,
 // summed over the pulled element's nodes -> f[3].  Ids outside 1..numel are an
 // error (the reference would raise a BoundsError).
 int orc_pull_force(void* h, const double* xms, const double* cps, double* f) {
   ORC_TRY({
     Mesh* m = (Mesh*)h;
     const int poly = m->p.poly, numel = m->numel, n1 = m->p.num1el;
-    const int pull = (numel + 1) / 2;  // ceil(numel / 2), 1-based
+    const int pull = pull_el_id(m->p, m->args);  // ceil(numel / 2) or the centre element, 1-based
     std::vector<int> pull_nodes;
     for (int a = 1; a <= NEN; ++a) pull_nodes.push_back(m->IX(a, pull));
     std::vector<double> rv_pull((size_t)3 * NEN, 0.0);

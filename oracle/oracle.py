@@ -37,14 +37,17 @@ class _Params(C.Structure):
         ("pn", C.c_double), ("poly", C.c_int), ("gp1d", C.c_int), ("nders", C.c_int),
         ("nen", C.c_int), ("adb", C.c_double), ("am", C.c_double), ("eps_k", C.c_double),
         ("eps_nr", C.c_double), ("pull_speed", C.c_double), ("bend_tm", C.c_double),
-        ("bend_mf", C.c_double),
+        ("bend_mf", C.c_double), ("lambda0", C.c_double), ("pull_centre", C.c_int),
     ]
 
 
 @dataclass
 class Params:
     """Mirror of the reference's ``Params`` (src/input/Params.jl:36-55) plus the
-    keyword arguments the hot path reads (pull_speed, bend_tm, bend_mf)."""
+    keyword arguments the hot path reads (pull_speed, bend_tm, bend_mf), and two
+    F_PULL extensions with no reference keyword: lambda0 (edge tension and
+    initial λ; 0 = the reference's kb / 4) and pull_centre (1 = pull the centre
+    element (floor(n1/2) + 1, floor(n2/2) + 1) instead of ceil(numel / 2))."""
 
     motion: int = ALEVB
     scenario: int = F_PULL
@@ -66,13 +69,15 @@ class Params:
     pull_speed: float = 0.0
     bend_tm: float = 1.0
     bend_mf: float = 0.0
+    lambda0: float = 0.0
+    pull_centre: int = 0
 
     def to_c(self) -> _Params:
         adb = self.length ** 2 if self.adb is None else self.adb
         return _Params(self.motion, self.scenario, self.num1el, self.num2el, self.length,
                        self.kb, self.kg, self.zv, self.pn, self.poly, self.gp1d, self.nders,
                        self.nen, adb, self.am, self.eps_k, self.eps_nr, self.pull_speed,
-                       self.bend_tm, self.bend_mf)
+                       self.bend_tm, self.bend_mf, self.lambda0, self.pull_centre)
 
 
 def build() -> str:
@@ -560,6 +565,38 @@ def time_step_sparse(mesh: Mesh, xms, cps, time: float, dt: float, nthreads: int
     if not eps[-1] < mesh.p.eps_nr:
         raise AssertionFailed("did not reach Newton--Raphson tolerance")
     return eps
+
+
+# ---- seeded initial states -------------------------------------------------------------
+# The benchmarks' synthetic input: prepare_input's flat patch plus an out-of-plane
+# perturbation of the interior nodes drawn from SplitMix64 (Steele, Lea and Flood,
+# "Fast splittable pseudorandom number generators", OOPSLA 2014; the published
+# constants).  The product's Python layer draws the same numbers; this copy lets the
+# CPU baseline build its input without loading the product library.
+
+def splitmix64(seed: int, n: int) -> np.ndarray:
+    """n uniform doubles in [0, 1): the top 53 bits of successive SplitMix64 outputs."""
+    mask = (1 << 64) - 1
+    s = seed & mask
+    out = np.empty(n, dtype=np.float64)
+    for i in range(n):
+        s = (s + 0x9E3779B97F4A7C15) & mask
+        z = s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & mask
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & mask
+        z ^= z >> 31
+        out[i] = (z >> 11) * (1.0 / 9007199254740992.0)
+    return out
+
+
+def perturb_interior_z(mesh: Mesh, xms: np.ndarray, seed: int = 0, amp: float = 1e-4) -> np.ndarray:
+    """z += amp (2u - 1), u ~ SplitMix64(seed), on the nodes off the outer boundary."""
+    u = splitmix64(seed, mesh.numnp)
+    s1 = np.arange(mesh.numnp) % mesh.num1np
+    s2 = np.arange(mesh.numnp) // mesh.num1np
+    interior = (s1 > 0) & (s1 < mesh.num1np - 1) & (s2 > 0) & (s2 < mesh.num2np - 1)
+    xms[:, 2] += np.where(interior, amp * (2.0 * u - 1.0), 0.0)
+    return xms
 
 
 # ---- state files ---------------------------------------------------------------------

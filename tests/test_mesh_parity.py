@@ -78,3 +78,52 @@ def test_errors_like_the_reference():
     assert M.Mesh(p).numnp == O.Mesh(q).numnp == 25
     with pytest.raises(O.AssertionFailed):  # Params.jl:108-115
         O.Mesh(O.Params(scenario=O.F_POIS, motion=O.LAG, num1el=3, num2el=3))
+
+
+# The two F_PULL extensions (no reference keyword): lambda0 (edge tension and
+# initial λ instead of kb / 4, Bc.jl:259, Input.jl:85) and pull_centre (the
+# element (floor(n1/2) + 1, floor(n2/2) + 1) instead of ceil(numel / 2),
+# PullForce.jl:8-13).  Library and oracle must agree bit for bit.
+EXT_CASES = [(M.LAG, 8, 8, 0.0, 1), (M.ALEVB, 12, 12, 2.5, 1), (M.ALEVB, 48, 48, 0.1, 1),
+             (M.LAG, 9, 9, 10.0, 0), (M.ALEV, 6, 7, 0.7, 1), (M.ALEVB, 16, 16, 0.0, 0)]
+
+
+@pytest.mark.parametrize("motion,n1,n2,lam0,centre", EXT_CASES)
+def test_pull_extensions_bit_exact(motion, n1, n2, lam0, centre):
+    p, q = params_pair(motion, M.F_PULL, n1, n2, kb=1.3, lambda0=lam0, pull_centre=centre)
+    m, o = M.Mesh(p), O.Mesh(q)
+    assert np.array_equal(m.ID, o.ID) and np.array_equal(m.LM, o.LM) and m.half_bw == o.half_bw
+    assert m.neumann() == o.neumann() and m.dirichlet() == o.dirichlet()
+    lv = lam0 if lam0 > 0 else 1.3 / 4
+    assert [v for _, _, v in m.neumann()] == [lv] * 4
+    _, x1, c1 = M.prepare_input(p, m)
+    x2, c2 = o.prepare_input()
+    assert np.array_equal(c1, c2)
+    assert np.all(c1[:, m.dofs[6] - 1] == lv)
+    # the pulled nodes: the nine nodes of the chosen element carry the pull speed
+    e = (n1 // 2 + 1) + n1 * (n2 // 2) if centre else (n1 * n2 + 1) // 2
+    pulled = sorted({nd for u, nd, v in m.dirichlet() if u == 3})
+    assert pulled == sorted(m.IX[:, e - 1].tolist())
+
+
+def test_centre_rule_is_the_reference_rule_for_odd_square_patches():
+    for n in (5, 9, 17, 49):
+        a = M.Mesh(M.Params(motion=M.LAG, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, pull_speed=0.1))
+        b = M.Mesh(M.Params(motion=M.LAG, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, pull_speed=0.1,
+                            pull_centre=1))
+        assert np.array_equal(a.ID, b.ID) and a.dirichlet() == b.dirichlet()
+
+
+def test_pull_extension_arguments_rejected():
+    for kw in (dict(lambda0=-1.0), dict(lambda0=float("nan")), dict(pull_centre=2)):
+        p, q = params_pair(M.LAG, M.F_PULL, 4, 4, **kw)
+        with pytest.raises(M.MafemError):
+            M.Mesh(p)
+        if "lambda0" in kw:
+            with pytest.raises(O.AssertionFailed):
+                O.Mesh(q)
+    p, q = params_pair(M.STATIC, M.F_COUE, 3, 3, lambda0=1.0)  # F_PULL only
+    with pytest.raises(M.MafemError):
+        M.Mesh(p)
+    with pytest.raises(O.AssertionFailed):
+        O.Mesh(q)

@@ -18,10 +18,14 @@ pytestmark = pytest.mark.gpu
 
 # (the 32x32 benchmark mesh with the benchmark's step: larger pull speeds lose
 # Newton convergence on it, in the oracle as on the GPU)
-@pytest.mark.parametrize("motion,n,speed,dt", [(M.ALEVB, 9, 1.0, 0.01), (M.ALEVB, 8, 1.0, 0.01),
-                                               (M.LAG, 7, 1.0, 0.01), (M.ALEVB, 32, 0.02, 0.005)])
-def test_pull_force_matches_oracle(motion, n, speed, dt):
-    p, q = params_pair(motion, M.F_PULL, n, n, pull_speed=speed)
+# The last two cases use the F_PULL extensions: the centre element of an even
+# patch and a tension lambda0 other than kb / 4.
+@pytest.mark.parametrize("motion,n,speed,dt,ext", [(M.ALEVB, 9, 1.0, 0.01, {}), (M.ALEVB, 8, 1.0, 0.01, {}),
+                                                   (M.LAG, 7, 1.0, 0.01, {}), (M.ALEVB, 32, 0.02, 0.005, {}),
+                                                   (M.ALEVB, 8, 1.0, 0.01, dict(pull_centre=1, lambda0=2.0)),
+                                                   (M.LAG, 10, 0.5, 0.01, dict(pull_centre=1, lambda0=0.3))])
+def test_pull_force_matches_oracle(motion, n, speed, dt, ext):
+    p, q = params_pair(motion, M.F_PULL, n, n, pull_speed=speed, **ext)
     mesh, om = M.Mesh(p), O.Mesh(q)
     xms, cps = state(p, mesh, seed=2, amp=1e-4)
     t = 0.0

@@ -27,7 +27,7 @@ assert dist is not None and world == 2 and rank == int(os.environ["RANK"])
 bench.barrier(dist)
 m = bench.allmax(dist, 10.0 * (rank + 1))
 bench.cpu_baseline = lambda **kw: {"value": 0.5, "unit": "time-steps/s", "cores": 1, "kind": "port",
-                                   "sample": "stub"}
+                                   "sample": "stub", "steps_timed": 2, "first_timed_step": 4}
 sys.argv = ["bench.py", "--impl", "reference", "--gpus", "2", "--steps", "2", "--warmup", "3"]
 buf = io.StringIO()
 with contextlib.redirect_stdout(buf):
@@ -83,10 +83,22 @@ def test_cpu_baseline_times_the_oracle_on_a_small_patch():
     LU on the host cores), on a 6 x 6 version of the workload."""
     import bench
     wl = dict(bench.WORKLOAD, n=6)
-    cb = bench.cpu_baseline(wl=wl, max_seconds=10.0, max_steps=2)
+    cb = bench.cpu_baseline(wl=wl, warmup=1, max_seconds=10.0, max_steps=2)
     assert cb["kind"] == "port" and cb["unit"] == "time-steps/s"
     assert cb["value"] > 0 and cb["cores"] >= 1
-    assert cb["sample"].startswith("first 2 time steps")
+    assert cb["steps_timed"] == 2 and cb["first_timed_step"] == 2
+    assert cb["sample"].startswith("time steps 2..3")
+
+
+def test_reference_arm_loads_only_the_oracle():
+    """The CPU baseline builds its mesh and seeded initial state with the oracle:
+    the product library is never loaded into that process."""
+    code = ("import sys; sys.path.insert(0, sys.argv[1]); import bench; "
+            "bench.cpu_baseline(wl=dict(bench.WORKLOAD, n=6), warmup=1, max_steps=1); "
+            "maps = open('/proc/self/maps').read(); "
+            "print(int('libmafem' in maps), int('liboracle' in maps))")
+    out = subprocess.run([sys.executable, "-c", code, ROOT], capture_output=True, text=True, check=True)
+    assert out.stdout.split() == ["0", "1"], out.stdout + out.stderr
 
 
 def test_rel_err_vs_oracle_report():
@@ -102,8 +114,8 @@ def test_rel_err_vs_oracle_report():
 
     wl = dict(bench.WORKLOAD, n=6)
     ref = {}
-    bench.cpu_baseline(wl=wl, max_seconds=10.0, max_steps=2, state_out=ref)
-    assert ref["steps"] == 2
+    bench.cpu_baseline(wl=wl, warmup=1, max_seconds=10.0, max_steps=2, state_out=ref)
+    assert ref["steps"] == 3
 
     fields = {f.name for f in dataclasses.fields(O.Params)}
 
@@ -134,5 +146,5 @@ def test_rel_err_vs_oracle_report():
     fake = types.SimpleNamespace(**{k: getattr(M, k) for k in dir(M) if not k.startswith("__")})
     fake.Solver = OracleSolver
     rep = bench.rel_err_vs_oracle(fake, ref, wl)
-    assert rep["steps"] == 2 and rep["bar"] == 1e-9
+    assert rep["steps"] == 3 and rep["bar"] == 1e-9
     assert max(rep["xms"], rep["velocities"], rep["lambda"]) < 1e-11, rep
