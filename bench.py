@@ -40,8 +40,7 @@ WORKLOAD = dict(name="ALEVB tether pull, 32x32 graded patch (34x34 control point
                 motion=5, n=32, length=1.0, kb=1.0, kg=-0.5, zeta_v=1.0, dt=0.005, pull_speed=0.02,
                 seed=0, amp=1e-4)
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the
-# dominant kernel, from one ncu capture of this workload (profiles/
-# blk_factor_persist_kernel.alevb32.md gives the command); None until captured.
+# dominant kernel, from one ncu capture of this workload; None until captured.
 NCU_TRAFFIC = {"blk_factor_persist_kernel<double>": 74_519_552 + 18_702_336}
 METRIC = "membrane time-steps/s"
 

@@ -95,10 +95,13 @@ typedef struct mafem_args {
 
 /* A view of the reference's `Mesh` struct (src/input/Mesh.jl:48-80): the fields
  * the hot path reads, in the reference's own layout.  A Julia caller fills it
- * from its `mesh` (see INTEGRATION.md); mafem_mesh_view() fills it from a mesh
+ * from its `mesh`; mafem_mesh_view() fills it from a mesh
  * built by mafem_mesh_build().  GP tables pack one GpBasisFnsζα
  * (src/input/GpBasisFn.jl:96-112) as 55 doubles: w, N[9], ∂Nα (9x2
  * column-major), ∂∂Nαβ (9x3 column-major, Voigt order 11, 22, 12). */
+/* mafem_create checks IX against the tensor-product connectivity of
+ * construct_IX (src/input/Mesh.jl:574-593) and every ID, uel_ids and dofs entry
+ * against its range, and rejects (MAFEM_ERR_ARG) a mesh that differs. */
 typedef struct mafem_mesh_desc {
   int64_t num1el, num2el, numel, num1np, num2np, numnp, ndf, nmdf;
   int64_t dofs[8];        /* mesh.dofs[Dof.vx .. Dof.pm]: 1-based dof index, 0 if absent */
@@ -328,6 +331,31 @@ int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, int64_t* ou
 /* Number of kernels this handle has enqueued since mafem_create. */
 int64_t mafem_launch_count(const mafem_handle* h);
 
+/* Solve K x = rhs (host arrays, nmdf entries) for a caller's K -- a host band in
+ * the layout mafem_calc_r_K writes (column j at band + j*ldab, A(i,j) at row
+ * kl+ku+i-j, kl = ku = mafem_mesh_half_bandwidth()) -- through the handle's own
+ * factorisation: node-block pivoting, full partial pivoting when a node block
+ * has no usable pivot, FP64 refinement in the FP32 form.  The reference solves
+ * with `K \ r` (src/analysis/FiniteElement.jl:38); this entry point exposes the
+ * same solver to systems the assembly would not produce (tests, diagnostics).
+ * MAFEM_ZERO_PIVOT when K is singular.  The next mafem_solve needs a new
+ * mafem_calc_r_K. */
+int mafem_solve_band(mafem_handle* h, const double* band, int64_t ldab, const double* rhs, double* x_out);
+/* Factorisations this handle redid with full partial pivoting because a node
+ * block had no usable pivot (or the batched FP32 solve handed the iteration
+ * back). */
+int64_t mafem_fallback_count(const mafem_handle* h);
+/* Failure-detection test hook (no reference counterpart; the reference has no
+ * inter-CTA waits).  The cooperative forward and back substitutions' waits for
+ * another CTA give up after limit_polls polls (0: the default, 2^22), and the
+ * back substitution never publishes the completion flag of the panel
+ * withhold_panel places before the last (0: the last panel, which every panel
+ * whose columns reach it waits for; -1: none).  A Newton iteration
+ * whose wait ran out leaves the state unchanged and returns MAFEM_ERR_CUDA
+ * ("a bounded wait ... ran out"); every CTA returns, the device stays usable,
+ * and the next call (after mafem_set_wait_test(h, 0, -1)) runs normally. */
+int mafem_set_wait_test(mafem_handle* h, int32_t limit_polls, int32_t withhold_panel);
+
 /* FP32 form: FP64 iterative refinement of each linear solve stops at tol
  * (default 1e-10) or fails after max_sweeps sweeps (default 30) or when it stops
  * converging (MAFEM_REFINE_STALLED).  A handle stepped on its own stops when
@@ -369,11 +397,13 @@ int mafem_probe_fp64_tflops(double* tflops);
  * device byte, or a loop that cannot afford cudaMalloc's device-wide
  * synchronisation.  Its scratch is one static 32 MiB device array inside the
  * library (held by every GPU that loads it until exit): systems needing more --
- * about 8*n*(3kl+65) + 4*n*(kl+33)/32 bytes -- return MAFEM_ERR_ARG.  All calls
- * share that array, so calls that overlap on the GPU race; order them on one
- * stream.  The first call on a device looks the array up (cudaGetSymbolAddress)
- * and must come before any stream capture.  Runs on `stream` (NULL = default
- * stream) and returns after synchronising it. */
+ * about 8*n*(3kl+65) + 4*n*(kl+33)/32 bytes, e.g. a 16x16 ALEVB tangent fits and
+ * a 24x24 one does not -- return MAFEM_ERR_ARG.  All calls share that array, so
+ * calls that overlap on the GPU race; order them on one stream.  Each call looks
+ * the array up on the current device (cudaGetSymbolAddress).  Full partial
+ * pivoting (LAPACK gbtrf's pivot rule); a zero, infinite or NaN pivot gives
+ * MAFEM_ZERO_PIVOT, a NaN or infinity in x MAFEM_NAN_DETECTED.  Runs on
+ * `stream` (NULL = default stream) and returns after synchronising it. */
 int mafem_band_solve_noalloc(const double* band_dev, int64_t n, int64_t kl, int64_t ku, int64_t ldab,
                              const double* rhs_dev, double* x_dev, void* stream);
 

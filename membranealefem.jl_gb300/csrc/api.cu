@@ -126,6 +126,8 @@ struct mafem_handle {
   bool patch_ok = false;
   bool ss_patch = false;  // the iteration in progress ran through a batch's patch solve
   PatchJob job{};
+  WaitTest wait_test;                   // mafem_set_wait_test (failure-detection tests)
+  const double* host_band = nullptr;    // mafem_solve_band: the caller's band (padded layout), for the fallback
   std::unique_ptr<StateWriter> writer;  // state files, created by the first write
   double* d_snap = nullptr;             // device snapshots: nsnap x [xms | cps]
   int nsnap = 0;
@@ -202,6 +204,40 @@ static int validate(const mafem_mesh_desc* d, const mafem_params* p, std::string
     return MAFEM_ERR_ARG;
   }
   if (!d->IX || !d->ID || !d->uel_ids || !d->ufns) { err = "missing mesh arrays"; return MAFEM_ERR_ARG; }
+  // The gathers and the pull-force neighbourhood rely on the tensor-product
+  // connectivity of construct_IX (Mesh.jl:574-593): node (a1, a2) of element
+  // (e1, e2) is control point (e1 + a1) + num1np (e2 + a2) (0-based).  Any other
+  // IX -- or an entry out of range -- is rejected rather than silently misread.
+  for (int64_t e2 = 0; e2 < d->num2el; ++e2)
+    for (int64_t e1 = 0; e1 < d->num1el; ++e1)
+      for (int a = 0; a < 9; ++a) {
+        const int64_t want = 1 + (e1 + a % 3) + d->num1np * (e2 + a / 3);
+        if (d->IX[a + 9 * (e1 + d->num1el * e2)] != want) {
+          err = "IX differs from the tensor-product connectivity (Mesh.jl:574-593) at element " +
+                std::to_string(1 + e1 + d->num1el * e2) + ", node " + std::to_string(a + 1);
+          return MAFEM_ERR_ARG;
+        }
+      }
+  for (int64_t k = 0; k < d->ndf * d->numnp; ++k)
+    if (d->ID[k] < 0 || d->ID[k] > d->nmdf) { err = "ID entry outside 0..nmdf"; return MAFEM_ERR_ARG; }
+  if (d->n_uel < 1) { err = "n_uel must be >= 1"; return MAFEM_ERR_ARG; }
+  for (int64_t e = 0; e < d->numel; ++e)
+    if (d->uel_ids[e] < 1 || d->uel_ids[e] > d->n_uel) { err = "uel_ids entry outside 1..n_uel"; return MAFEM_ERR_ARG; }
+  for (int b = 0; b < 4; ++b) {
+    const int64_t nb = (b == 0 || b == 2) ? d->num1el : d->num2el;
+    if (d->bdry_n_uel[b] > 0 && d->bdry_uel_ids[b] && d->bdry_ufns[b]) {
+      for (int64_t k = 0; k < nb; ++k)
+        if (d->bdry_uel_ids[b][k] < 1 || d->bdry_uel_ids[b][k] > d->bdry_n_uel[b]) {
+          err = "bdry_uel_ids entry outside 1..bdry_n_uel";
+          return MAFEM_ERR_ARG;
+        }
+    } else if (d->bdry_n_uel[b] != 0) {
+      err = "missing boundary tables";
+      return MAFEM_ERR_ARG;
+    }
+  }
+  for (int u = 0; u < 8; ++u)
+    if (d->dofs[u] < 0 || d->dofs[u] > d->ndf) { err = "dofs entry outside 0..ndf"; return MAFEM_ERR_ARG; }
   if (d->n_neu < 0 || d->n_neu > kMaxNeu) { err = "at most 8 Neumann entries are supported"; return MAFEM_ERR_ARG; }
   for (int64_t k = 0; k < d->n_neu; ++k) {
     if (d->neu_bdry[k] < 1 || d->neu_bdry[k] > 4) { err = "bad Neumann boundary"; return MAFEM_ERR_ARG; }
@@ -678,9 +714,13 @@ static int factor(mafem_handle* h, double* x, const double* rhs0) {
       h->last_blk = true;
       return MAFEM_OK;
     }
-    // fallback: rebuild the band from the element blocks, then full pivoting
+    // fallback: rebuild the band from the element blocks (or the caller's band
+    // of mafem_solve_band), then full pivoting
     ++h->fallbacks;
-    if (fp64)
+    if (fp64 && h->host_band)
+      CK(cudaMemcpyAsync(h->d_band, h->host_band, (size_t)h->L.ldb * n * sizeof(double), cudaMemcpyHostToDevice,
+                         h->st));
+    else if (fp64)
       launch_band_gather<double>(h->P, h->ndf, h->nq, h->L, (const double*)h->d_Kel, (double*)h->d_band, h->st);
     else
       CK(cudaMemcpyAsync(h->d_band, h->d_band0, (size_t)h->L.ldb * n * sizeof(float), cudaMemcpyDeviceToDevice,
@@ -710,7 +750,7 @@ static void blk_back_solve(mafem_handle* h, double* y) {
   if (h->bwd_grid > 0) {
     ++h->epoch;
     if (blk_backward<double, T>((const T*)h->d_band, h->L, h->blk, (const T*)h->d_rdiag, y, h->d_flags, h->epoch,
-                                h->d_info + 1, h->bwd_grid, h->st) == 0) {
+                                h->d_info + 1, h->bwd_grid, h->st, h->wait_test) == 0) {
       h->launches += 1;
       return;
     }
@@ -728,7 +768,7 @@ static void blk_fwd_solve(mafem_handle* h, double* y) {
   if (h->bwd_grid > 0) {
     ++h->epoch;
     if (blk_forward_coop<double, T>((const T*)h->d_band, h->L, h->blk, h->d_perm, (const T*)h->d_rdiag, y, h->d_zbuf,
-                                    h->d_flags, h->epoch, h->d_info + 1, h->bwd_grid, h->st) == 0) {
+                                    h->d_flags, h->epoch, h->d_info + 1, h->bwd_grid, h->st, h->wait_test) == 0) {
       h->launches += 1;
       return;
     }
@@ -870,6 +910,7 @@ extern "C" int mafem_calc_r_K(mafem_handle* h, double time, double dt, double* r
 extern "C" int mafem_solve(mafem_handle* h, const double* r, double* du_out) {
   if (!h || !r || !du_out) return MAFEM_ERR_ARG;
   const int64_t n = h->nmdf;
+  CK(cudaMemsetAsync(h->d_info, 0, 2 * sizeof(int), h->st));
   CK(cudaMemcpyAsync(h->d_res, r, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
   // keep the right-hand side in d_dx for the plain path (factor_and_solve reads rhs_dev)
   double* rhs = h->precision == MAFEM_PLAIN_FP64 ? h->d_dx : h->d_r;
@@ -919,6 +960,7 @@ static void step_begin(mafem_handle* h, double time, double dt) {
 static int iter_enqueue(mafem_handle* h) {
   const int64_t n = h->nmdf;
   h->ss_patch = false;
+  CK(cudaMemsetAsync(h->d_info, 0, 2 * sizeof(int), h->st));  // zero-pivot column, wait-ran-out word
   cudaEventRecord(h->ev[0], h->st);
   int rc = assemble(h, h->ss_time, h->ss_dt);
   if (rc) return rc;
@@ -934,7 +976,7 @@ static int iter_enqueue(mafem_handle* h) {
     return rc;
   }
   cudaEventRecord(h->ev[3], h->st);
-  launch_newton_update(h->P, h->pp, h->ss_dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st, h->d_info);
+  launch_newton_update(h->P, h->pp, h->ss_dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st, h->d_info, h->d_info + 1);
   h->launches += 2;
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -964,7 +1006,8 @@ static int iter_enqueue_patch_end(mafem_handle* h, cudaEvent_t solved) {
   cudaEventRecord(h->ev[2], h->st);
   cudaEventRecord(h->ev[3], h->st);
   // the update is skipped when the patch solve failed (status word nonzero)
-  launch_newton_update(h->P, h->pp, h->ss_dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st, h->d_info + 2);
+  launch_newton_update(h->P, h->pp, h->ss_dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st, h->d_info + 2,
+                       h->d_info + 1);
   h->launches += 2;
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -990,6 +1033,10 @@ enum { kIterAgain = -100, kIterDone = -101 };
 static int iter_finish(mafem_handle* h) {
   CK(cudaEventSynchronize(h->ev[4]));
   accum_times(h);
+  if (!std::isfinite(h->h_out[1])) {  // the FP64 residual itself is not finite: nothing to redo
+    h->err = "non-finite residual";
+    return MAFEM_NAN_DETECTED;
+  }
   if (h->ss_patch) {
     int ps[4];
     std::memcpy(ps, h->h_out + 5, sizeof ps);
@@ -1924,6 +1971,64 @@ extern "C" int mafem_restore(mafem_handle* h, int32_t slot) {
   CK(cudaMemcpyAsync(h->P.cps, cps, sizeof(double) * h->numnp * h->ndf, cudaMemcpyDeviceToDevice, h->st));
   return MAFEM_OK;
 }
+
+extern "C" int mafem_set_wait_test(mafem_handle* h, int32_t limit_polls, int32_t withhold_panel) {
+  if (!h || limit_polls < 0 || withhold_panel < -1) return MAFEM_ERR_ARG;
+  h->wait_test.limit = limit_polls;
+  h->wait_test.withhold = withhold_panel;
+  return MAFEM_OK;
+}
+
+// Solve K x = rhs for a caller's K (host band in mafem_calc_r_K's layout)
+// through the handle's own factorisation and solves: the band replaces the
+// assembled tangent (and, in the FP32 form, the refinement's A0).
+extern "C" int mafem_solve_band(mafem_handle* h, const double* band, int64_t ldab, const double* rhs, double* x_out) {
+  if (!h || !band || !rhs || !x_out) return MAFEM_ERR_ARG;
+  const BandLayout& L = h->L;
+  if (ldab < 2LL * L.kl + L.ku + 1) {
+    h->err = "ldab must be >= 2*kl + ku + 1";
+    return MAFEM_ERR_ARG;
+  }
+  const int64_t n = h->nmdf;
+  const size_t rows = 2 * (size_t)L.kl + L.ku + 1;
+  // the handle's padded layout: column j at j*ldb, the caller's row r at row nb + r
+  // (rows 0..nb-1 and nb+rows..ldb-1 of every column are padding, zero)
+  std::vector<double> hb64;
+  if (h->precision == MAFEM_PLAIN_FP64) {
+    hb64.assign((size_t)L.ldb * n, 0.0);
+    for (int64_t j = 0; j < n; ++j)
+      for (size_t r = 0; r < rows; ++r) hb64[(size_t)j * L.ldb + L.nb + r] = band[j * ldab + r];
+    CK(cudaMemcpyAsync(h->d_band, hb64.data(), hb64.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  } else {
+    std::vector<float> tmp((size_t)L.ldb * n, 0.0f);
+    for (int64_t j = 0; j < n; ++j)
+      for (size_t r = 0; r < rows; ++r) tmp[(size_t)j * L.ldb + L.nb + r] = (float)band[j * ldab + r];
+    CK(cudaMemcpyAsync(h->d_band, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  h->factored = false;
+  CK(cudaMemsetAsync(h->d_info, 0, 2 * sizeof(int), h->st));
+  CK(cudaMemcpyAsync(h->d_res, rhs, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  double* rdev = h->precision == MAFEM_PLAIN_FP64 ? h->d_dx : h->d_r;
+  CK(cudaMemcpyAsync(rdev, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+  int sweeps = 0;
+  const int64_t fb0 = h->fallbacks;
+  h->host_band = h->precision == MAFEM_PLAIN_FP64 ? hb64.data() : nullptr;
+  int rc = factor_and_solve(h, rdev, &sweeps);
+  if (rc == MAFEM_OK) CK(cudaStreamSynchronize(h->st));  // hb64 must outlive the fallback's copy
+  h->host_band = nullptr;
+  h->factored = false;  // the band holds the caller's matrix, not the assembled tangent
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(x_out, h->d_x, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 2 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  rc = check_info(h);
+  if (rc == MAFEM_OK && h->fallbacks > fb0) h->err = "solved with full partial pivoting (a node block had no usable pivot)";
+  return rc;
+}
+
+extern "C" int64_t mafem_fallback_count(const mafem_handle* h) { return h ? h->fallbacks : -1; }
 
 extern "C" int mafem_set_refinement(mafem_handle* h, int32_t max_sweeps, double tol) {
   if (!h || max_sweeps < 1 || max_sweeps > 1000 || !(tol > 0.0) || !(tol < 1.0)) return MAFEM_ERR_ARG;

@@ -85,25 +85,25 @@ __global__ void predictor_kernel(DevPatch P, PhysParams pp, double dt) {
 
 // Newton update (FiniteElement.jl:41-46): Δu = -x, Δcps[ID_inv] = Δu, cps += Δcps,
 // xms[:, j] += dt Δcps[:, m_motion_order[j]]; per-block partial sums of Δu² and r².
-// skip: when *skip != 0 (the factorisation found no usable pivot) the state is
-// left unchanged; the host redoes the iteration with full partial pivoting.
+// skip, skip2: when either word is nonzero (the factorisation found no usable
+// pivot, the batched solve failed, or a bounded wait ran out) the state is left
+// unchanged and only r² is summed (so a non-finite residual still shows); the
+// host redoes the iteration or reports the failure.
 __global__ void newton_update_kernel(DevPatch P, PhysParams pp, double dt, const double* __restrict__ x,
                                      const double* __restrict__ r, double* __restrict__ part,
-                                     const int* __restrict__ skip) {
+                                     const int* __restrict__ skip, const int* __restrict__ skip2) {
   __shared__ double s_du[32], s_r[32];
-  if (skip && *skip) {
-    if (threadIdx.x == 0) part[2 * blockIdx.x] = part[2 * blockIdx.x + 1] = 0.0;
-    return;
-  }
+  const bool hold = (skip && *skip) || (skip2 && *skip2);
   double du2 = 0.0, r2 = 0.0;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P.nmdf; q += (int64_t)gridDim.x * blockDim.x) {
+    r2 += r[q] * r[q];
+    if (hold) continue;
     const double du = -x[q];
     const int node = P.unk_node[q], d = P.unk_dof[q];
     P.cps[(size_t)d * P.numnp + node] += du;
     for (int j = 0; j < 3; ++j)
       if (pp.mmo[j] == d) P.xms[(size_t)j * P.numnp + node] += dt * du;
     du2 += du * du;
-    r2 += r[q] * r[q];
   }
   for (int o = 16; o > 0; o >>= 1) {
     du2 += __shfl_down_sync(0xffffffffu, du2, o);
@@ -248,9 +248,9 @@ void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaSt
 }
 int newton_update_blocks(int64_t nmdf) { return (int)min64(256, (nmdf + 255) / 256); }
 void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
-                          double* part, double* out, cudaStream_t st, const int* skip) {
+                          double* part, double* out, cudaStream_t st, const int* skip, const int* skip2) {
   const int blocks = newton_update_blocks(P.nmdf);
-  newton_update_kernel<<<blocks, 256, 0, st>>>(P, pp, dt, x, r, part, skip);
+  newton_update_kernel<<<blocks, 256, 0, st>>>(P, pp, dt, x, r, part, skip, skip2);
   newton_norm_kernel<<<1, 32, 0, st>>>(part, blocks, P.nmdf, out);
 }
 int band_residual_blocks(int64_t n) { return (int)min64(304, (n + 255) / 256); }

@@ -84,11 +84,11 @@ __device__ __forceinline__ T tabs(T x) { return x < T(0) ? -x : x; }
 // only for column jj+2, after that barrier.
 __device__ __forceinline__ unsigned long long abs_key(double v) {
   unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
-  return b > 0x7ff0000000000000ULL ? 0ULL : b;  // NaN -> 0 (never a valid pivot)
+  return b >= 0x7ff0000000000000ULL ? 0ULL : b;  // NaN, ±Inf -> 0 (never a valid pivot)
 }
 __device__ __forceinline__ unsigned long long abs_key(float v) {
   unsigned b = (unsigned)__float_as_int(v) & 0x7fffffffu;
-  return b > 0x7f800000u ? 0ULL : (unsigned long long)b;
+  return b >= 0x7f800000u ? 0ULL : (unsigned long long)b;
 }
 // 1/x for the pivot: FP32 seed + two Newton steps (no FP64 divide sequence).
 __device__ __forceinline__ double fast_rcp(double x) {

@@ -326,13 +326,16 @@ __global__ void __launch_bounds__(1024) blk_backward_kernel(const T* __restrict_
 // long before it needs them), then solves its U11 triangle and publishes
 // x(q) with a release store of the flag.  Flags hold the epoch of the solve
 // that set them, so they never need clearing.  Waits are bounded: after
-// kSpinLimit polls the kernel records MAFEM status in *err and every CTA
-// returns (no GPU hang; the host reports the error).
+// wt.limit polls (kSpinLimit by default) the kernel records MAFEM status in
+// *err and every CTA returns (no GPU hang; the host reports the error).
+// wt.withhold = k >= 0 (failure-detection tests only): the flag of panel
+// npan - 1 - k is never published, so the CTAs that need it run out of polls
+// and every CTA returns.
 template <class T, class V>
 __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restrict__ ab, BandLayout L, int kuf,
                                                                 const int* __restrict__ ps, int npan,
                                                                 const T* __restrict__ rdiag, V* y, int* flags,
-                                                                int epoch, int* err) {
+                                                                int epoch, int* err, WaitTest wt) {
   __shared__ V part[8][33];
   __shared__ V Us[32][33];
   __shared__ int s_ok;
@@ -349,7 +352,7 @@ __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restr
     while (pl + 1 < npan && ps[pl + 1] < jend) ++pl;
     V acc = V(0);
     for (int p = (j1 < jend) ? pl : q; p > q; --p) {
-      if (!wait_flag(flags, p, epoch, err, &s_ok)) return;
+      if (!wait_flag(flags, p, epoch, err, &s_ok, wt.limit)) return;
       const int64_t cb = ps[p], ce = min64b(ps[p + 1], jend);
       if (lane < w)
         for (int64_t c = cb + warp; c < ce; c += 8) acc += V(ab[bix(L, j0 + lane, c)]) * __ldcg(y + c);
@@ -376,7 +379,7 @@ __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restr
       if (lane < w) __stcg(y + j0 + lane, v);
       __threadfence();
       __syncwarp();
-      if (lane == 0) st_release(flags + q, epoch);
+      if (lane == 0 && npan - 1 - q != wt.withhold) st_release(flags + q, epoch);
     }
     __syncthreads();
   }
@@ -397,7 +400,7 @@ __global__ void __launch_bounds__(256) blk_forward_coop_kernel(const T* __restri
                                                                const int* __restrict__ ps, int npan,
                                                                const int* __restrict__ perm_all,
                                                                const T* __restrict__ rdiag, V* b, V* zbuf,
-                                                               int* flags, int epoch, int* err) {
+                                                               int* flags, int epoch, int* err, WaitTest wt) {
   __shared__ V part[8][33];
   __shared__ V Ls[32][33];
   __shared__ V accs[32];
@@ -414,7 +417,7 @@ __global__ void __launch_bounds__(256) blk_forward_coop_kernel(const T* __restri
     while (pf > 0 && ps[pf] + L.kl > j0) --pf;
     V acc = V(0);
     for (int q = pf; q < p; ++q) {
-      if (!wait_flag(flags, q, epoch, err, &s_ok)) return;
+      if (!wait_flag(flags, q, epoch, err, &s_ok, wt.limit)) return;
       const int64_t q0 = ps[q];
       const int wq = ps[q + 1] - ps[q];
       if (lane < w)
@@ -595,12 +598,12 @@ void blk_forward(const T* ab, const BandLayout& L, const BlkPlan& B, const int* 
 }
 template <class V, class T>
 int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, int* flags, int epoch,
-                 int* err, int grid, cudaStream_t st) {
+                 int* err, int grid, cudaStream_t st, WaitTest wt) {
   const int npan = B.npan();
   int kuf = B.kuf;
   const int* ps = B.d_ps;
   void* args[] = {(void*)&ab, (void*)&L, (void*)&kuf, (void*)&ps, (void*)&npan, (void*)&rdiag, (void*)&y,
-                  (void*)&flags, (void*)&epoch, (void*)&err};
+                  (void*)&flags, (void*)&epoch, (void*)&err, (void*)&wt};
   const cudaError_t e = cudaLaunchCooperativeKernel((const void*)blk_backward_coop_kernel<T, V>,
                                                     dim3(std::min(grid, npan)), dim3(256), args, 0, st);
   return e == cudaSuccess ? 0 : -1;
@@ -613,11 +616,11 @@ void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const
 // cooperative forward substitution; returns 0, or -1 if the launch was refused
 template <class V, class T>
 int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
-                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st) {
+                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st, WaitTest wt) {
   const int npan = B.npan();
   const int* ps = B.d_ps;
   void* args[] = {(void*)&ab,    (void*)&L,    (void*)&ps,    (void*)&npan,  (void*)&perm_all, (void*)&rdiag,
-                  (void*)&b,     (void*)&zbuf, (void*)&flags, (void*)&epoch, (void*)&err};
+                  (void*)&b,     (void*)&zbuf, (void*)&flags, (void*)&epoch, (void*)&err, (void*)&wt};
   const cudaError_t e = cudaLaunchCooperativeKernel((const void*)blk_forward_coop_kernel<T, V>,
                                                     dim3(std::min(grid, npan)), dim3(256), args, 0, st);
   return e == cudaSuccess ? 0 : -1;
@@ -643,9 +646,9 @@ template void blk_forward<double, double>(const double*, const BandLayout&, cons
 template void blk_forward<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*, const float*,
                                          double*, cudaStream_t);
 template int blk_backward<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*, double*,
-                                          int*, int, int*, int, cudaStream_t);
+                                          int*, int, int*, int, cudaStream_t, WaitTest);
 template int blk_backward<double, float>(const float*, const BandLayout&, const BlkPlan&, const float*, double*, int*,
-                                         int, int*, int, cudaStream_t);
+                                         int, int*, int, cudaStream_t, WaitTest);
 template void blk_backward_1cta<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*,
                                                 double*, cudaStream_t);
 template void blk_backward_1cta<double, float>(const float*, const BandLayout&, const BlkPlan&, const float*, double*,
@@ -653,8 +656,9 @@ template void blk_backward_1cta<double, float>(const float*, const BandLayout&, 
 template int blk_backward_grid<double, double>();
 template int blk_backward_grid<double, float>();
 template int blk_forward_coop<double, double>(const double*, const BandLayout&, const BlkPlan&, const int*,
-                                              const double*, double*, double*, int*, int, int*, int, cudaStream_t);
+                                              const double*, double*, double*, int*, int, int*, int, cudaStream_t,
+                                              WaitTest);
 template int blk_forward_coop<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*, const float*,
-                                             double*, double*, int*, int, int*, int, cudaStream_t);
+                                             double*, double*, int*, int, int*, int, cudaStream_t, WaitTest);
 
 }  // namespace mafem

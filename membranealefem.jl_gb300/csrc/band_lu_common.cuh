@@ -124,12 +124,14 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-// thread 0 waits for flags[p] == epoch; returns false (all threads) on timeout / abort
-__device__ __forceinline__ bool wait_flag(const int* flags, int p, int epoch, int* err, int* s_ok) {
+// thread 0 waits for flags[p] == epoch; returns false (all threads) after
+// `limit` polls (kSpinLimit when limit <= 0) or when another CTA has set *err
+__device__ __forceinline__ bool wait_flag(const int* flags, int p, int epoch, int* err, int* s_ok, int limit = 0) {
   if (threadIdx.x == 0) {
+    const int lim = limit > 0 ? limit : kSpinLimit;
     int ok = 1;
     for (int it = 0; ld_acquire(flags + p) != epoch; ++it) {
-      if (it > kSpinLimit || *(volatile int*)err) {
+      if (it > lim || *(volatile int*)err) {
         atomicCAS(err, 0, 1);
         ok = 0;
         break;

@@ -31,7 +31,8 @@
 // nq = 9*ndf threads each; the element's tangent columns accumulate in shared
 // memory ([row][q], conflict-free) and are written once, column-major, to a
 // staging buffer K_el[e][q][row].  A second kernel gathers, for every band
-// entry, the <= 4 element contributions that land on it (no atomics: each
+// entry, the <= 9 element contributions that land on it (a biquadratic node
+// lies in up to 3 x 3 elements; no atomics: each
 // output is written by exactly one thread), zero-filling the rest of the band.
 
 #include <cuda_runtime.h>

@@ -124,7 +124,8 @@ void launch_resid_gather(const DevPatch& P, int ndf, int nq, const double* r_el,
 void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaStream_t st);
 int newton_update_blocks(int64_t nmdf);
 void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
-                          double* part, double* out, cudaStream_t st, const int* skip = nullptr);
+                          double* part, double* out, cudaStream_t st, const int* skip = nullptr,
+                          const int* skip2 = nullptr);
 int band_residual_blocks(int64_t n);
 template <class T>
 void launch_band_residual(const T* a0, const BandLayout& L, const double* x, const double* r, double* res,
@@ -179,9 +180,16 @@ void blk_forward(const T* ab, const BandLayout& L, const BlkPlan& B, const int* 
 // `grid` CTAs, grid <= blk_backward_grid()).  flags: npan ints, epoch: a value
 // they do not hold yet (incremented per call); err: nonzero after a bounded
 // wait ran out.  Returns -1 if the launch failed.
+// Failure-detection test hook of the cooperative substitutions: limit = polls
+// before a wait gives up (<= 0: the default), withhold = k: the back
+// substitution never publishes the flag of panel npan - 1 - k (-1: none).
+struct WaitTest {
+  int limit = 0;
+  int withhold = -1;
+};
 template <class V, class T>
 int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, int* flags, int epoch,
-                 int* err, int grid, cudaStream_t st);
+                 int* err, int grid, cudaStream_t st, WaitTest wt = WaitTest());
 template <class V, class T>
 int blk_backward_grid();
 // Forward substitution (P, L11, A21 of the stored panels) on `grid` CTAs of one
@@ -189,7 +197,7 @@ int blk_backward_grid();
 // for blk_backward.  Returns 0, or -1 if the cooperative launch was refused.
 template <class V, class T>
 int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
-                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st);
+                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st, WaitTest wt = WaitTest());
 // Persistent cooperative factorisation (band_lu_persist.cu): launch shape and
 // per-panel flags.  Flags are zeroed once; epochs make them reusable.
 struct BlkPersist {

@@ -20,15 +20,17 @@
 //  - It keeps whatever the previous call left.  Every call rewrites the whole
 //    padded band (zeros outside the caller's band) and clears the pivot flag
 //    before use, so nothing stale is read.
-//  - The device address of the array is looked up once per device, with that
-//    device current, on the first call made on it (cudaGetSymbolAddress); make
-//    that first call before any stream capture.
+//  - Every call looks up the array's device address on the current device
+//    (cudaGetSymbolAddress, which allocates nothing), so a device or context
+//    reset between calls cannot leave a stale address behind.
 //  - Systems whose working set does not fit are rejected with MAFEM_ERR_ARG.
+//  - A zero, infinite or NaN pivot gives MAFEM_ZERO_PIVOT; a non-finite entry
+//    of x (a NaN or Inf in the band that never became a pivot) gives
+//    MAFEM_NAN_DETECTED.
 
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#include <mutex>
 #include <string>
 
 #include "mafem.h"
@@ -42,9 +44,13 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void* g_scratch_ptr[kMaxDevices] = {};  // device address of g_noalloc_scratch, per device
+// Sets *flag when x holds a NaN or an infinity.
+__global__ void nonfinite_kernel(const double* __restrict__ x, int64_t n, int* __restrict__ flag) {
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    bad |= !isfinite(x[i]);
+  if (__syncthreads_or(bad) && threadIdx.x == 0) atomicExch(flag, 1);
+}
 
 // LAPACK band (A(i,j) at band[j*ldab + kl+ku+i-j]) -> the factorisation's padded
 // layout; every stored entry of every column is written (zero outside the band).
@@ -80,6 +86,10 @@ extern "C" int mafem_band_solve_noalloc(const double* band_dev, int64_t n, int64
     set_global_error("mafem_band_solve_noalloc: bad arguments (kl must equal ku, ldab >= 2kl+ku+1)");
     return MAFEM_ERR_ARG;
   }
+  if (kl > 4096 || n > ((int64_t)1 << 40)) {  // before any narrowing: far beyond what the scratch holds
+    set_global_error("mafem_band_solve_noalloc: half bandwidth or size too large");
+    return MAFEM_ERR_ARG;
+  }
   const int nb = pick_nb((int)kl);
   if (!nb) {
     set_global_error("mafem_band_solve_noalloc: half bandwidth too large");
@@ -93,38 +103,21 @@ extern "C" int mafem_band_solve_noalloc(const double* band_dev, int64_t n, int64
   const size_t perm_bytes = (size_t)npan * rmax * sizeof(int);
   const size_t ipiv_off = (perm_off + perm_bytes + 255) / 256 * 256;
   const size_t info_off = (ipiv_off + (size_t)n * sizeof(int) + 255) / 256 * 256;
-  const size_t need = info_off + 256;
+  const size_t need = info_off + 256;  // info[0]: zero-pivot column, info[1]: non-finite x
   if (need > kNoAllocScratchBytes) {
     set_global_error("mafem_band_solve_noalloc: needs " + std::to_string(need) + " bytes of scratch, the limit is " +
                      std::to_string(kNoAllocScratchBytes) + " (reduce n or the bandwidth, or use mafem_solve)");
     return MAFEM_ERR_ARG;
   }
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-    set_global_error("mafem_band_solve_noalloc: no usable current device");
+  // the array's address on the current device, looked up on every call
+  void* base = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+  if (e != cudaSuccess || !base) {
+    set_global_error(std::string("mafem_band_solve_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     return MAFEM_ERR_CUDA;
   }
-  void* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {  // one-time set-up on this device (it is current here)
-      void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        set_global_error(std::string("mafem_band_solve_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        return MAFEM_ERR_CUDA;
-      }
-      e = band_lu_setup<double>(L, 256);
-      if (e != cudaSuccess) {
-        set_global_error(std::string("mafem_band_solve_noalloc: kernel set-up: ") + cudaGetErrorString(e));
-        return MAFEM_ERR_CUDA;
-      }
-      g_scratch_ptr[dev] = p;
-    }
-    base = g_scratch_ptr[dev];
-  }
-  // dynamic shared-memory limits depend on kl; re-apply for this size (no allocation)
-  cudaError_t e = band_lu_setup<double>(L, 256);
+  // dynamic shared-memory limits depend on kl; set them for this size (no allocation)
+  e = band_lu_setup<double>(L, 256);
   if (e != cudaSuccess) {
     set_global_error(std::string("mafem_band_solve_noalloc: kernel set-up: ") + cudaGetErrorString(e));
     return MAFEM_ERR_CUDA;
@@ -137,7 +130,7 @@ extern "C" int mafem_band_solve_noalloc(const double* band_dev, int64_t n, int64
   int* info = reinterpret_cast<int*>(sb + info_off);
   dim3 grid((unsigned)((L.ldb + 255) / 256), (unsigned)(n < 65535 ? n : 65535));
   lapack_to_padded_kernel<<<grid, 256, 0, st>>>(band_dev, ldab, L, ab);
-  if ((e = cudaMemsetAsync(info, 0, sizeof(int), st)) != cudaSuccess ||
+  if ((e = cudaMemsetAsync(info, 0, 2 * sizeof(int), st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(x_dev, rhs_dev, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, st)) != cudaSuccess) {
     set_global_error(std::string("mafem_band_solve_noalloc: ") + cudaGetErrorString(e));
     return MAFEM_ERR_CUDA;
@@ -149,16 +142,21 @@ extern "C" int mafem_band_solve_noalloc(const double* band_dev, int64_t n, int64
     return MAFEM_ERR_CUDA;
   }
   band_backward<double, double>(ab, L, x_dev, st);
-  int h_info = 0;
+  nonfinite_kernel<<<(unsigned)(n < 152 * 256 ? (n + 255) / 256 : 152), 256, 0, st>>>(x_dev, n, info + 1);
+  int h_info[2] = {0, 0};
   if ((e = cudaGetLastError()) != cudaSuccess ||
-      (e = cudaMemcpyAsync(&h_info, info, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(h_info, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess) {
     set_global_error(std::string("mafem_band_solve_noalloc: ") + cudaGetErrorString(e));
     return MAFEM_ERR_CUDA;
   }
-  if (h_info) {
-    set_global_error("mafem_band_solve_noalloc: zero or non-finite pivot in column " + std::to_string(h_info));
+  if (h_info[0]) {
+    set_global_error("mafem_band_solve_noalloc: zero or non-finite pivot in column " + std::to_string(h_info[0]));
     return MAFEM_ZERO_PIVOT;
+  }
+  if (h_info[1]) {
+    set_global_error("mafem_band_solve_noalloc: the solution holds a NaN or an infinity");
+    return MAFEM_NAN_DETECTED;
   }
   return MAFEM_OK;
 }

@@ -166,6 +166,10 @@ def lib():
         L.mafem_launch_count.restype = C.c_int64
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
         L.mafem_set_refinement.argtypes = [vp, C.c_int32, C.c_double]
+        L.mafem_set_wait_test.argtypes = [vp, C.c_int32, C.c_int32]
+        L.mafem_solve_band.argtypes = [vp, _PD, C.c_int64, _PD, _PD]
+        L.mafem_fallback_count.argtypes = [vp]
+        L.mafem_fallback_count.restype = C.c_int64
         L.mafem_trace_patch_solve.argtypes = [vp, C.c_double, C.c_double, C.POINTER(C.c_int64), C.c_int64]
         L.mafem_pull_force.argtypes = [vp, _PD]
         L.mafem_pull_position.argtypes = [vp, _PD]
@@ -480,6 +484,25 @@ class Solver:
         self.last_refine_trace = a[6 * npan + 2: 6 * npan + 130].reshape(32, 4)
         self.last_solve_phases = a[6 * npan + 130:]
         return a[: 6 * npan].reshape(npan, 6), a[6 * npan] / 1e6, a[6 * npan + 1] / 1e6
+
+    def solve_band(self, band, rhs):
+        """x with K x = rhs for a caller's band K (LAPACK layout of calc_r_K's band,
+        ldab >= 3 kl + 1) through this handle's factorisation and solves."""
+        band = np.ascontiguousarray(band, dtype=np.float64)  # row j = band column j
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        x = np.zeros(self.nmdf)
+        _raise(lib().mafem_solve_band(self.h, _dp(band), band.shape[1], _dp(rhs), _dp(x)), self.h)
+        return x
+
+    def fallback_count(self) -> int:
+        """Factorisations redone with full partial pivoting so far."""
+        return int(lib().mafem_fallback_count(self.h))
+
+    def set_wait_test(self, limit_polls: int = 0, withhold_panel: int = -1) -> None:
+        """Failure-detection test hook (mafem_set_wait_test): bounded inter-CTA waits
+        give up after limit_polls polls; the back substitution withholds the flag of
+        the panel withhold_panel places before the last.  (0, -1) restores the default."""
+        _raise(lib().mafem_set_wait_test(self.h, limit_polls, withhold_panel), self.h)
 
     def set_lu_path(self, path: int) -> None:
         """Select the banded LU: LU_AUTO (default), LU_PANELS or LU_FULL."""
