@@ -269,15 +269,19 @@ def run_gb300(args, rank, world, local, dist):
     return out
 
 
-# The batched form on a mixed set of patches.  Sizes stop at 32: from the flat
-# start with the reference's velocity-controlled pull, every 48x48 patch of this
-# mix loses Newton convergence on its first step (with full partial pivoting as
-# well as node-block pivoting), as do some 32x32 ALE patches with kb > 1.25 at
-# dt 0.01; dt 0.005 and half the pull speed keep the rest converging.  A patch
-# that still fails when stepped alone is left out of both measurements (counted).
-BATCH = dict(name="mixed batch: 256 independent tether-pull patches, n in {8,12,16,24,32} (seed 1), "
-                  "half LAG / half ALEVB, kb log-uniform [0.5, 2], pull speed 0.01 f/6 with f ~ U[2, 10], dt 0.005",
-             patches=256, sizes=(8, 12, 16, 24, 32), seed=1, dt=0.005)
+# The batching workload: 256 independent tether pulls of mixed sizes and
+# parameters.  Two F_PULL extensions make it the workload as stated: lambda0
+# (the tension drawn per patch instead of the reference's fixed kb / 4) and the
+# centre pull element (every size is even, and the reference's ceil(numel / 2)
+# would pull at the right edge).  The reference's pull is velocity-driven
+# (Bc.jl:227-243); the stated pull force f sets the pulling speed, f times
+# PULL_SPEED_PER_FORCE, and the reaction force the patches reach is measured
+# (calc_pull_force) and reported beside it.
+PULL_SPEED_PER_FORCE = 0.01
+BATCH = dict(name="batching workload: 256 independent tether-pull patches, n ~ U{8,12,16,24,32,48} elements per "
+                  "side (seed 1), kb log-U[0.5, 2], lambda0 log-U[0.1, 10], pull force f ~ U[2, 10] driving the pull "
+                  "at speed 0.01 f, half LAG / half ALEVB, centre pull element, dt 0.01",
+             patches=256, sizes=(8, 12, 16, 24, 32, 48), seed=1, dt=0.01, steps=30)
 
 
 def batch_patches(M, wl=BATCH):
@@ -287,13 +291,13 @@ def batch_patches(M, wl=BATCH):
     for k in range(wl["patches"]):
         n = int(rng.choice(wl["sizes"]))
         kb = float(np.exp(rng.uniform(np.log(0.5), np.log(2.0))))
+        lam0 = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
         f = float(rng.uniform(2.0, 10.0))
         motion = M.LAG if k % 2 == 0 else M.ALEVB
-        p = M.Params(motion=motion, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, kb=kb,
-                     pull_speed=0.01 * f / 6.0)
+        p = M.Params(motion=motion, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, kb=kb, lambda0=lam0,
+                     pull_centre=1, pull_speed=PULL_SPEED_PER_FORCE * f)
         mesh = M.Mesh(p)
-        _, xms, cps = M.prepare_input(p, mesh)
-        M.perturb_interior_z(mesh, xms, seed=k, amp=1e-4)
+        _, xms, cps = M.prepare_input(p, mesh)  # flat start: the workload states no perturbation
         out.append((p, mesh, xms, cps))
     return out
 
@@ -322,101 +326,77 @@ def _relmax(a, b):
     return float(np.abs(a - b).max() / max(float(np.abs(b).max()), 1e-300))
 
 
-def run_batched(steps, warmup, wl=BATCH):
-    """The same patches (a) one at a time through the plain FP64 path, each
-    factorisation on all SMs, (b) as one plain FP64 batch (mafem_batch_step,
-    each patch's factorisation on its smallest grid), and (c) as one batch of
-    the FP32 form (FP32 tangent, batched one-CTA-per-patch FP32 LU, FP64
-    refinement) -- the headline, with its error against (a).  Host wall clock
-    around the steps, device synchronised on both sides; patch time-steps/s.
-    Patches that fail to converge when stepped alone are left out of all three."""
+def run_batched(steps=None, wl=BATCH):
+    """The batching workload, every patch for `steps` time steps (the
+    workload's 30 by default) from the same seeded initial states:
+    (a) plain FP64, one patch after another, each factorisation on all SMs --
+        the baseline of the ratio;
+    (b) the FP32 form batched (mafem_batch_step: FP32 tangent, the batched
+        one-patch-per-CTA / per-cluster FP32 LU with the tensor-core trailing
+        update, FP64 refinement) -- the headline, with its largest relative
+        error against (a) and the p50 / p99 of the batch-step latency;
+    (c) the same FP32 form under continuous batching (mafem_server), every
+        patch advancing through its steps on its own.
+    Host wall clock around the steps, device synchronised on both sides;
+    patch time-steps/s.  No patch is left out: a failed patch-step is counted."""
     import mafem as M
     cu = Cudart()
+    steps = steps or wl["steps"]
     patches = batch_patches(M, wl)
-    solvers = [M.Solver(mesh, p, M.PLAIN_FP64) for p, mesh, _, _ in patches]
     dt = wl["dt"]
-    try:
-        # (a) one at a time
-        seq_ms, ok = 0.0, []
-        for i, (s, (p, mesh, x0, c0)) in enumerate(zip(solvers, patches)):
+    # (a) plain FP64, one at a time
+    seq_ms, seq_state, seq_fail = 0.0, [], 0
+    for p, mesh, x0, c0 in patches:
+        with M.Solver(mesh, p, M.PLAIN_FP64) as s:
             s.set_launch_ctas(0)
             s.upload(x0, c0)
-            t, lat = 0.0, []
-            try:
-                for k in range(warmup + steps):
-                    t += dt
-                    cu.sync()
-                    h0 = time.perf_counter()
-                    s.predict(dt)
-                    s.time_step_resident(t, dt)
-                    cu.sync()
-                    if k >= warmup:
-                        lat.append((time.perf_counter() - h0) * 1e3)
-            except M.NewtonNotConverged:
-                continue
-            seq_ms += sum(lat)
-            ok.append(i)
-        seq_state = {i: solvers[i].download() for i in ok}
-        # (b) batched, from the same initial states
-        bsolvers = [solvers[i] for i in ok]
-        for i in ok:
-            solvers[i].upload(patches[i][2], patches[i][3])
-        with M.Batch(bsolvers) as b:
-            t, bat_lat, fails = 0.0, [], 0
-            for k in range(warmup + steps):
+            t = 0.0
+            cu.sync()
+            h0 = time.perf_counter()
+            for _ in range(steps):
                 t += dt
-                cu.sync()
-                h0 = time.perf_counter()
-                status, _ = b.step(t, dt)
-                cu.sync()
-                fails += sum(1 for x in status if x != M.OK)
-                if k >= warmup:
-                    bat_lat.append((time.perf_counter() - h0) * 1e3)
-        err = 0.0
-        for i in ok:
-            xs, cs = seq_state[i]
-            xb, cb = solvers[i].download()
-            err = max(err, _relmax(xb, xs), _relmax(cb, cs))
-    finally:
-        for s in solvers:
-            s.close()
-    # (c) the FP32 form batched: FP32 tangent, one-CTA-per-patch FP32 LU and
-    # FP64 refinement (mafem_batch_step's batched solve), refinement to 1e-4
-    # relative per linear solve -- Newton's FP64 criterion decides convergence
-    fsolvers = [M.Solver(patches[i][1], patches[i][0], M.FP32_REFINE) for i in ok]
+                s.predict(dt)
+                try:
+                    s.time_step_resident(t, dt)
+                except M.NewtonNotConverged:
+                    seq_fail += 1
+            cu.sync()
+            seq_ms += (time.perf_counter() - h0) * 1e3
+            seq_state.append(s.download())
+    # (b) the FP32 form batched, refinement to FP32_REFINE_TOL per linear solve
+    # (Newton's FP64 criterion decides convergence)
+    fsolvers = [M.Solver(mesh, p, M.FP32_REFINE) for p, mesh, _, _ in patches]
     try:
-        for s, i in zip(fsolvers, ok):
-            s.upload(patches[i][2], patches[i][3])
+        for s, (_, _, x0, c0) in zip(fsolvers, patches):
+            s.upload(x0, c0)
             s.set_refinement(30, FP32_REFINE_TOL)
         with M.Batch(fsolvers) as b:
             t, f_lat, f_fails, f_iters, f_sweeps = 0.0, [], 0, 0, 0
-            for k in range(warmup + steps):
+            for k in range(steps):
                 t += dt
                 cu.sync()
                 h0 = time.perf_counter()
                 status, st = b.step(t, dt)
                 cu.sync()
+                f_lat.append((time.perf_counter() - h0) * 1e3)
                 f_fails += sum(1 for x in status if x != M.OK)
-                if k >= warmup:
-                    f_lat.append((time.perf_counter() - h0) * 1e3)
-                    f_iters += sum(x["newton_iters"] for x in st)
-                    f_sweeps += sum(x["refine_iters"] for x in st)
-        f_err = 0.0
-        for s, i in zip(fsolvers, ok):
-            xs, cs = seq_state[i]
+                f_iters += sum(x["newton_iters"] for x in st)
+                f_sweeps += sum(x["refine_iters"] for x in st)
+        f_err, forces = 0.0, []
+        for s, (xs, cs) in zip(fsolvers, seq_state):
             xf, cf = s.download()
             f_err = max(f_err, _relmax(xf, xs), _relmax(cf, cs))
+            forces.append(float(s.pull_force()[2]))
     finally:
         for s in fsolvers:
             s.close()
-    # (d) the same FP32 form under continuous batching (mafem_server): every
-    # patch advances through its steps on its own, no barrier between steps
+    # (c) continuous batching of the same FP32 solves
     with M.Server() as srv:
-        ids = [srv.submit(patches[i][1], patches[i][0], patches[i][2], patches[i][3], warmup + steps, dt,
-                          precision=M.FP32_REFINE, refine_tol=FP32_REFINE_TOL) for i in ok]
+        ids = [srv.submit(mesh, p, x0, c0, steps, dt, precision=M.FP32_REFINE, refine_tol=FP32_REFINE_TOL)
+               for p, mesh, x0, c0 in patches]
         cu.sync()
         h0 = time.perf_counter()
-        got, c_err, c_fail = {}, 0.0, 0
+        got = {}
         while len(got) < len(ids):
             srv.round()
             for k, rid in enumerate(ids):
@@ -427,47 +407,38 @@ def run_batched(steps, warmup, wl=BATCH):
         cu.sync()
         c_wall = time.perf_counter() - h0
         c_stats = srv.stats()
-    for k, i in enumerate(ok):
+    c_err, c_fail = 0.0, 0
+    for k, (xs, cs) in enumerate(seq_state):
         stt, xc, cc = got[k]
         c_fail += stt != M.OK
-        xs, cs = seq_state[i]
         c_err = max(c_err, _relmax(xc, xs), _relmax(cc, cs))
-    n = len(ok)
-    bat_ms = sum(bat_lat)
-    lat = sorted(bat_lat)
+    n = len(patches)
     f_ms = sum(f_lat)
     flat = sorted(f_lat)
 
     def pct(a, q):
         return a[min(len(a) - 1, int(q * len(a)))]
     sizes = {}
-    for i in ok:
-        sizes[patches[i][0].num1el] = sizes.get(patches[i][0].num1el, 0) + 1
-    return {"workload": wl["name"], "patches": n, "patches_left_out_not_converging": len(patches) - n,
-            "steps": steps, "warmup": warmup,
+    for p, _, _, _ in patches:
+        sizes[p.num1el] = sizes.get(p.num1el, 0) + 1
+    fz = np.array(forces)
+    return {"workload": wl["name"], "patches": n, "steps": steps,
             "value": n * steps / (f_ms / 1e3), "unit": "patch time-steps/s",
-            "form": "FP32 tangent + batched one-CTA-per-patch FP32 LU + FP64 refinement (tol %g per solve), "
-                    "mafem_batch_step; host wall clock around each batch step" % FP32_REFINE_TOL,
+            "form": "FP32 tangent + batched FP32 LU (tcgen05 3xTF32 trailing update) + FP64 refinement to %g per "
+                    "solve, mafem_batch_step" % FP32_REFINE_TOL,
             "speedup_vs_plain_fp64_one_at_a_time": seq_ms / f_ms,
             "p50_batch_step_ms": pct(flat, 0.5), "p99_batch_step_ms": pct(flat, 0.99),
             "max_rel_err_vs_plain_fp64": f_err, "failed_patch_steps": f_fails,
             "newton_iters_per_patch_step": f_iters / (n * steps), "refine_sweeps_per_patch_step": f_sweeps / (n * steps),
             "one_at_a_time": {"value": n * steps / (seq_ms / 1e3), "unit": "patch time-steps/s",
-                              "form": "plain FP64, patches stepped one after another, all SMs each"},
-            "plain_fp64_batched": {"value": n * steps / (bat_ms / 1e3), "unit": "patch time-steps/s",
-                                   "speedup_vs_one_at_a_time": seq_ms / bat_ms,
-                                   "p50_batch_step_ms": pct(lat, 0.5), "p99_batch_step_ms": pct(lat, 0.99),
-                                   "max_rel_diff_vs_one_at_a_time": err, "failed_patch_steps": fails,
-                                   "form": "plain FP64, mafem_batch_step: every patch's Newton iteration enqueued "
-                                           "on its own stream before any is waited for"},
-            "continuous": {"value": n * (warmup + steps) / c_wall, "unit": "patch time-steps/s",
-                           "speedup_vs_plain_fp64_one_at_a_time": (n * (warmup + steps) / c_wall)
-                           / (n * steps / (seq_ms / 1e3)),
+                              "failed_patch_steps": seq_fail, "form": "plain FP64, one patch after another"},
+            "continuous": {"value": n * steps / c_wall, "unit": "patch time-steps/s",
+                           "speedup_vs_plain_fp64_one_at_a_time": (n * steps / c_wall) / (n * steps / (seq_ms / 1e3)),
                            "p50_step_ms": c_stats["p50_step_ms"], "p99_step_ms": c_stats["p99_step_ms"],
                            "max_rel_err_vs_plain_fp64": c_err, "failed_patches": c_fail,
-                           "form": "the FP32 form under continuous batching (mafem_server): all patches "
-                                   "submitted at once, each advancing %d steps on its own; wall clock from the "
-                                   "first round to the last result" % (warmup + steps)},
+                           "form": "the FP32 form under continuous batching (mafem_server), all patches submitted "
+                                   "at once"},
+            "pull_force_z_after": {"min": float(fz.min()), "median": float(np.median(fz)), "max": float(fz.max())},
             "size_histogram": {str(k): v for k, v in sorted(sizes.items())}}
 
 
@@ -684,7 +655,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
-    ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--batch-steps", type=int, default=0, help="time steps of the batching workload (0: its 30)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--case", choices=["fp32-patch32", "fp32-batch16"],
                     help="run a small profiling case instead of the bench (prints no bench line)")
@@ -760,7 +731,7 @@ def main():
         "mesh": r["mesh"],
     }
     if rank == 0 and not args.no_batch:
-        line["batched"] = run_batched(args.batch_steps, 1)
+        line["batched"] = run_batched(args.batch_steps)
     if rank == 0 and not args.no_serve:
         line["serving"] = run_serving()
     if rank == 0 and not args.no_cpu_baseline:

@@ -128,6 +128,8 @@ struct mafem_handle {
   PatchJob job{};
   WaitTest wait_test;                   // mafem_set_wait_test (failure-detection tests)
   const double* host_band = nullptr;    // mafem_solve_band: the caller's band (padded layout), for the fallback
+  int* d_rstate = nullptr;              // refinement state {done, sweeps, status} (FP32 form)
+  int* h_rstate = nullptr;              // its pinned host copy
   std::unique_ptr<StateWriter> writer;  // state files, created by the first write
   double* d_snap = nullptr;             // device snapshots: nsnap x [xms | cps]
   int nsnap = 0;
@@ -504,6 +506,7 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
   AL(h->d_out, 16);
   AL(h->d_ipiv, n);
   AL(h->d_perm, std::max((size_t)h->npan * h->rmax, (size_t)h->blk.npan() * kBlkW));
+  AL(h->d_rstate, 4);
   AL(h->d_info, 4);  // [0] zero-pivot column (1-based), [1] nonzero: a bounded device wait ran out
   cudaMemset(h->d_info, 0, 4 * sizeof(int));
   const size_t band_elems = (size_t)h->L.ldb * n;
@@ -526,7 +529,8 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     h->d_band0 = band0;
     h->d_rdiag = rd;
   }
-  ce = cudaMallocHost(&h->h_out, 16 * sizeof(double));
+  ce = cudaMallocHost(&h->h_out, 20 * sizeof(double));
+  if (ce == cudaSuccess) h->h_rstate = reinterpret_cast<int*>(h->h_out + 16);
   if (ce != cudaSuccess) {
     set_global_error("cudaMallocHost failed");
     mafem_destroy(hp.release());
@@ -540,6 +544,8 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
     if (dyn > 0 && patch_factor_smem(h->L.kl) <= (size_t)dyn && patch_refine_smem(n) <= (size_t)dyn) {
       AL(h->d_inv, (size_t)h->blk.npan() * 2 * kBlkW * kBlkW);
       PatchJob& J = h->job;
+      J.a21_rows = patch_a21_rows(h->L.kl);
+      AL(J.a21, (size_t)8 * 2 * J.a21_rows * 4);
       J.band = (float*)h->d_band;
       J.band0 = (const float*)h->d_band0;
       J.inv = h->d_inv;
@@ -556,7 +562,7 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
       J.L = h->L;
       J.kuf = h->blk.kuf;
       J.npan = h->blk.npan();
-      h->patch_ok = true;
+      h->patch_ok = patch_a21_map(J);
     }
   }
   DevPatch& P = h->P;
@@ -741,16 +747,25 @@ static int factor(mafem_handle* h, double* x, const double* rhs0) {
   h->launches += nl;
   h->factored = true;
   h->last_blk = false;
+  // full partial pivoting found no usable pivot either: the matrix is singular
+  // (or not finite); report it before any solve uses the factors
+  int zp = 0;
+  CK(cudaMemcpyAsync(&zp, h->d_info, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (zp) {
+    h->err = "zero pivot in column " + std::to_string(zp);
+    return MAFEM_ZERO_PIVOT;
+  }
   return MAFEM_OK;
 }
 
 // Back substitution with the node-block factors, in place on y (device).
 template <class T>
-static void blk_back_solve(mafem_handle* h, double* y) {
+static void blk_back_solve(mafem_handle* h, double* y, const int* gate = nullptr) {
   if (h->bwd_grid > 0) {
     ++h->epoch;
     if (blk_backward<double, T>((const T*)h->d_band, h->L, h->blk, (const T*)h->d_rdiag, y, h->d_flags, h->epoch,
-                                h->d_info + 1, h->bwd_grid, h->st, h->wait_test) == 0) {
+                                h->d_info + 1, h->bwd_grid, h->st, h->wait_test, gate) == 0) {
       h->launches += 1;
       return;
     }
@@ -764,11 +779,12 @@ static void blk_back_solve(mafem_handle* h, double* y) {
 // Forward substitution with the node-block factors, in place on y (device):
 // the cooperative multi-CTA kernel where the device allows it.
 template <class T>
-static void blk_fwd_solve(mafem_handle* h, double* y) {
+static void blk_fwd_solve(mafem_handle* h, double* y, const int* gate = nullptr) {
   if (h->bwd_grid > 0) {
     ++h->epoch;
     if (blk_forward_coop<double, T>((const T*)h->d_band, h->L, h->blk, h->d_perm, (const T*)h->d_rdiag, y, h->d_zbuf,
-                                    h->d_flags, h->epoch, h->d_info + 1, h->bwd_grid, h->st, h->wait_test) == 0) {
+                                    h->d_flags, h->epoch, h->d_info + 1, h->bwd_grid, h->st, h->wait_test,
+                                    gate) == 0) {
       h->launches += 1;
       return;
     }
@@ -826,56 +842,57 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
     if (rc) return rc;
   }
   cudaEventRecord(h->ev[2], h->st);
+  // The sweeps run on the device with a device-side stopping test: every sweep
+  // (d = LU^-1 res, x += d, res = rhs - A0 x in FP64) ends with a check kernel
+  // that sets the handle's refinement state {done, sweeps, status}; the
+  // kernels of later sweeps see `done` and return at once.  Sweeps are
+  // enqueued kRefineChunk at a time and the host reads the state once per
+  // chunk -- one wait where the solve stops within a chunk -- instead of once
+  // per sweep.  The stopping rule: |rhs - A0 x| <= tol |rhs| (this solver is
+  // also the fallback of the batched solve when that one stalls on an
+  // ill-conditioned tangent, where a small correction says nothing about the
+  // error of x); stall after the fourth sweep if |r| > |r_prev| / 2.
+  constexpr int kRefineChunk = 3;
+  int* gate = h->d_rstate;
   CK(cudaMemsetAsync(h->d_x, 0, n * sizeof(double), h->st));
-  CK(cudaMemcpyAsync(h->d_res, rhs_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-  // ‖rhs‖
   launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part, h->d_out + 4,
-                              h->st);
-  h->launches += 2;
-  CK(cudaMemcpyAsync(h->h_out + 4, h->d_out + 4, sizeof(double), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  const double r0 = h->h_out[4];
-  if (!(r0 > 0.0)) return MAFEM_OK;
-  // stop when the residual has dropped by tol.  This solver is also the
-  // fallback of the batched solve when that one stalls on an ill-conditioned
-  // tangent (FP32 LU contraction near 1, where a small correction says nothing
-  // about the error of x): the residual test still lets Newton, which checks
-  // the FP64 residual itself, proceed.  |dx| and |x| are formed for the stats.
-  double prev = r0;
-  for (int k = 0; k < h->max_refine; ++k) {
-    CK(cudaMemcpyAsync(h->d_dx, h->d_res, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
-    if (h->last_blk) {
-      blk_fwd_solve<float>(h, h->d_dx);
-      blk_back_solve<float>(h, h->d_dx);
-    } else {
-      band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
-      band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
-      h->launches += 2;
+                              h->st);  // res = rhs, |rhs|
+  launch_refine_init(h->d_out + 4, gate, h->d_out + 12, h->st);
+  h->launches += 3;
+  int state[3] = {0, 0, MAFEM_OK};
+  for (int chunk = 0; !state[0]; ++chunk) {
+    for (int k = 0; k < kRefineChunk; ++k) {
+      launch_copy_gated(n, h->d_res, h->d_dx, gate, h->st);
+      if (h->last_blk) {
+        blk_fwd_solve<float>(h, h->d_dx, gate);
+        blk_back_solve<float>(h, h->d_dx, gate);
+      } else {  // full partial pivoting: single-CTA substitutions (ungated: they only rewrite d_dx)
+        band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
+        band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
+        h->launches += 2;
+      }
+      launch_axpy_norms(n, h->d_dx, h->d_x, h->d_part, h->d_out + 8, h->st, gate);
+      launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part,
+                                  h->d_out + 3, h->st, gate);
+      launch_refine_check(h->d_out + 3, h->d_out + 8, gate, h->d_out + 12, h->refine_tol, h->max_refine, h->st);
+      h->launches += 6;
     }
-    launch_axpy_norms(n, h->d_dx, h->d_x, h->d_part, h->d_out + 8, h->st);
-    launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part,
-                                h->d_out + 3, h->st);
-    h->launches += 4;
-    CK(cudaMemcpyAsync(h->h_out + 3, h->d_out + 3, sizeof(double), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaMemcpyAsync(h->h_out + 8, h->d_out + 8, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h->h_rstate, gate, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
-    *sweeps = k + 1;
-    const double rn = h->h_out[3], dn = h->h_out[8], xn = h->h_out[9];
-    if (!std::isfinite(rn) || !std::isfinite(dn) || !std::isfinite(xn)) {
-      h->err = "non-finite refinement residual or correction";
-      return MAFEM_NAN_DETECTED;
-    }
-    (void)dn;
-    (void)xn;
-    if (rn <= h->refine_tol * r0) return MAFEM_OK;
-    if (rn > 0.5 * prev && k >= 3) {
-      h->err = "iterative refinement stalled at relative residual " + std::to_string(rn / r0);
-      return MAFEM_REFINE_STALLED;
-    }
-    prev = rn;
+    std::memcpy(state, h->h_rstate, sizeof state);
+    if (!state[0] && state[1] >= h->max_refine) break;  // cannot happen: the check stops at max_sweeps
   }
-  h->err = "iterative refinement did not reach its tolerance";
-  return MAFEM_REFINE_STALLED;
+  *sweeps = state[1];
+  if (state[2] == MAFEM_NAN_DETECTED) {
+    h->err = "non-finite refinement residual or correction";
+    return MAFEM_NAN_DETECTED;
+  }
+  if (state[2] == MAFEM_REFINE_STALLED) {
+    h->err = "iterative refinement stalled or did not reach its tolerance in " + std::to_string(state[1]) + " sweeps";
+    return MAFEM_REFINE_STALLED;
+  }
+  return MAFEM_OK;
 }
 
 extern "C" int mafem_calc_r_K(mafem_handle* h, double time, double dt, double* r_out, double* band_out,
@@ -1041,6 +1058,10 @@ static int iter_finish(mafem_handle* h) {
     int ps[4];
     std::memcpy(ps, h->h_out + 5, sizeof ps);
     h->ss_sweeps = ps[3];
+    if (ps[1] != 0) {
+      h->err = "batched FP32 factorisation: a bounded wait ran out";
+      return MAFEM_ERR_CUDA;
+    }
     if (ps[2] != MAFEM_OK) {
       // the patch solve found no usable pivot in a node block, or its
       // refinement failed: the update was skipped; redo this iteration with

@@ -147,8 +147,9 @@ __global__ void newton_norm_kernel(const double* __restrict__ part, int nblk, in
 template <class T>
 __global__ void band_residual_kernel(const T* __restrict__ a0, BandLayout L, const double* __restrict__ x,
                                      const double* __restrict__ r, double* __restrict__ res,
-                                     double* __restrict__ part) {
+                                     double* __restrict__ part, const int* __restrict__ gate) {
   __shared__ double s_p[32];
+  if (gate && *gate) return;  // the refinement has already stopped
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
   double nrm = 0.0;
@@ -175,7 +176,9 @@ __global__ void band_residual_kernel(const T* __restrict__ a0, BandLayout L, con
     part[blockIdx.x] = a;
   }
 }
-__global__ void sqrt_sum_kernel(const double* __restrict__ part, int n, double* __restrict__ out) {
+__global__ void sqrt_sum_kernel(const double* __restrict__ part, int n, double* __restrict__ out,
+                                const int* __restrict__ gate) {
+  if (gate && *gate) return;
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double a = 0;
     for (int k = 0; k < n; ++k) a += part[k];
@@ -189,7 +192,8 @@ __global__ void axpy_kernel(int64_t n, const double* __restrict__ dx, double* __
 
 // x += dx with the partial sums of |dx|^2 and |x|^2 per block (part[2 b], part[2 b + 1])
 __global__ void axpy_norms_kernel(int64_t n, const double* __restrict__ dx, double* __restrict__ x,
-                                  double* __restrict__ part) {
+                                  double* __restrict__ part, const int* __restrict__ gate) {
+  if (gate && *gate) return;
   double dd = 0.0, xx = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double d = dx[i];
@@ -219,7 +223,9 @@ __global__ void axpy_norms_kernel(int64_t n, const double* __restrict__ dx, doub
   }
 }
 // out[0] = |dx|, out[1] = |x| from the block partial sums, in a fixed order
-__global__ void sqrt_pair_kernel(const double* __restrict__ part, int nblk, double* __restrict__ out) {
+__global__ void sqrt_pair_kernel(const double* __restrict__ part, int nblk, double* __restrict__ out,
+                                 const int* __restrict__ gate) {
+  if (gate && *gate) return;
   if (threadIdx.x == 0) {
     double a = 0.0, b = 0.0;
     for (int k = 0; k < nblk; ++k) {
@@ -256,15 +262,71 @@ void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, co
 int band_residual_blocks(int64_t n) { return (int)min64(304, (n + 255) / 256); }
 template <class T>
 void launch_band_residual(const T* a0, const BandLayout& L, const double* x, const double* r, double* res,
-                          double* part, double* out, cudaStream_t st) {
+                          double* part, double* out, cudaStream_t st, const int* gate) {
   const int blocks = band_residual_blocks(L.n);
-  band_residual_kernel<T><<<blocks, 256, 0, st>>>(a0, L, x, r, res, part);
-  sqrt_sum_kernel<<<1, 32, 0, st>>>(part, blocks, out);
+  band_residual_kernel<T><<<blocks, 256, 0, st>>>(a0, L, x, r, res, part, gate);
+  sqrt_sum_kernel<<<1, 32, 0, st>>>(part, blocks, out, gate);
 }
-void launch_axpy_norms(int64_t n, const double* dx, double* x, double* part, double* out, cudaStream_t st) {
+void launch_axpy_norms(int64_t n, const double* dx, double* x, double* part, double* out, cudaStream_t st,
+                       const int* gate) {
   const int blocks = (int)min64(1024, (n + 255) / 256);  // part holds 2048 doubles
-  axpy_norms_kernel<<<blocks, 256, 0, st>>>(n, dx, x, part);
-  sqrt_pair_kernel<<<1, 32, 0, st>>>(part, blocks, out);
+  axpy_norms_kernel<<<blocks, 256, 0, st>>>(n, dx, x, part, gate);
+  sqrt_pair_kernel<<<1, 32, 0, st>>>(part, blocks, out, gate);
+}
+
+// ---- device-side stopping test of one handle's iterative refinement ----------------
+// st[0] done, st[1] sweeps, st[2] status; nrm[0] |r0|, nrm[1] the previous
+// residual norm.  rn: the residual norm after the sweep (band_residual's out).
+__global__ void refine_init_kernel(const double* __restrict__ r0, int* __restrict__ st, double* __restrict__ nrm) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const double v = *r0;
+    nrm[0] = v;
+    nrm[1] = v;
+    st[1] = 0;
+    st[2] = MAFEM_OK;
+    st[0] = (v > 0.0) ? 0 : 1;  // a zero right-hand side: x = 0, nothing to refine
+    if (!(v == v) || v > 1.7976931348623157e308) {  // NaN or Inf
+      st[0] = 1;
+      st[2] = MAFEM_NAN_DETECTED;
+    }
+  }
+}
+// After each sweep: stop on |r| <= tol |r0| (MAFEM_OK), a non-finite norm
+// (MAFEM_NAN_DETECTED), a stall -- |r| > |r_prev| / 2 after the fourth sweep --
+// or max_sweeps (MAFEM_REFINE_STALLED).
+__global__ void refine_check_kernel(const double* __restrict__ rn, const double* __restrict__ dxn, int* __restrict__ st,
+                                    double* __restrict__ nrm, double tol, int max_sweeps) {
+  if (threadIdx.x != 0 || blockIdx.x != 0 || st[0]) return;
+  const double r = *rn, d = dxn[0], xv = dxn[1];
+  const int k = st[1] + 1;
+  st[1] = k;
+  if (!isfinite(r) || !isfinite(d) || !isfinite(xv)) {
+    st[2] = MAFEM_NAN_DETECTED;
+    st[0] = 1;
+  } else if (r <= tol * nrm[0]) {
+    st[0] = 1;
+  } else if ((k >= 4 && r > 0.5 * nrm[1]) || k >= max_sweeps) {
+    st[2] = MAFEM_REFINE_STALLED;
+    st[0] = 1;
+  }
+  nrm[1] = r;
+}
+__global__ void copy_gated_kernel(int64_t n, const double* __restrict__ src, double* __restrict__ dst,
+                                  const int* __restrict__ gate) {
+  if (gate && *gate) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+void launch_refine_init(const double* r0, int* st, double* nrm, cudaStream_t s) {
+  refine_init_kernel<<<1, 32, 0, s>>>(r0, st, nrm);
+}
+void launch_refine_check(const double* rn, const double* dxn, int* st, double* nrm, double tol, int max_sweeps,
+                         cudaStream_t s) {
+  refine_check_kernel<<<1, 32, 0, s>>>(rn, dxn, st, nrm, tol, max_sweeps);
+}
+void launch_copy_gated(int64_t n, const double* src, double* dst, const int* gate, cudaStream_t s) {
+  const int blocks = (int)min64(304, (n + 255) / 256);
+  copy_gated_kernel<<<blocks, 256, 0, s>>>(n, src, dst, gate);
 }
 void launch_axpy(int64_t n, const double* dx, double* x, cudaStream_t st) {
   const int blocks = (int)min64(1024, (n + 255) / 256);
@@ -276,8 +338,8 @@ template void launch_band_gather<double>(const DevPatch&, int, int, const BandLa
 template void launch_band_gather<float>(const DevPatch&, int, int, const BandLayout&, const float*, float*,
                                         cudaStream_t, float*);
 template void launch_band_residual<double>(const double*, const BandLayout&, const double*, const double*, double*,
-                                           double*, double*, cudaStream_t);
+                                           double*, double*, cudaStream_t, const int*);
 template void launch_band_residual<float>(const float*, const BandLayout&, const double*, const double*, double*,
-                                          double*, double*, cudaStream_t);
+                                          double*, double*, cudaStream_t, const int*);
 
 }  // namespace mafem

@@ -335,10 +335,12 @@ template <class T, class V>
 __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restrict__ ab, BandLayout L, int kuf,
                                                                 const int* __restrict__ ps, int npan,
                                                                 const T* __restrict__ rdiag, V* y, int* flags,
-                                                                int epoch, int* err, WaitTest wt) {
+                                                                int epoch, int* err, WaitTest wt,
+                                                                const int* gate) {
   __shared__ V part[8][33];
   __shared__ V Us[32][33];
   __shared__ int s_ok;
+  if (gate && *gate) return;  // every CTA reads the same word: all return (refinement already stopped)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int q = npan - 1 - (int)blockIdx.x; q >= 0; q -= gridDim.x) {
     const int64_t j0 = ps[q], j1 = ps[q + 1];
@@ -400,11 +402,13 @@ __global__ void __launch_bounds__(256) blk_forward_coop_kernel(const T* __restri
                                                                const int* __restrict__ ps, int npan,
                                                                const int* __restrict__ perm_all,
                                                                const T* __restrict__ rdiag, V* b, V* zbuf,
-                                                               int* flags, int epoch, int* err, WaitTest wt) {
+                                                               int* flags, int epoch, int* err, WaitTest wt,
+                                                               const int* gate) {
   __shared__ V part[8][33];
   __shared__ V Ls[32][33];
   __shared__ V accs[32];
   __shared__ int s_ok;
+  if (gate && *gate) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int p = blockIdx.x; p < npan; p += gridDim.x) {
     const int64_t j0 = ps[p], j1 = ps[p + 1];
@@ -598,12 +602,12 @@ void blk_forward(const T* ab, const BandLayout& L, const BlkPlan& B, const int* 
 }
 template <class V, class T>
 int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, int* flags, int epoch,
-                 int* err, int grid, cudaStream_t st, WaitTest wt) {
+                 int* err, int grid, cudaStream_t st, WaitTest wt, const int* gate) {
   const int npan = B.npan();
   int kuf = B.kuf;
   const int* ps = B.d_ps;
-  void* args[] = {(void*)&ab, (void*)&L, (void*)&kuf, (void*)&ps, (void*)&npan, (void*)&rdiag, (void*)&y,
-                  (void*)&flags, (void*)&epoch, (void*)&err, (void*)&wt};
+  void* args[] = {(void*)&ab,    (void*)&L,     (void*)&kuf, (void*)&ps, (void*)&npan, (void*)&rdiag,
+                  (void*)&y,     (void*)&flags, (void*)&epoch, (void*)&err, (void*)&wt,  (void*)&gate};
   const cudaError_t e = cudaLaunchCooperativeKernel((const void*)blk_backward_coop_kernel<T, V>,
                                                     dim3(std::min(grid, npan)), dim3(256), args, 0, st);
   return e == cudaSuccess ? 0 : -1;
@@ -616,11 +620,12 @@ void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const
 // cooperative forward substitution; returns 0, or -1 if the launch was refused
 template <class V, class T>
 int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
-                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st, WaitTest wt) {
+                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st, WaitTest wt,
+                     const int* gate) {
   const int npan = B.npan();
   const int* ps = B.d_ps;
   void* args[] = {(void*)&ab,    (void*)&L,    (void*)&ps,    (void*)&npan,  (void*)&perm_all, (void*)&rdiag,
-                  (void*)&b,     (void*)&zbuf, (void*)&flags, (void*)&epoch, (void*)&err, (void*)&wt};
+                  (void*)&b,     (void*)&zbuf, (void*)&flags, (void*)&epoch, (void*)&err, (void*)&wt, (void*)&gate};
   const cudaError_t e = cudaLaunchCooperativeKernel((const void*)blk_forward_coop_kernel<T, V>,
                                                     dim3(std::min(grid, npan)), dim3(256), args, 0, st);
   return e == cudaSuccess ? 0 : -1;
@@ -646,9 +651,9 @@ template void blk_forward<double, double>(const double*, const BandLayout&, cons
 template void blk_forward<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*, const float*,
                                          double*, cudaStream_t);
 template int blk_backward<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*, double*,
-                                          int*, int, int*, int, cudaStream_t, WaitTest);
+                                          int*, int, int*, int, cudaStream_t, WaitTest, const int*);
 template int blk_backward<double, float>(const float*, const BandLayout&, const BlkPlan&, const float*, double*, int*,
-                                         int, int*, int, cudaStream_t, WaitTest);
+                                         int, int*, int, cudaStream_t, WaitTest, const int*);
 template void blk_backward_1cta<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*,
                                                 double*, cudaStream_t);
 template void blk_backward_1cta<double, float>(const float*, const BandLayout&, const BlkPlan&, const float*, double*,
@@ -657,8 +662,9 @@ template int blk_backward_grid<double, double>();
 template int blk_backward_grid<double, float>();
 template int blk_forward_coop<double, double>(const double*, const BandLayout&, const BlkPlan&, const int*,
                                               const double*, double*, double*, int*, int, int*, int, cudaStream_t,
-                                              WaitTest);
+                                              WaitTest, const int*);
 template int blk_forward_coop<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*, const float*,
-                                             double*, double*, int*, int, int*, int, cudaStream_t, WaitTest);
+                                             double*, double*, int*, int, int*, int, cudaStream_t, WaitTest,
+                                             const int*);
 
 }  // namespace mafem

@@ -31,35 +31,50 @@
 #include <cstdint>
 
 #include "band_lu_common.cuh"
+#include "tcgen05.cuh"
 
 namespace mafem {
 
 constexpr int kPT = 512;   // threads per CTA of the factorisation (16 warps)
 constexpr int kRT = 768;   // threads per CTA of the refinement (24 warps)
-constexpr int kPCH = 288;      // trailing columns per chunk (a 32 x 32 patch's ~550 in two)
-constexpr int kYS = kPCH + 8;  // row stride of Y (uint2 hi/lo pairs) in shared memory
+constexpr int kNCH = 256;  // trailing columns per chunk at most (the MMA's N <= 256)
+constexpr int kMT = 128;   // rows of A22 per tensor-core tile (the MMA's M)
 constexpr int kIS = 36;    // shared-memory row stride of the 32 x 32 inverses (16-byte rows)
+// Y (the MMA's B operand, K-major core matrices): element (k, c) of a chunk at
+// float (k / 4) * 4 kNCH + 4 c + k % 4, hi and lo parts in two such arrays
+constexpr uint32_t kYPlane = 16u * kNCH;                // bytes between k-quads (the LBO of B)
+constexpr uint32_t kYBytes = 8u * kYPlane;              // one of Yh / Yl: 32 KB
+constexpr uint32_t kATile = 8u * kMT * 16u;             // one of A21h / A21l per M tile: 16 KB
+constexpr uint32_t kChunkBytes = 2 * kYBytes + 4 * kATile;  // Yh, Yl and two (A21h, A21l) tile buffers: 128 KB
+constexpr uint32_t kTmemCols = 2 * kNCH;                // two FP32 accumulators of 128 x 256
+// A factorisation CTA asks for at least this much dynamic shared memory, so no
+// two of them share an SM and its Tensor Memory (each allocates all 512 columns).
+constexpr size_t kExclusiveSmem = 116 * 1024;
 
-// panel column stride in shared memory: >= 32 + kl, == 8 mod 32 (conflict-free MMA fragments)
+// panel column stride in shared memory: >= 32 + kl, == 8 mod 32 (conflict-free column staging)
 __host__ __device__ inline int patch_rp(int kl) { return ((kBlkW + kl + 23) & ~31) + 8; }
+__host__ __device__ inline size_t patch_region0(int kl) {
+  const size_t lp = sizeof(float) * (size_t)kBlkW * patch_rp(kl);
+  const size_t r = lp > kChunkBytes ? lp : kChunkBytes;
+  return (r + 1023) & ~(size_t)1023;
+}
 
 size_t patch_factor_smem(int kl) {
-  return sizeof(float) * ((size_t)kBlkW * patch_rp(kl) + 2 * (size_t)kBlkW * kYS + 3 * (size_t)kBlkW * kIS);
+  const size_t s = patch_region0(kl) + sizeof(float) * 3 * (size_t)kBlkW * kIS;
+  return s > kExclusiveSmem ? s : kExclusiveSmem;
 }
+// Rows of the split-A21 buffer per part (hi, lo): the most rows below a panel's
+// diagonal block (kl), rounded up to whole M tiles.
+int patch_a21_rows(int kl) { return (kl + kMT - 1) / kMT * kMT; }
 
-// D += A B on the tensor cores: A 16 x 8 (row), B 8 x 8 (col), TF32 in, FP32 accumulate
-__device__ __forceinline__ void mma_tf32(float (&d)[4], const unsigned (&a)[4], const unsigned (&b)[2]) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
-      "{%0, %1, %2, %3};"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
 // x = hi + lo with hi, lo TF32 (round to nearest): the 3xTF32 split
-__device__ __forceinline__ void split_tf32(float x, unsigned& hi, unsigned& lo) {
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
-  const float r = x - __uint_as_float(hi);
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+__device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
+  unsigned h, l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  const float r = x - __uint_as_float(h);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(r));
+  hi = __uint_as_float(h);
+  lo = __uint_as_float(l);
 }
 size_t patch_refine_smem(int64_t n) { return sizeof(float) * (size_t)n; }
 
@@ -77,18 +92,40 @@ __device__ __forceinline__ void cluster_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
+// Bounded wait on an mbarrier phase: after kMbarPolls polls the wait gives up
+// and records 1 in *err (the patch's wait-ran-out word); once that word is
+// set every later wait gives up at its first poll, so the kernel runs to its
+// end quickly, and the host reports the failure.
+constexpr int kMbarPolls = 1 << 20;
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t* bar, uint32_t& ph, int* err) {
+  for (int it = 0; !mbar_try_wait(bar, ph); ++it)
+    if (it > kMbarPolls || *(volatile int*)err) {
+      atomicExch(err, 1);
+      break;
+    }
+  ph ^= 1u;
+}
+
 // trace (J.trace, optional): per panel 6 globaltimer stamps -- [0] start,
-// [1] diagonal block factored, [2] panel staged and inverses formed,
+// [1] diagonal block factored, [2] panel staged, inverses formed and A21 split,
 // [3] U12 / Y of the first chunk, [4] its trailing update, [5] panel done
 //
 // NR = 2: a patch on a cluster of two CTAs (launched with cluster dims (2,1,1)).
-// Rank 0 factors the diagonal block; both ranks stage the panel and form the
-// inverses; rank r updates the trailing chunks r, r + 2, ... .  A column moves
-// from rank 1's chunks to rank 0's as the panels advance, so every band read
-// goes to L2 (ld.global.cg) and each panel ends at a cluster barrier; the
-// factored block is published by another after the panel factorisation.  Both
-// ranks run the same panel loop, so every barrier is reached by all threads of
-// both CTAs.
+// Rank 0 factors the diagonal block; both ranks stage the panel, form the
+// inverses and split half of A21 each; rank r updates the trailing chunks
+// r, r + 2, ... .  A column moves from rank 1's chunks to rank 0's as the
+// panels advance, so every band read goes to L2 (ld.global.cg) and each panel
+// ends at a cluster barrier; the factored block is published by another after
+// the panel factorisation.  Both ranks run the same panel loop, so every
+// barrier is reached by all threads of both CTAs.
+//
+// The trailing update A22 -= A21 Y runs on the fifth-generation tensor cores:
+// per 128-row tile of A22, 3 x 4 tcgen05.mma of kind::tf32 (the 3xTF32 split
+// a b ~ al bh + ah bl + ah bh over K = 32 in steps of 8) accumulate A21 Y in
+// Tensor Memory; the A21 tiles come by TMA (a 3-D tensor map over the patch's
+// split-A21 buffer, written once per panel) into two shared-memory buffers, so
+// the copy of tile t + 2 and the MMAs of tile t + 1 run while all 16 warps read
+// tile t's accumulators back (tcgen05.ld) and write A22 - A21 Y to the band.
 template <int NR>
 __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __restrict__ jobs,
                                                              const int* __restrict__ order) {
@@ -98,18 +135,42 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
   const BandLayout L = J.L;
   float* __restrict__ ab = J.band;
   const int Rp = patch_rp(L.kl);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* Lp = reinterpret_cast<float*>(smem_raw);  // [32][Rp]: A(j0 + r, j0 + c) at Lp[c * Rp + r]
-  uint2* Ys = reinterpret_cast<uint2*>(Lp + (size_t)kBlkW * Rp);  // [32][kYS]: Y = Mi P A12 split hi/lo (TF32)
-  float* Li = reinterpret_cast<float*>(Ys + kBlkW * kYS);          // [32][kIS]
+  extern __shared__ __align__(1024) unsigned char smem_fac[];
+  // region 0: the panel's columns while the panel is staged, then the chunk buffers
+  float* Lp = reinterpret_cast<float*>(smem_fac);  // [32][Rp]: A(j0 + r, j0 + c) at Lp[c * Rp + r]
+  float* Yh = reinterpret_cast<float*>(smem_fac);  // [8][kNCH][4]
+  float* Yl = reinterpret_cast<float*>(smem_fac + kYBytes);
+  unsigned char* Abuf = smem_fac + 2 * kYBytes;  // [2][A21h tile | A21l tile]
+  float* Li = reinterpret_cast<float*>(smem_fac + patch_region0(L.kl));  // [32][kIS]
   float* Ui = Li + kBlkW * kIS;
   float* Mi = Ui + kBlkW * kIS;
   __shared__ float s_l[2][32];
   __shared__ int s_p[2];
   __shared__ int sp[32];
   __shared__ float rd[32];
+  __shared__ __align__(8) uint64_t bar_tma[2], bar_mma[2];
+  __shared__ uint32_t s_tmem;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t ldm = L.ldb - 1;  // A(i, j + 1) - A(i, j) in the band array
+  const int nrp = J.a21_rows;     // rows per part of the split-A21 buffer
+  int* err = J.info + 1;
+
+  if (tid == 0) {
+    mbar_init(&bar_tma[0], 1);
+    mbar_init(&bar_tma[1], 1);
+    mbar_init(&bar_mma[0], 1);
+    mbar_init(&bar_mma[1], 1);
+    mbar_init_fence();
+  }
+  if (warp == 0) {
+    tc::tmem_alloc(&s_tmem, kTmemCols);
+    tc::tmem_relinquish();
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = s_tmem;
+  uint32_t ph_tma[2] = {0u, 0u}, ph_mma[2] = {0u, 0u};  // phases (thread 0 uses ph_tma)
 
   for (int p = 0; p < J.npan; ++p) {
     const int64_t j0 = J.ps[p], j1 = J.ps[p + 1];
@@ -169,6 +230,30 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
       float* X = warp == 0 ? Li : Ui;
 #pragma unroll
       for (int i = 0; i < 32; ++i) X[i * kIS + lane] = (lane < w && i < w) ? x[i] : 0.0f;
+    } else {
+      // A21 (rows w .. R-1 of the panel) split into TF32 hi / lo parts, written
+      // to the patch's split-A21 buffer as 8 k-quad planes [k/4][row][k%4]
+      // (hi rows 0 .. nrp-1, lo rows nrp .. 2 nrp-1), rows past the panel and
+      // columns k >= w zero; each rank of a cluster writes half of the rows
+      const int nr = R - w;
+      const int nrt = (nr + kMT - 1) / kMT * kMT;
+      const int rlo = NR > 1 ? rank * (nrt / 2) : 0, rhi = NR > 1 && rank == 0 ? nrt / 2 : nrt;
+      for (int idx = tid - 64; idx < (rhi - rlo) * 8; idx += kPT - 64) {
+        const int r = rlo + idx % (rhi - rlo), kq = idx / (rhi - rlo);
+        float4 h, l;
+        float* hv = &h.x;
+        float* lv = &l.x;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int k = 4 * kq + e;
+          const float v = (r < nr && k < w) ? Lp[k * Rp + w + r] : 0.0f;
+          split_tf32(v, hv[e], lv[e]);
+        }
+        float4* plane = reinterpret_cast<float4*>(J.a21) + (size_t)kq * 2 * nrp;
+        plane[r] = h;
+        plane[nrp + r] = l;
+      }
+      fence_proxy_async_global();  // read by TMA (this CTA or, after the cluster barrier, the other)
     }
     __syncthreads();
     float* inv = J.inv + (size_t)p * 2 * kBlkW * kBlkW;  // Li then Ui, 32 x 32, column-major
@@ -183,25 +268,32 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
       }
     }
     __syncthreads();
+    if (NR > 1) cluster_sync();  // both halves of the split A21 written (and Lp no longer read)
     stamp(tr, 2);
 
-    // 3. trailing columns [j1, j1 + C) in chunks of kPCH
+    // 3. trailing columns [j1, j1 + C) in chunks of nch <= kNCH, balanced over the ranks
     const int nr = R - w;
-    for (int cb = rank * kPCH; cb < C; cb += NR * kPCH) {
-      const int nc = min(kPCH, C - cb);
-      // U12 = Li P A12 and Y = Mi P A12: one thread per column, the column in registers
-      for (int c = tid; c < nc; c += kPT) {
+    const int ntile = (nr + kMT - 1) / kMT;
+    const int cpr = (C + NR * kNCH - 1) / (NR * kNCH);  // chunks per rank
+    const int nch = C > 0 ? ((C + NR * cpr - 1) / (NR * cpr) + 15) & ~15 : kNCH;
+    bool first = true;
+    for (int cb = rank * nch; cb < C; cb += NR * nch) {
+      const int nc = min(nch, C - cb);
+      const int ncp = (nc + 15) & ~15;  // the MMA's N
+      // U12 = Li P A12 and Y = Mi P A12: one thread per column, the column in
+      // registers; Y goes to Yh / Yl split into TF32 parts (zero beyond nc)
+      for (int c = tid; c < ncp; c += kPT) {
         const int64_t col = j1 + cb + c;
         float* dst = ab + bix(L, j0, col);  // A(j0 + r, col) = dst[r]
         float a[32];
 #pragma unroll
-        for (int k = 0; k < 32; ++k) a[k] = k < w ? ldx<CG>(dst + sp[k]) : 0.0f;
+        for (int k = 0; k < 32; ++k) a[k] = (c < nc && k < w) ? ldx<CG>(dst + sp[k]) : 0.0f;
 #pragma unroll 2
         for (int r = 0; r < 32; ++r) {
+          float u = 0.0f, y = 0.0f;
           if (r < w) {  // block-uniform
             const float4* l4 = reinterpret_cast<const float4*>(Li + r * kIS);
             const float4* m4 = reinterpret_cast<const float4*>(Mi + r * kIS);
-            float u = 0.0f, y = 0.0f;
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
               const float4 l = l4[k], m = m4[k];
@@ -214,105 +306,92 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
               y = fmaf(m.z, a[4 * k + 2], y);
               y = fmaf(m.w, a[4 * k + 3], y);
             }
-            dst[r] = u;  // U12
-            uint2 yy;
-            split_tf32(y, yy.x, yy.y);
-            Ys[r * kYS + c] = yy;
+            if (c < nc) dst[r] = u;  // U12
           }
+          float yh, yl;
+          split_tf32(y, yh, yl);  // rows r >= w: 0
+          const int o = (r >> 2) * (4 * kNCH) + 4 * c + (r & 3);
+          Yh[o] = yh;
+          Yl[o] = yl;
         }
       }
+      fence_proxy_async_smem();  // Yh / Yl are read by the tensor cores
       __syncthreads();
-      if (cb == 0) stamp(tr, 3);
-      // A22 -= A21 Y on the tensor cores, 3xTF32 (a b ~ ah bh + ah bl + al bh:
-      // FP32-level accuracy).  A warp task is a 16-row strip of A22 over half
-      // of the chunk's column tiles: the strip's A21 fragments (negated, so the
-      // MMAs accumulate A22 - A21 Y) are split once into registers; Y comes
-      // pre-split from shared memory; the next column tile's A22 values are
-      // loaded while the current tile's MMAs run.  Fragment layouts
-      // (m16n8k8, g = lane / 4, t = lane % 4): A a0 (g, t), a1 (g + 8, t),
-      // a2 (g, t + 4), a3 (g + 8, t + 4); B b0 (t, g), b1 (t + 4, g);
-      // C c0 (g, 2t), c1 (g, 2t + 1), c2 (g + 8, 2t), c3 (g + 8, 2t + 1).
-      {
-        const int g = lane >> 2, t4 = lane & 3;
-        const int nrs = (nr + 15) >> 4, nct = (nc + 31) >> 5;
-        const int nhalf = nct > 1 ? 2 : 1;
-        const int ksteps = (w + 7) >> 3;
-        for (int task = warp; task < nrs * nhalf; task += kPT / 32) {
-          const int rs = task / nhalf, hf = task - rs * nhalf;
-          const int ct0 = hf * ((nct + 1) >> 1), ct1 = hf + 1 == nhalf ? nct : (nct + 1) >> 1;
-          const int r0 = w + rs * 16;
-          const int ra = r0 + g, rb = r0 + g + 8;
-          const bool oka = ra < R, okb = rb < R;
-          unsigned ah[4][4], al[4][4];
-#pragma unroll
-          for (int ks = 0; ks < 4; ++ks) {
-            const int k0 = ks * 8 + t4, k1 = k0 + 4;
-            const int ca = min(ra, R - 1), cbr = min(rb, R - 1);
-            const float x0 = k0 < w ? -Lp[k0 * Rp + ca] : 0.0f;
-            const float x1 = k0 < w ? -Lp[k0 * Rp + cbr] : 0.0f;
-            const float x2 = k1 < w ? -Lp[k1 * Rp + ca] : 0.0f;
-            const float x3 = k1 < w ? -Lp[k1 * Rp + cbr] : 0.0f;
-            split_tf32(x0, ah[ks][0], al[ks][0]);
-            split_tf32(x1, ah[ks][1], al[ks][1]);
-            split_tf32(x2, ah[ks][2], al[ks][2]);
-            split_tf32(x3, ah[ks][3], al[ks][3]);
-          }
-          // rows ra / rb of the chunk's first column: A(j0 + r, j1 + cb) = row pointer
-          float* pa = ab + bix(L, j0 + ra, j1 + cb);
-          float* pb = ab + bix(L, j0 + rb, j1 + cb);
-          auto load_c = [&](int ct, float (&c)[4][4]) {
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-              const int cc = ct * 32 + nt * 8 + 2 * t4;
-              const bool c0k = cc < nc, c1k = cc + 1 < nc;
-              c[nt][0] = oka && c0k ? ldx<CG>(pa + (int64_t)cc * ldm) : 0.0f;
-              c[nt][1] = oka && c1k ? ldx<CG>(pa + (int64_t)(cc + 1) * ldm) : 0.0f;
-              c[nt][2] = okb && c0k ? ldx<CG>(pb + (int64_t)cc * ldm) : 0.0f;
-              c[nt][3] = okb && c1k ? ldx<CG>(pb + (int64_t)(cc + 1) * ldm) : 0.0f;
-            }
-          };
-          float acc[4][4], nxt[4][4];
-          if (ct0 < ct1) load_c(ct0, nxt);
-          for (int ct = ct0; ct < ct1; ++ct) {
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-              for (int e = 0; e < 4; ++e) acc[nt][e] = nxt[nt][e];
-            if (ct + 1 < ct1) load_c(ct + 1, nxt);
-#pragma unroll
-            for (int ks = 0; ks < 4; ++ks) {
-              if (ks >= ksteps) break;  // warp-uniform; the unrolled index keeps ah / al in registers
-              const int k0 = ks * 8 + t4;
-#pragma unroll
-              for (int nt = 0; nt < 4; ++nt) {
-                const int c = ct * 32 + nt * 8 + g;
-                // rows k >= w of Y are stale shared memory: mask them (0 * NaN would not vanish)
-                const uint2 y0 = k0 < w ? Ys[k0 * kYS + c] : make_uint2(0u, 0u);
-                const uint2 y1 = k0 + 4 < w ? Ys[(k0 + 4) * kYS + c] : make_uint2(0u, 0u);
-                const unsigned bh[2] = {y0.x, y1.x}, bl[2] = {y0.y, y1.y};
-                mma_tf32(acc[nt], al[ks], bh);
-                mma_tf32(acc[nt], ah[ks], bl);
-                mma_tf32(acc[nt], ah[ks], bh);
-              }
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-              const int cc = ct * 32 + nt * 8 + 2 * t4;
-              const bool c0k = cc < nc, c1k = cc + 1 < nc;
-              if (oka && c0k) pa[(int64_t)cc * ldm] = acc[nt][0];
-              if (oka && c1k) pa[(int64_t)(cc + 1) * ldm] = acc[nt][1];
-              if (okb && c0k) pb[(int64_t)cc * ldm] = acc[nt][2];
-              if (okb && c1k) pb[(int64_t)(cc + 1) * ldm] = acc[nt][3];
-            }
-          }
+      if (first) stamp(tr, 3);
+
+      // A22 -= A21 Y, 128 rows at a time
+      const uint32_t idesc = tc::idesc_tf32(kMT, ncp);
+      const uint32_t yh = tc::saddr(Yh), yl = tc::saddr(Yl), a0 = tc::saddr(Abuf);
+      const int ksteps = (w + 7) >> 3;
+      auto tma_tile = [&](int t) {  // thread 0: tile t's A21h and A21l into buffer t & 1
+        const int b = t & 1;
+        mbar_arrive_expect_tx(&bar_tma[b], 2 * kATile);
+        tc::tma_load_3d(Abuf + b * 2 * kATile, &J.a21_map, 0, t * kMT, 0, &bar_tma[b]);
+        tc::tma_load_3d(Abuf + b * 2 * kATile + kATile, &J.a21_map, 0, nrp + t * kMT, 0, &bar_tma[b]);
+      };
+      auto mma_tile = [&](int t) {  // thread 0: tile t's products into accumulator t & 1
+        const int b = t & 1;
+        mbar_wait_bounded(&bar_tma[b], ph_tma[b], err);
+        tc::fence_after();
+        const uint32_t ah = a0 + b * 2 * kATile, al = ah + kATile, d = tmem + b * kNCH;
+        for (int s = 0; s < ksteps; ++s) {  // k = 8 s .. 8 s + 7: k-quads 2 s and 2 s + 1
+          const uint64_t dah = tc::smem_desc(ah + 2 * s * (kMT * 16), kMT * 16, 128);
+          const uint64_t dal = tc::smem_desc(al + 2 * s * (kMT * 16), kMT * 16, 128);
+          const uint64_t dbh = tc::smem_desc(yh + 2 * s * kYPlane, kYPlane, 128);
+          const uint64_t dbl = tc::smem_desc(yl + 2 * s * kYPlane, kYPlane, 128);
+          tc::mma_tf32(d, dal, dbh, idesc, s > 0 ? 1u : 0u);
+          tc::mma_tf32(d, dah, dbl, idesc, 1u);
+          tc::mma_tf32(d, dah, dbh, idesc, 1u);
         }
+        tc::commit(&bar_mma[b]);
+      };
+      if (tid == 0 && ntile > 0) {
+        tma_tile(0);
+        if (ntile > 1) tma_tile(1);
+        mma_tile(0);
       }
-      __syncthreads();
-      if (cb == 0) stamp(tr, 4);
+      // epilogue roles: warp w reads lanes 32 (w % 4) .. + 31 (its rows) of
+      // column group w / 4 (a quarter of the chunk, in multiples of 8 columns)
+      const int q = warp & 3, grp = warp >> 2;
+      const int cpg = ((ncp >> 2) + 7) & ~7;
+      const int cs = min(ncp, grp * cpg), ce = min(ncp, cs + cpg);
+      for (int t = 0; t < ntile; ++t) {
+        const int b = t & 1;
+        mbar_wait_bounded(&bar_mma[b], ph_mma[b], err);  // tile t's products are in Tensor Memory
+        if (tid == 0) {
+          if (t + 2 < ntile) tma_tile(t + 2);  // buffer b is free: tile t's MMAs have completed
+          if (t + 1 < ntile) mma_tile(t + 1);  // into the other accumulator, read back at t - 1
+        }
+        tc::fence_after();
+        const int row = w + t * kMT + 32 * q + lane;  // panel row of this thread
+        const bool live = row < R;
+        float* pa = ab + bix(L, j0 + (live ? row : 0), j1 + cb);  // + c * ldm: A(j0 + row, j1 + cb + c)
+        const uint32_t dt = tmem + ((uint32_t)(32 * q) << 16) + b * kNCH;
+        for (int c0 = cs; c0 < ce; c0 += 16) {
+          float d0[8], d1[8];
+          tc::ld8(dt + c0, d0);
+          if (c0 + 8 < ce) tc::ld8(dt + c0 + 8, d1);
+          tc::wait_ld();
+          float v[16];
+#pragma unroll
+          for (int k = 0; k < 16; ++k) v[k] = (live && c0 + k < ce && c0 + k < nc) ? ldx<CG>(pa + (int64_t)(c0 + k) * ldm) : 0.0f;
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            if (live && c0 + k < ce && c0 + k < nc) pa[(int64_t)(c0 + k) * ldm] = v[k] - (k < 8 ? d0[k] : d1[k - 8]);
+        }
+        tc::fence_before();
+        __syncthreads();  // accumulator b is read before the MMAs of tile t + 2 overwrite it
+      }
+      if (first) stamp(tr, 4);
+      first = false;
     }
     if (NR > 1) cluster_sync();
     stamp(tr, 5);
   }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
 }
 
 // ---------------------------------------------------------------------------
@@ -577,9 +656,9 @@ __global__ void __launch_bounds__(kRT, 1) patch_refine_kernel(const PatchJob* __
   const int64_t n = J.L.n;
   int* stat = J.stat;  // [0] status, [1] sweeps
   float2* xs = J.xs;   // x split into two floats
-  if (J.info[0] != 0) {  // a node block without a usable pivot
+  if (J.info[1] != 0 || J.info[0] != 0) {  // a bounded wait ran out, or a node block had no usable pivot
     if (tid == 0) {
-      stat[0] = MAFEM_ZERO_PIVOT;
+      stat[0] = J.info[1] != 0 ? MAFEM_ERR_CUDA : MAFEM_ZERO_PIVOT;
       stat[1] = 0;
     }
     return;
@@ -654,7 +733,33 @@ __global__ void __launch_bounds__(kRT, 1) patch_refine_kernel(const PatchJob* __
   }
 }
 
-int patch_chunk_cols() { return kPCH; }
+int patch_chunk_cols() { return kNCH; }
+
+// The split-A21 buffer as a 3-D tensor (k % 4, row, k / 4) of FP32 with strides
+// 16 bytes (rows) and 2 a21_rows x 16 bytes (k-quad planes); one 4 x 128 x 8 box
+// is one M tile in the MMA's K-major core-matrix layout (k-quad planes 2 KB
+// apart, rows 16 bytes apart).
+bool patch_a21_map(PatchJob& J) {
+  using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static EncodeFn encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return false;
+    encode = reinterpret_cast<EncodeFn>(fn);
+  }
+  const cuuint64_t dims[3] = {4, (cuuint64_t)2 * J.a21_rows, 8};
+  const cuuint64_t strides[2] = {16, (cuuint64_t)2 * J.a21_rows * 16};
+  const cuuint32_t box[3] = {4, (cuuint32_t)kMT, 8};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(&J.a21_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, J.a21, dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 int patch_solve_setup() {
   int dev = 0, cap = 0;

@@ -110,6 +110,7 @@ BandLayout make_band_layout(int64_t n, int kl, int ku, int nb);
 }  // namespace mafem
 
 // ---- kernel launchers (elem.cu, assemble.cu, band_lu.cu) ----------------------
+#include <cuda.h>  // CUtensorMap
 #include <cuda_runtime.h>
 namespace mafem {
 template <class T>
@@ -129,10 +130,18 @@ void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, co
 int band_residual_blocks(int64_t n);
 template <class T>
 void launch_band_residual(const T* a0, const BandLayout& L, const double* x, const double* r, double* res,
-                          double* part, double* out, cudaStream_t st);
+                          double* part, double* out, cudaStream_t st, const int* gate = nullptr);
 void launch_axpy(int64_t n, const double* dx, double* x, cudaStream_t st);
 // x += dx; out[0] = |dx|, out[1] = |x| (part: 2048 doubles of scratch)
-void launch_axpy_norms(int64_t n, const double* dx, double* x, double* part, double* out, cudaStream_t st);
+void launch_axpy_norms(int64_t n, const double* dx, double* x, double* part, double* out, cudaStream_t st,
+                       const int* gate = nullptr);
+// Device-side stopping test of a handle's iterative refinement (assemble.cu):
+// st = {done, sweeps, status}, nrm = {|r0|, previous |r|}; kernels given
+// gate = st do nothing once done is set.
+void launch_refine_init(const double* r0, int* st, double* nrm, cudaStream_t s);
+void launch_refine_check(const double* rn, const double* dxn, int* st, double* nrm, double tol, int max_sweeps,
+                         cudaStream_t s);
+void launch_copy_gated(int64_t n, const double* src, double* dst, const int* gate, cudaStream_t s);
 
 template <class T>
 size_t apply_smem_bytes(const BandLayout& L, int threads);
@@ -189,7 +198,7 @@ struct WaitTest {
 };
 template <class V, class T>
 int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, int* flags, int epoch,
-                 int* err, int grid, cudaStream_t st, WaitTest wt = WaitTest());
+                 int* err, int grid, cudaStream_t st, WaitTest wt = WaitTest(), const int* gate = nullptr);
 template <class V, class T>
 int blk_backward_grid();
 // Forward substitution (P, L11, A21 of the stored panels) on `grid` CTAs of one
@@ -197,7 +206,8 @@ int blk_backward_grid();
 // for blk_backward.  Returns 0, or -1 if the cooperative launch was refused.
 template <class V, class T>
 int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
-                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st, WaitTest wt = WaitTest());
+                     V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st, WaitTest wt = WaitTest(),
+                     const int* gate = nullptr);
 // Persistent cooperative factorisation (band_lu_persist.cu): launch shape and
 // per-panel flags.  Flags are zeroed once; epochs make them reusable.
 struct BlkPersist {
@@ -231,6 +241,7 @@ namespace mafem {
 // One patch's FP32 solve in the batched form (band_lu_patch.cu): device
 // pointers of the handle that owns them.
 struct PatchJob {
+  CUtensorMap a21_map;  // TMA view of a21: 3-D (k % 4, row, k / 4), box 4 x 128 x 8
   float* band;          // factored in place
   const float* band0;   // the unfactored band (refinement residual)
   float* inv;           // [npan][2][32][32]: L11^-1, U11^-1 per panel, column-major
@@ -247,7 +258,14 @@ struct PatchJob {
   BandLayout L;
   int kuf, npan;
   long long* trace;     // optional: 6 globaltimer stamps per panel (patch_factor_kernel)
+  float* a21;           // split A21 of the current panel: [8][2 a21_rows][4] floats (TF32 hi rows, then lo rows)
+  int a21_rows;         // rows per part, a multiple of 128 (patch_a21_rows)
 };
+// Rows per part of a patch's split-A21 buffer for half bandwidth kl.
+int patch_a21_rows(int kl);
+// Encodes J.a21_map over J.a21 (J.a21, J.a21_rows set); returns false if the
+// driver refuses the tensor map.
+bool patch_a21_map(PatchJob& J);
 size_t patch_factor_smem(int kl);
 size_t patch_refine_smem(int64_t n);
 // Sets the kernels' shared-memory limits; returns the dynamic bytes available (0: unusable).
