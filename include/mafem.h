@@ -288,6 +288,9 @@ typedef struct mafem_request {
   const double* xms0;           /* initial state, copied at submit */
   const double* cps0;
   double refine_tol;            /* FP32 form: mafem_set_refinement's tol; 0 = default */
+  int32_t ramp_steps;           /* > 0: before step k the inhomogeneous Dirichlet values are scaled by
+                                   min(1, (k + 1) / ramp_steps), as mafem_set_dirichlet_scale does */
+  int32_t reserved;             /* 0 */
 } mafem_request;
 typedef struct mafem_server_stats {
   int64_t steps_done, rounds;
@@ -345,6 +348,14 @@ int mafem_solve_band(mafem_handle* h, const double* band, int64_t ldab, const do
  * block had no usable pivot (or the batched FP32 solve handed the iteration
  * back). */
 int64_t mafem_fallback_count(const mafem_handle* h);
+/* Set the inhomogeneous Dirichlet entries of the resident state (the mesh's
+ * dir_unknown / dir_node / dir_val, as prepare_input applies them,
+ * src/Input.jl:103-108) to scale * value, stream-ordered before the next step:
+ * a pull whose speed is ramped up over the first steps.  The reference sets
+ * these entries once; a run that changes them goes through restart with an
+ * edited cps file (src/MembraneAleFem.jl:75-107), which this replaces without
+ * a host round trip. */
+int mafem_set_dirichlet_scale(mafem_handle* h, double scale);
 /* Failure-detection test hook (no reference counterpart; the reference has no
  * inter-CTA waits).  The cooperative forward and back substitutions' waits for
  * another CTA give up after limit_polls polls (0: the default, 2^22), and the

@@ -128,6 +128,9 @@ struct mafem_handle {
   PatchJob job{};
   WaitTest wait_test;                   // mafem_set_wait_test (failure-detection tests)
   const double* host_band = nullptr;    // mafem_solve_band: the caller's band (padded layout), for the fallback
+  int n_dir = 0;                        // inhomogeneous Dirichlet entries of the state (mafem_set_dirichlet_scale)
+  int* d_dir_idx = nullptr;             // their index dof * numnp + node into cps
+  double* d_dir_val = nullptr;          // their values
   int* d_rstate = nullptr;              // refinement state {done, sweeps, status} (FP32 form)
   int* h_rstate = nullptr;              // its pinned host copy
   std::unique_ptr<StateWriter> writer;  // state files, created by the first write
@@ -206,6 +209,10 @@ static int validate(const mafem_mesh_desc* d, const mafem_params* p, std::string
     return MAFEM_ERR_ARG;
   }
   if (!d->IX || !d->ID || !d->uel_ids || !d->ufns) { err = "missing mesh arrays"; return MAFEM_ERR_ARG; }
+  if (d->n_dir < 0 || (d->n_dir > 0 && (!d->dir_unknown || !d->dir_node || !d->dir_val))) {
+    err = "missing Dirichlet arrays";
+    return MAFEM_ERR_ARG;
+  }
   // The gathers and the pull-force neighbourhood rely on the tensor-product
   // connectivity of construct_IX (Mesh.jl:574-593): node (a1, a2) of element
   // (e1, e2) is control point (e1 + a1) + num1np (e2 + a2) (0-based).  Any other
@@ -437,6 +444,27 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
   } while (0)
   UP(d_ix, ix);
   h->h_ix = ix;
+  {  // inhomogeneous Dirichlet entries as prepare_input applies them (Input.jl:103-108)
+    std::vector<int> didx;
+    std::vector<double> dval;
+    for (int64_t k = 0; k < d->n_dir; ++k) {
+      const int64_t u = d->dir_unknown[k], nd = d->dir_node[k];
+      if (u < 1 || u > 8 || nd < 1 || nd > numnp || pp.dof_of[u - 1] < 0) {
+        set_global_error("Dirichlet entry with an unknown or node out of range");
+        mafem_destroy(hp.release());
+        return MAFEM_ERR_ARG;
+      }
+      didx.push_back(pp.dof_of[u - 1] * numnp + (int)(nd - 1));
+      dval.push_back(d->dir_val[k]);
+      if (p->scenario == MAFEM_F_PULL && p->motion == MAFEM_EUL && pp.dof_of[5] >= 0) {
+        didx.push_back(pp.dof_of[5] * numnp + (int)(nd - 1));
+        dval.push_back(d->dir_val[k]);
+      }
+    }
+    h->n_dir = (int)didx.size();
+    UP(h->d_dir_idx, didx);
+    UP(h->d_dir_val, dval);
+  }
   AL(h->d_pull_list, 25);
   AL(h->d_pull_r, (size_t)25 * nq);
   UP(d_lm, lm);
@@ -957,6 +985,16 @@ extern "C" int mafem_predict(mafem_handle* h, double dt) {
   return MAFEM_OK;
 }
 
+// Whether the assembled residual d_r is finite (one norm, waits for the stream).
+static bool residual_finite(mafem_handle* h) {
+  launch_axpy_norms(h->nmdf, h->d_r, h->d_res, h->d_part, h->d_out + 10, h->st);  // |r| (d_res is scratch here)
+  double nr[2] = {0.0, 0.0};
+  if (cudaMemcpyAsync(nr, h->d_out + 10, sizeof nr, cudaMemcpyDeviceToHost, h->st) != cudaSuccess ||
+      cudaStreamSynchronize(h->st) != cudaSuccess)
+    return true;
+  return std::isfinite(nr[0]);
+}
+
 // ---- a time step as step_begin / iter_enqueue / iter_finish: mafem_time_step
 // runs them for one handle, mafem_batch_step interleaves many handles ----
 
@@ -990,6 +1028,12 @@ static int iter_enqueue(mafem_handle* h) {
     cudaEventRecord(h->ev[2], h->st);
     blk_back_solve<double>(h, h->d_x);
   } else if ((rc = factor_and_solve(h, h->d_r, &h->ss_sweeps)) != MAFEM_OK) {
+    // a singular or stalled solve of a non-finite system: report the NaN (the
+    // residual itself is not finite), as the other paths do
+    if (rc > 0 && !residual_finite(h)) {
+      h->err = "non-finite residual";
+      return MAFEM_NAN_DETECTED;
+    }
     return rc;
   }
   cudaEventRecord(h->ev[3], h->st);
@@ -1540,6 +1584,10 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
   for (ServerReq* q : s->active) {
     if (q->state != ServerReq::IDLE) continue;
     if (!q->in_step) {  // predictor (Analysis.jl:70) + step_begin
+      if (q->r.ramp_steps > 0) {  // the Dirichlet values ramped over the request's first steps
+        const double sc = std::min(1.0, (double)(q->step + 1) / q->r.ramp_steps);
+        launch_dirichlet_scale(q->h->P.cps, q->h->d_dir_idx, q->h->d_dir_val, q->h->n_dir, sc, q->h->st);
+      }
       launch_predictor(q->h->P, q->h->pp, q->r.dt, q->h->st);
       q->h->launches += 1;
       step_begin(q->h, q->t + q->r.dt, q->r.dt);
@@ -1990,6 +2038,14 @@ extern "C" int mafem_restore(mafem_handle* h, int32_t slot) {
   if (rc) return rc;
   CK(cudaMemcpyAsync(h->P.xms, xms, sizeof(double) * h->numnp * 3, cudaMemcpyDeviceToDevice, h->st));
   CK(cudaMemcpyAsync(h->P.cps, cps, sizeof(double) * h->numnp * h->ndf, cudaMemcpyDeviceToDevice, h->st));
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_set_dirichlet_scale(mafem_handle* h, double scale) {
+  if (!h || !std::isfinite(scale)) return MAFEM_ERR_ARG;
+  launch_dirichlet_scale(h->P.cps, h->d_dir_idx, h->d_dir_val, h->n_dir, scale, h->st);
+  h->launches += h->n_dir > 0 ? 1 : 0;
+  CK(cudaGetLastError());
   return MAFEM_OK;
 }
 

@@ -248,6 +248,14 @@ void launch_resid_gather(const DevPatch& P, int ndf, int nq, const double* r_el,
   const int blocks = (int)min64(1024, (P.nmdf + 255) / 256);
   resid_gather_kernel<<<blocks, 256, 0, st>>>(P, ndf, nq, r_el, r);
 }
+// cps[idx[k]] = s * val[k]: the inhomogeneous Dirichlet entries of the state, scaled
+__global__ void dirichlet_scale_kernel(double* __restrict__ cps, const int* __restrict__ idx,
+                                       const double* __restrict__ val, int n, double s) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) cps[idx[k]] = s * val[k];
+}
+void launch_dirichlet_scale(double* cps, const int* idx, const double* val, int n, double s, cudaStream_t st) {
+  if (n > 0) dirichlet_scale_kernel<<<(n + 255) / 256, 256, 0, st>>>(cps, idx, val, n, s);
+}
 void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaStream_t st) {
   const int blocks = (int)min64(1024, (3LL * P.numnp + 255) / 256);
   predictor_kernel<<<blocks, 256, 0, st>>>(P, pp, dt);

@@ -123,6 +123,8 @@ void launch_band_gather(const DevPatch& P, int ndf, int nq, const BandLayout& L,
                         cudaStream_t st, T* ab2 = nullptr);
 void launch_resid_gather(const DevPatch& P, int ndf, int nq, const double* r_el, double* r, cudaStream_t st);
 void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaStream_t st);
+// cps[idx[k]] = s * val[k] for k < n (the scaled inhomogeneous Dirichlet values)
+void launch_dirichlet_scale(double* cps, const int* idx, const double* val, int n, double s, cudaStream_t st);
 int newton_update_blocks(int64_t nmdf);
 void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
                           double* part, double* out, cudaStream_t st, const int* skip = nullptr,

@@ -103,7 +103,8 @@ class StepStats(C.Structure):
 class _CRequest(C.Structure):
     _fields_ = [("mesh", C.c_void_p), ("params", C.c_void_p), ("args", C.c_void_p), ("precision", C.c_int32),
                 ("nsteps", C.c_int32), ("t0", C.c_double), ("dt", C.c_double), ("xms0", C.c_void_p),
-                ("cps0", C.c_void_p), ("refine_tol", C.c_double)]
+                ("cps0", C.c_void_p), ("refine_tol", C.c_double), ("ramp_steps", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class ServerStats(C.Structure):
@@ -167,6 +168,7 @@ def lib():
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
         L.mafem_set_refinement.argtypes = [vp, C.c_int32, C.c_double]
         L.mafem_set_wait_test.argtypes = [vp, C.c_int32, C.c_int32]
+        L.mafem_set_dirichlet_scale.argtypes = [vp, C.c_double]
         L.mafem_solve_band.argtypes = [vp, _PD, C.c_int64, _PD, _PD]
         L.mafem_fallback_count.argtypes = [vp]
         L.mafem_fallback_count.restype = C.c_int64
@@ -494,6 +496,11 @@ class Solver:
         _raise(lib().mafem_solve_band(self.h, _dp(band), band.shape[1], _dp(rhs), _dp(x)), self.h)
         return x
 
+    def set_dirichlet_scale(self, scale: float) -> None:
+        """Inhomogeneous Dirichlet entries of the resident state = scale x their
+        values (stream-ordered before the next step): a ramped pull."""
+        _raise(lib().mafem_set_dirichlet_scale(self.h, float(scale)), self.h)
+
     def fallback_count(self) -> int:
         """Factorisations redone with full partial pivoting so far."""
         return int(lib().mafem_fallback_count(self.h))
@@ -673,12 +680,13 @@ class Server:
         self._keep = {}  # id -> objects the library reads until the request is admitted
 
     def submit(self, mesh, p, xms, cps, nsteps: int, dt: float, t0: float = 0.0,
-               precision: int = FP32_REFINE, refine_tol: float = 0.0) -> int:
+               precision: int = FP32_REFINE, refine_tol: float = 0.0, ramp_steps: int = 0) -> int:
         xms = np.asfortranarray(xms, dtype=np.float64)
         cps = np.asfortranarray(cps, dtype=np.float64)
         cp, ca = p.c_params(), p.c_args()
         req = _CRequest(C.addressof(mesh.desc), C.addressof(cp), C.addressof(ca), precision, int(nsteps),
-                        float(t0), float(dt), xms.ctypes.data, cps.ctypes.data, float(refine_tol))
+                        float(t0), float(dt), xms.ctypes.data, cps.ctypes.data, float(refine_tol),
+                        int(ramp_steps), 0)
         rid = C.c_int64()
         _raise(lib().mafem_server_submit(self.s, C.byref(req), C.byref(rid)))
         self._keep[rid.value] = (mesh, cp, ca, (mesh.numnp, mesh.ndf))
