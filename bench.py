@@ -274,14 +274,21 @@ def run_gb300(args, rank, world, local, dist):
 # (the tension drawn per patch instead of the reference's fixed kb / 4) and the
 # centre pull element (every size is even, and the reference's ceil(numel / 2)
 # would pull at the right edge).  The reference's pull is velocity-driven
-# (Bc.jl:227-243); the stated pull force f sets the pulling speed, f times
-# PULL_SPEED_PER_FORCE, and the reaction force the patches reach is measured
-# (calc_pull_force) and reported beside it.
-PULL_SPEED_PER_FORCE = 0.01
+# (Bc.jl:227-243): the stated pull force f sets the pulling speed, f times
+# PULL_SPEED_PER_FORCE, ramped linearly from 0 over the run's 30 steps (as the
+# force ramp of the smaller workloads) through the state's Dirichlet entries
+# (mafem_set_dirichlet_scale before each step); the reaction force the patches
+# reach is measured (calc_pull_force) and reported beside it.  Flat start: the
+# workload states no perturbation, and grid-scale noise on the graded 32 x 32
+# and 48 x 48 meshes, like an unramped start of the pull, makes the first
+# implicit step too stiff for the reference's plain Newton at dt 0.01 (in the
+# oracle as on the GPU).
+PULL_SPEED_PER_FORCE = 0.1
 BATCH = dict(name="batching workload: 256 independent tether-pull patches, n ~ U{8,12,16,24,32,48} elements per "
                   "side (seed 1), kb log-U[0.5, 2], lambda0 log-U[0.1, 10], pull force f ~ U[2, 10] driving the pull "
-                  "at speed 0.01 f, half LAG / half ALEVB, centre pull element, dt 0.01",
-             patches=256, sizes=(8, 12, 16, 24, 32, 48), seed=1, dt=0.01, steps=30)
+                  "at speed 0.1 f ramped from 0 over 30 steps, half LAG / half ALEVB, centre pull element, flat "
+                  "start, dt 0.01",
+             patches=256, sizes=(8, 12, 16, 24, 32, 48), seed=1, dt=0.01, steps=30, ramp=30)
 
 
 def batch_patches(M, wl=BATCH):
@@ -353,8 +360,9 @@ def run_batched(steps=None, wl=BATCH):
             t = 0.0
             cu.sync()
             h0 = time.perf_counter()
-            for _ in range(steps):
+            for k in range(steps):
                 t += dt
+                s.set_dirichlet_scale(min(1.0, (k + 1) / wl["ramp"]))
                 s.predict(dt)
                 try:
                     s.time_step_resident(t, dt)
@@ -376,6 +384,8 @@ def run_batched(steps=None, wl=BATCH):
                 t += dt
                 cu.sync()
                 h0 = time.perf_counter()
+                for s in fsolvers:  # the pull's ramp, stream-ordered before the step
+                    s.set_dirichlet_scale(min(1.0, (k + 1) / wl["ramp"]))
                 status, st = b.step(t, dt)
                 cu.sync()
                 f_lat.append((time.perf_counter() - h0) * 1e3)
@@ -392,8 +402,8 @@ def run_batched(steps=None, wl=BATCH):
             s.close()
     # (c) continuous batching of the same FP32 solves
     with M.Server() as srv:
-        ids = [srv.submit(mesh, p, x0, c0, steps, dt, precision=M.FP32_REFINE, refine_tol=FP32_REFINE_TOL)
-               for p, mesh, x0, c0 in patches]
+        ids = [srv.submit(mesh, p, x0, c0, steps, dt, precision=M.FP32_REFINE, refine_tol=FP32_REFINE_TOL,
+                          ramp_steps=wl["ramp"]) for p, mesh, x0, c0 in patches]
         cu.sync()
         h0 = time.perf_counter()
         got = {}
@@ -442,11 +452,12 @@ def run_batched(steps=None, wl=BATCH):
             "size_histogram": {str(k): v for k, v in sorted(sizes.items())}}
 
 
-SERVE = dict(name="serving: Poisson arrivals of tether-pull solves, n in {8,16,32,64} elements per side with "
-                  "probabilities {0.4,0.3,0.2,0.1} (seed 2), half LAG / half ALEVB, kb log-uniform [0.5, 2], "
-                  "pull speed 0.01 f/6 with f ~ U[2, 10], dt 0.005",
-             rates=(50, 200, 800), requests=48, sizes=(8, 16, 32, 64), probs=(0.4, 0.3, 0.2, 0.1), seed=2,
-             steps=(20, 100), step_scale=0.1, dt=0.005)
+SERVE = dict(name="serving workload: Poisson arrivals of tether-pull solves, n in {8,16,32,64} elements per side "
+                  "with probabilities {0.4,0.3,0.2,0.1} (seed 2), parameters drawn as in the batching workload "
+                  "(kb, lambda0, pull force, half LAG / half ALEVB, centre pull ramped over 30 steps, flat start), "
+                  "dt 0.01, 20-100 time steps per request",
+             rates=(50, 200, 800), requests=32, sizes=(8, 16, 32, 64), probs=(0.4, 0.3, 0.2, 0.1), seed=2,
+             steps=(20, 100), dt=0.01, ramp=30)
 
 
 def serve_requests(M, wl=SERVE):
@@ -457,29 +468,26 @@ def serve_requests(M, wl=SERVE):
     for k in range(wl["requests"]):
         n = int(rng.choice(wl["sizes"], p=wl["probs"]))
         kb = float(np.exp(rng.uniform(np.log(0.5), np.log(2.0))))
+        lam0 = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
         f = float(rng.uniform(2.0, 10.0))
         steps = int(rng.integers(wl["steps"][0], wl["steps"][1] + 1))
-        steps = max(2, int(round(steps * wl["step_scale"])))
         t += float(rng.exponential(1.0))
         motion = M.LAG if k % 2 == 0 else M.ALEVB
-        p = M.Params(motion=motion, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, kb=kb,
-                     pull_speed=0.01 * f / 6.0)
+        p = M.Params(motion=motion, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, kb=kb, lambda0=lam0,
+                     pull_centre=1, pull_speed=PULL_SPEED_PER_FORCE * f)
         mesh = M.Mesh(p)
         _, xms, cps = M.prepare_input(p, mesh)
-        M.perturb_interior_z(mesh, xms, seed=1000 + k, amp=1e-4)
         out.append((p, mesh, xms, cps, steps, t))
     return out
 
 
 def run_serving(wl=SERVE):
     """Continuous batching (mafem_server) of a Poisson stream of requests at each
-    rate, against the same requests solved one at a time with the plain FP64
-    path.  Requests whose FP32 band does not fit one CTA (the 64 x 64 patches)
-    are served in the plain FP64 form, which the server interleaves without
-    host waits; the others in the FP32 form with batched solves.  Per-step
-    latency is the wall time from a step's first Newton iteration to its
-    convergence; throughput is time steps per wall second from the first
-    arrival to the last result."""
+    rate, every request in the FP32 form with batched solves, against the same
+    requests solved one at a time with the plain FP64 path.  Per-step latency is
+    the wall time from a step's first Newton iteration to its convergence;
+    throughput is time steps per wall second from the first arrival to the last
+    result."""
     import mafem as M
     cu = Cudart()
     reqs = serve_requests(M, wl)
@@ -491,19 +499,22 @@ def run_serving(wl=SERVE):
             s.upload(x0, c0)
             cu.sync()
             h0 = time.perf_counter()
-            try:
-                s.run_analysis([dt] * steps)
-                ok = True
-            except M.NewtonNotConverged:
-                ok = False
+            ok, t = True, 0.0
+            for k in range(steps):
+                t += dt
+                s.set_dirichlet_scale(min(1.0, (k + 1) / wl["ramp"]))
+                s.predict(dt)
+                try:
+                    s.time_step_resident(t, dt)
+                except M.NewtonNotConverged:
+                    ok = False
+                    break
             cu.sync()
             seq_s += time.perf_counter() - h0
             ref.append(s.download() if ok else None)
         total_steps += steps
     out = {"workload": wl["name"], "requests": len(reqs),
-           "steps_per_request": "U{%d..%d} scaled by %g (bounded sample)" % (wl["steps"][0], wl["steps"][1],
-                                                                               wl["step_scale"]),
-           "time_steps": total_steps,
+           "steps_per_request": "U{%d..%d}" % (wl["steps"][0], wl["steps"][1]), "time_steps": total_steps,
            "plain_fp64_one_at_a_time": {"value": total_steps / seq_s, "unit": "time-steps/s"}, "rates": {}}
     for rate in wl["rates"]:
         with M.Server() as srv:
@@ -515,10 +526,8 @@ def run_serving(wl=SERVE):
                 now = time.perf_counter() - t0
                 while nxt < len(reqs) and reqs[nxt][5] / rate <= now:
                     p, mesh, x0, c0, steps, _ = reqs[nxt]
-                    fits = mesh.half_bw <= 600  # the one-CTA FP32 solve's shared-memory limit, with margin
-                    ids[nxt] = srv.submit(mesh, p, x0, c0, steps, dt,
-                                          precision=M.FP32_REFINE if fits else M.PLAIN_FP64,
-                                          refine_tol=FP32_REFINE_TOL)
+                    ids[nxt] = srv.submit(mesh, p, x0, c0, steps, dt, precision=M.FP32_REFINE,
+                                          refine_tol=FP32_REFINE_TOL, ramp_steps=wl["ramp"])
                     nxt += 1
                 active, pending = srv.round()
                 for k, rid in ids.items():
@@ -549,6 +558,88 @@ def run_serving(wl=SERVE):
     return out
 
 
+# The precision workload: one 64 x 64 ALEVB patch (66 x 66 control points,
+# 33 262 unknowns, half bandwidth 1055), flat start, dt 0.005: the tether
+# pulled at the centre for 40 steps (speed ramped from 0 to its final value),
+# then translated for 100 steps -- the pull nodes' vz (and vmz) taken back to 0
+# and vx (and vmx) brought to 0.3 L / (100 dt) over the first 10 of them --
+# through the state's Dirichlet entries, the state the reference's restart
+# reads (src/MembraneAleFem.jl:75-107, Bc.jl:227-243).  The FP32 form (FP32
+# tangent and LU, FP64 refinement to 1e-10 relative, FP64 residual, norm and
+# geometry update) and the plain FP64 path step side by side from the same
+# state; the relative error of positions, velocities and tensions is taken
+# after every step.
+PREC64 = dict(name="precision workload: ALEVB tether pull then translation, 64x64 graded patch (66x66 control "
+                   "points), centre pull, flat start, dt 0.005",
+              n=64, motion=5, dt=0.005, pull_steps=40, trans_steps=100, trans_ramp=10, pull_speed=2.0,
+              trans_dist=0.3, refine_tol=1e-10)
+
+
+def _pull_state(mesh, cps, vz, vx):
+    """The pull nodes' Dirichlet entries of the state: vz (and vmz) = vz, vx (and vmx) = vx."""
+    for u, node, _ in mesh.dirichlet():
+        if u in (3, 6):  # vz, vmz
+            cps[node - 1, mesh.dofs[u - 1] - 1] = vz
+            cps[node - 1, mesh.dofs[u - 3] - 1] = vx  # vx, vmx
+    return cps
+
+
+def run_precision64(wl=PREC64):
+    """Per-step relative error of the FP32 form against plain FP64 on the precision
+    workload, and both forms' time-steps/s (device time of each Newton loop)."""
+    import mafem as M
+    p = M.Params(motion=wl["motion"], scenario=M.F_PULL, num1el=wl["n"], num2el=wl["n"], length=1.0,
+                 pull_speed=wl["pull_speed"], pull_centre=1)
+    mesh = M.Mesh(p)
+    _, x0, c0 = M.prepare_input(p, mesh)
+    dt, npull, ntr = wl["dt"], wl["pull_steps"], wl["trans_steps"]
+    vtr = wl["trans_dist"] / (ntr * dt)
+    lam = mesh.dofs[6] - 1
+    vel = [d for d in range(mesh.ndf) if d != lam]
+    errs, ms64, ms32, it32, sw32, fail = [], 0.0, 0.0, 0, 0, None
+    with M.Solver(mesh, p, M.PLAIN_FP64) as s64, M.Solver(mesh, p, M.FP32_REFINE) as s32:
+        s32.set_refinement(30, wl["refine_tol"])
+        s64.upload(x0, c0)
+        s32.upload(x0, c0)
+        t = 0.0
+        for k in range(npull + ntr):
+            for s in (s64, s32):
+                if k < npull:
+                    s.set_dirichlet_scale((k + 1) / npull)
+                else:
+                    a = min(1.0, (k - npull + 1) / wl["trans_ramp"])
+                    xs, cs = s.download()
+                    s.upload(xs, _pull_state(mesh, cs, (1 - a) * wl["pull_speed"], a * vtr))
+            t += dt
+            try:
+                s64.predict(dt)
+                ms64 += s64.time_step_resident(t, dt)["ms_total"]
+                s32.predict(dt)
+                st = s32.time_step_resident(t, dt)
+            except (M.MafemError, M.NewtonNotConverged) as e:
+                fail = (k, repr(e)[:160])
+                break
+            ms32 += st["ms_total"]
+            it32 += st["newton_iters"]
+            sw32 += st["refine_iters"]
+            x1, c1 = s64.download()
+            x2, c2 = s32.download()
+            errs.append((_relmax(x2, x1), _relmax(c2[:, vel], c1[:, vel]), _relmax(c2[:, lam], c1[:, lam])))
+        x_pull = s64.pull_position().tolist()
+    e = np.array(errs) if errs else np.zeros((1, 3))
+    n = len(errs)
+    return {"workload": wl["name"], "steps": n, "pull_steps": npull, "trans_steps": ntr,
+            "final_pull_speed": wl["pull_speed"], "translation_speed": vtr, "failed_at": fail,
+            "x_pull_after": x_pull,
+            "fp32_refine": {"value": n / (ms32 / 1e3) if ms32 else None, "unit": "time-steps/s",
+                            "newton_iters_per_step": it32 / max(n, 1), "refine_sweeps_per_step": sw32 / max(n, 1),
+                            "refine_tol": wl["refine_tol"]},
+            "plain_fp64": {"value": n / (ms64 / 1e3) if ms64 else None, "unit": "time-steps/s"},
+            "rel_err_vs_plain_fp64": {"max_xms": float(e[:, 0].max()), "max_velocities": float(e[:, 1].max()),
+                                      "max_lambda": float(e[:, 2].max()),
+                                      "per_step_max": [float(v) for v in e.max(axis=1)]}}
+
+
 def run_case(case):
     """Small fixed cases for ncu captures (no bench line): `fp32-patch32` is one
     batched FP32-form step of the bench's 32 x 32 ALEVB patch alone;
@@ -573,8 +664,11 @@ def run_case(case):
         dt = BATCH["dt"] if case != "fp32-patch32" else WORKLOAD["dt"]
         with M.Batch(solvers) as b:
             t = 0.0
-            for _ in range(nsteps):
+            for k in range(nsteps):
                 t += dt
+                if case != "fp32-patch32":  # the batching workload's ramped pull
+                    for s in solvers:
+                        s.set_dirichlet_scale(min(1.0, (k + 1) / BATCH["ramp"]))
                 h0 = time.perf_counter()
                 status, st = b.step(t, dt)
                 out.append({"ms": (time.perf_counter() - h0) * 1e3, "status": status,
@@ -657,6 +751,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-form measurement")
     ap.add_argument("--batch-steps", type=int, default=0, help="time steps of the batching workload (0: its 30)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 64 x 64 precision measurement")
     ap.add_argument("--case", choices=["fp32-patch32", "fp32-batch16"],
                     help="run a small profiling case instead of the bench (prints no bench line)")
     args = ap.parse_args()
@@ -734,6 +829,8 @@ def main():
         line["batched"] = run_batched(args.batch_steps)
     if rank == 0 and not args.no_serve:
         line["serving"] = run_serving()
+    if rank == 0 and not args.no_precision:
+        line["precision_64"] = run_precision64()
     if rank == 0 and not args.no_cpu_baseline:
         ref = {}
         line["cpu_baseline"] = cpu_baseline(warmup=args.warmup, max_steps=2, state_out=ref)
@@ -743,6 +840,15 @@ def main():
         except Exception as e:  # the accuracy report must not cost the bench line
             line["rel_err_vs_oracle"] = {"error": repr(e)[:300]}
     if rank == 0:
+        # the benchmark spec's figures, last, so that the tail of the line shows them
+        b = line.get("batched")
+        if b:
+            line["north_star"] = {
+                "batched_fp32_patch_steps_per_s": b["value"],
+                "plain_fp64_one_at_a_time_patch_steps_per_s": b["one_at_a_time"]["value"],
+                "ratio": b["speedup_vs_plain_fp64_one_at_a_time"], "target_ratio": 10.0,
+                "p99_batch_step_ms": b["p99_batch_step_ms"], "max_rel_err_vs_plain_fp64": b["max_rel_err_vs_plain_fp64"],
+                "failed_patch_steps": b["failed_patch_steps"], "patches": b["patches"], "steps": b["steps"]}
         print(json.dumps(line))
 
 
