@@ -117,3 +117,25 @@ def test_admission_by_footprint():
         with pytest.raises(M.MafemError) as e:
             srv.submit(mesh, p, xms, cps, 2, DT)
         assert e.value.code == M.ERR_ADMISSION
+
+
+def test_ramped_request_matches_the_oracle():
+    """A request with ramp_steps: before its step k the server scales the pull's
+    Dirichlet values by min(1, (k + 1) / ramp_steps) -- the state edit the
+    oracle makes here by hand before each of its steps."""
+    ramp, steps = 4, 3
+    p, q, mesh, xms, cps = _req(M.ALEVB, 10, 11)
+    with M.Server() as srv:
+        rid = srv.submit(mesh, p, xms, cps, steps, DT, precision=M.FP32_REFINE, ramp_steps=ramp)
+        res = _drain(srv, [rid])[0]
+    assert res[0] == M.OK
+    om = O.Mesh(q)
+    x, c = xms.copy(order="F"), cps.copy(order="F")
+    t = 0.0
+    for k in range(steps):
+        for u, node, v in om.dirichlet():
+            c[node - 1, om.dofs[u - 1] - 1] = min(1.0, (k + 1) / ramp) * v
+        t += DT
+        om.update_xms(x, c, DT)
+        om.time_step(x, c, t, DT, nthreads=4)
+    assert rel(res[1], x) < 1e-8 and rel(res[2], c) < 1e-8
