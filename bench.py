@@ -562,7 +562,7 @@ def run_serving(wl=SERVE):
 # 33 262 unknowns, half bandwidth 1055), flat start, dt 0.005: the tether
 # pulled at the centre for 40 steps (speed ramped from 0 to its final value),
 # then translated for 100 steps -- the pull nodes' vz (and vmz) taken back to 0
-# and vx (and vmx) brought to 0.3 L / (100 dt) over the first 10 of them --
+# and vx (and vmx) brought to 0.3 L / (100 dt) over the first 50 of them --
 # through the state's Dirichlet entries, the state the reference's restart
 # reads (src/MembraneAleFem.jl:75-107, Bc.jl:227-243).  The FP32 form (FP32
 # tangent and LU, FP64 refinement to 1e-10 relative, FP64 residual, norm and
@@ -571,7 +571,7 @@ def run_serving(wl=SERVE):
 # after every step.
 PREC64 = dict(name="precision workload: ALEVB tether pull then translation, 64x64 graded patch (66x66 control "
                    "points), centre pull, flat start, dt 0.005",
-              n=64, motion=5, dt=0.005, pull_steps=40, trans_steps=100, trans_ramp=10, pull_speed=2.0,
+              n=64, motion=5, dt=0.005, pull_steps=40, trans_steps=100, trans_ramp=50, pull_speed=0.5,
               trans_dist=0.3, refine_tol=1e-10)
 
 

@@ -1184,19 +1184,22 @@ extern "C" int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas) {
   return h->pers.max_grid > 0 ? h->pers.grid : h->bwd_grid;
 }
 
-// Order of a round's batched solves: the patches factored on two-CTA clusters
-// (more trailing columns than one chunk) first, then the single-CTA ones, each
-// group largest first.  Returns the number of cluster patches.
-static int order_patch_jobs(std::vector<mafem_handle*>& hv, std::vector<int>& idx) {
-  auto big = [&](int k) { return hv[k]->blk.kuf > patch_chunk_cols(); };
+// Order of a round's batched solves: the patches factored on four-CTA
+// clusters first, then those on two-CTA clusters, then the single-CTA ones,
+// each group largest first.  Returns the size of the first group in *n4 and of
+// the second in *n2.
+static void order_patch_jobs(std::vector<mafem_handle*>& hv, std::vector<int>& idx, int* n4, int* n2) {
+  auto nr = [&](int k) { return patch_cluster_ctas(hv[k]->blk.kuf); };
   auto cost = [&](int k) { return (double)hv[k]->blk.npan() * hv[k]->L.kl * hv[k]->blk.kuf; };
   std::sort(idx.begin(), idx.end(), [&](int a, int b) {
-    if (big(a) != big(b)) return big(a);
+    if (nr(a) != nr(b)) return nr(a) > nr(b);
     return cost(a) > cost(b);
   });
-  int nbig = 0;
-  for (int k : idx) nbig += big(k) ? 1 : 0;
-  return nbig;
+  *n4 = *n2 = 0;
+  for (int k : idx) {
+    *n4 += nr(k) == 4 ? 1 : 0;
+    *n2 += nr(k) == 2 ? 1 : 0;
+  }
 }
 
 struct mafem_batch {
@@ -1323,7 +1326,8 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
         pj.push_back(i);
     }
     if (!pj.empty()) {
-      const int nbig = order_patch_jobs(b->hs, pj);
+      int n4 = 0, n2 = 0;
+      order_patch_jobs(b->hs, pj, &n4, &n2);
       // one launch serves every patch: the strictest tolerance and the largest sweep cap among them
       b->max_sweeps = 1;
       b->tol = 1.0;
@@ -1337,7 +1341,7 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
       }
       cudaError_t e = cudaMemcpyAsync(b->d_order, b->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice, b->bst);
       if (e == cudaSuccess)
-        e = patch_solve(b->d_jobs, b->d_order, nbig, (int)pj.size(), b->smem_f, b->smem_r, b->max_sweeps, b->tol,
+        e = patch_solve(b->d_jobs, b->d_order, n4, n2, (int)pj.size(), b->smem_f, b->smem_r, b->max_sweeps, b->tol,
                         b->bst, b->bst2, b->efork, b->ejoin);
       if (e == cudaSuccess) e = cudaEventRecord(b->bev, b->bst);
       for (int i : pj) {
@@ -1617,7 +1621,8 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
   if (!pj.empty() && lane) {
     std::vector<mafem_handle*> hv(s->active.size());
     for (size_t k = 0; k < s->active.size(); ++k) hv[k] = s->active[k]->h;
-    const int nbig = order_patch_jobs(hv, pj);
+    int n4 = 0, n2 = 0;
+    order_patch_jobs(hv, pj, &n4, &n2);
     size_t smf = 0, smr = 0;
     int max_sw = 1;
     double tol = 1.0;
@@ -1633,7 +1638,7 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
     cudaError_t e = cudaMemcpyAsync(lane->d_order, lane->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice,
                                     lane->st);
     if (e == cudaSuccess)
-      e = patch_solve(s->d_jobs, lane->d_order, nbig, (int)pj.size(), smf, smr, max_sw, tol, lane->st, lane->st2,
+      e = patch_solve(s->d_jobs, lane->d_order, n4, n2, (int)pj.size(), smf, smr, max_sw, tol, lane->st, lane->st2,
                       lane->efork, lane->ejoin);
     if (e == cudaSuccess) e = cudaEventRecord(lane->done, lane->st);
     lane->busy = true;
@@ -1866,7 +1871,7 @@ extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, 
   cudaEventCreate(&e2);
   const int dyn = patch_solve_setup();
   cudaEventRecord(e0, h->st);
-  const int nr = h->blk.kuf > patch_chunk_cols() ? 2 : 1;  // as a batch would run it
+  const int nr = patch_cluster_ctas(h->blk.kuf);  // as a batch would run it
   patch_solve_stage(d_job, d_ord, 1, nr, patch_factor_smem(h->L.kl), 0, 0, 0.0, h->st);
   cudaEventRecord(e1, h->st);
   patch_solve_stage(d_job, d_ord, 1, 1, 0, patch_refine_smem(h->L.n), h->max_refine, h->refine_tol, h->st);

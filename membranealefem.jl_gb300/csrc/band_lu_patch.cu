@@ -234,10 +234,10 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
       // A21 (rows w .. R-1 of the panel) split into TF32 hi / lo parts, written
       // to the patch's split-A21 buffer as 8 k-quad planes [k/4][row][k%4]
       // (hi rows 0 .. nrp-1, lo rows nrp .. 2 nrp-1), rows past the panel and
-      // columns k >= w zero; each rank of a cluster writes half of the rows
+      // columns k >= w zero; each rank of a cluster writes its share of the rows
       const int nr = R - w;
       const int nrt = (nr + kMT - 1) / kMT * kMT;
-      const int rlo = NR > 1 ? rank * (nrt / 2) : 0, rhi = NR > 1 && rank == 0 ? nrt / 2 : nrt;
+      const int rlo = rank * (nrt / NR), rhi = rank + 1 == NR ? nrt : (rank + 1) * (nrt / NR);
       for (int idx = tid - 64; idx < (rhi - rlo) * 8; idx += kPT - 64) {
         const int r = rlo + idx % (rhi - rlo), kq = idx / (rhi - rlo);
         float4 h, l;
@@ -787,10 +787,13 @@ int patch_solve_setup() {
   const int dyn = cap - 20 * 1024;  // room for the kernels' static shared memory (refine: ~19 KB)
   if (cudaFuncSetAttribute(patch_factor_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(patch_factor_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
+      cudaFuncSetAttribute(patch_factor_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess ||
       cudaFuncSetAttribute(patch_refine_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
     return 0;
   return dyn;
 }
+
+int patch_cluster_ctas(int kuf) { return kuf > 2 * kNCH ? 4 : kuf > kNCH ? 2 : 1; }
 
 static cudaError_t launch_factor(const PatchJob* d_jobs, const int* d_order, int njobs, int nr, size_t smem,
                                  cudaStream_t st) {
@@ -800,18 +803,19 @@ static cudaError_t launch_factor(const PatchJob* d_jobs, const int* d_order, int
     return cudaGetLastError();
   }
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(2 * njobs));
+  cfg.gridDim = dim3((unsigned)(nr * njobs));
   cfg.blockDim = dim3(kPT);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.x = (unsigned)nr;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, patch_factor_kernel<2>, d_jobs, d_order);
+  return nr == 4 ? cudaLaunchKernelEx(&cfg, patch_factor_kernel<4>, d_jobs, d_order)
+                 : cudaLaunchKernelEx(&cfg, patch_factor_kernel<2>, d_jobs, d_order);
 }
 
 cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int njobs, int nr, size_t smem_factor,
@@ -825,22 +829,30 @@ cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int nj
   return cudaGetLastError();
 }
 
-cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int nbig, int njobs, size_t smem_factor,
+cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int n4, int n2, int njobs, size_t smem_factor,
                         size_t smem_refine, int max_sweeps, double tol, cudaStream_t st, cudaStream_t st2,
                         cudaEvent_t ev_fork, cudaEvent_t ev_join) {
   if (njobs <= 0) return cudaSuccess;
   cudaError_t e = cudaSuccess;
-  const int nsmall = njobs - nbig;
-  if (nsmall > 0 && nbig > 0) {  // the single-CTA patches beside the clusters, on the second stream
+  // the groups in launch order: four-CTA clusters, two-CTA clusters, single
+  // CTAs; the first non-empty group on st, the others one after the other on
+  // st2 beside it (their chains are the shorter ones)
+  const int cnt[3] = {n4, n2, njobs - n4 - n2}, nrs[3] = {4, 2, 1};
+  int first = 0;
+  while (first < 3 && cnt[first] == 0) ++first;
+  const bool fork = cnt[first] < njobs;
+  if (fork) {
     e = cudaEventRecord(ev_fork, st);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(st2, ev_fork, 0);
-    if (e == cudaSuccess) e = launch_factor(d_jobs, d_order, nbig, 2, smem_factor, st);
-    if (e == cudaSuccess) e = launch_factor(d_jobs, d_order + nbig, nsmall, 1, smem_factor, st2);
-    if (e == cudaSuccess) e = cudaEventRecord(ev_join, st2);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_join, 0);
-  } else {
-    e = launch_factor(d_jobs, d_order, njobs, nbig > 0 ? 2 : 1, smem_factor, st);
   }
+  int off = 0;
+  for (int g = 0; g < 3 && e == cudaSuccess; ++g) {
+    if (cnt[g] == 0) continue;
+    e = launch_factor(d_jobs, d_order + off, cnt[g], nrs[g], smem_factor, g == first ? st : st2);
+    off += cnt[g];
+  }
+  if (fork && e == cudaSuccess) e = cudaEventRecord(ev_join, st2);
+  if (fork && e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_join, 0);
   if (e != cudaSuccess) return e;
   patch_refine_kernel<<<njobs, kRT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
   return cudaGetLastError();

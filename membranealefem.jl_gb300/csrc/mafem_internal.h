@@ -272,18 +272,20 @@ size_t patch_factor_smem(int kl);
 size_t patch_refine_smem(int64_t n);
 // Sets the kernels' shared-memory limits; returns the dynamic bytes available (0: unusable).
 int patch_solve_setup();
-// Factor and solve every job listed in d_order[0 .. njobs): one CTA per job.
-// Trailing columns per chunk of the factorisation; a patch with more (kuf >
-// this) is factored on a two-CTA cluster, each CTA updating every other chunk.
+// Trailing columns per chunk of the factorisation (at most).
 int patch_chunk_cols();
-// The factor kernel alone (smem_refine == 0; nr = CTAs per patch, 1 or 2) or the
-// refine kernel alone (smem_factor == 0).
+// CTAs that factor a patch with kuf trailing columns: 4 (a cluster, one chunk
+// per CTA) above two chunks, 2 above one chunk, else 1.
+int patch_cluster_ctas(int kuf);
+// The factor kernel alone (smem_refine == 0; nr = CTAs per patch, 1, 2 or 4) or
+// the refine kernel alone (smem_factor == 0).
 cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int njobs, int nr, size_t smem_factor,
                               size_t smem_refine, int max_sweeps, double tol, cudaStream_t st);
-// Factor and solve the jobs d_order[0 .. njobs): the first nbig on two-CTA
-// clusters (on st), the others one CTA each (on st2, forked from and joined to
-// st with ev_fork / ev_join); then the refinement of all of them on st.
-cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int nbig, int njobs, size_t smem_factor,
+// Factor and solve the jobs d_order[0 .. njobs): the first n4 on four-CTA
+// clusters, the next n2 on two-CTA clusters, the rest one CTA each -- the first
+// non-empty group on st, the others after one another on st2 (forked from and
+// joined to st with ev_fork / ev_join); then the refinement of all on st.
+cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int n4, int n2, int njobs, size_t smem_factor,
                         size_t smem_refine, int max_sweeps, double tol, cudaStream_t st, cudaStream_t st2,
                         cudaEvent_t ev_fork, cudaEvent_t ev_join);
 }  // namespace mafem
