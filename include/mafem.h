@@ -17,8 +17,10 @@
  *    reference @asserts); < 0 = usage, CUDA or memory error.  The message of
  *    the last failure is available from mafem_last_error().
  *  - A handle is used by one host thread at a time.  Handles are independent.
- *  - No function allocates device memory after mafem_create(); every device
- *    buffer of a handle is allocated there and freed by mafem_destroy().
+ *  - No function allocates device memory after mafem_create() (the
+ *    diagnostic mafem_trace_patch_solve excepted: it allocates and frees its
+ *    trace buffer); every device buffer of a handle is allocated there and
+ *    freed by mafem_destroy().
  */
 #ifndef MAFEM_H
 #define MAFEM_H
@@ -327,7 +329,9 @@ int mafem_trace_factor(mafem_handle* h, double time, double dt, int64_t* out, in
  * the factor and refine kernels' event times in ns, then 4 stamps per
  * refinement sweep for up to 32 sweeps (start, substitutions done, x updated,
  * residual done; 0 where not reached), then 16 phase sums (ns) of the first
- * sweep's substitutions (see patch_lu_solve).  cap >= 6 npan + 146.
+ * sweep's substitutions (see patch_lu_solve), then the relative residual
+ * |r - A0 x| / |r| after each sweep (up to 32, as double bit patterns), then
+ * the refinement's status and sweep count.  cap >= 6 npan + 182.
  * Returns npan, or MAFEM_ERR_UNSUPPORTED if the handle cannot use that solve. */
 int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap);
 

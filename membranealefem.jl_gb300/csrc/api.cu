@@ -1849,8 +1849,9 @@ extern "C" int mafem_trace_factor(mafem_handle* h, double time, double dt, int64
 extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, int64_t* out, int64_t cap) {
   if (!h || !out || !h->patch_ok) return MAFEM_ERR_UNSUPPORTED;
   const int npan = h->blk.npan();
-  const int64_t ntr = 6LL * npan + 4 * 32 + 16;  // factor stamps, 4 per refinement sweep (up to 32), 16 phase sums
-  if (cap < ntr + 2) return MAFEM_ERR_ARG;  // 6 npan + 146
+  // factor stamps, 4 per refinement sweep (up to 32), 16 phase sums, 32 relative residuals
+  const int64_t ntr = 6LL * npan + 4 * 32 + 16 + 32;
+  if (cap < ntr + 4) return MAFEM_ERR_ARG;  // 6 npan + 182
   long long* d_tr = nullptr;
   PatchJob* d_job = nullptr;
   int* d_ord = nullptr;
@@ -1885,7 +1886,11 @@ extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, 
   for (int64_t k = 0; k < 6LL * npan; ++k) out[k] = tr[(size_t)k];
   out[6 * npan] = (int64_t)(mf * 1e6);
   out[6 * npan + 1] = (int64_t)(mr * 1e6);
-  for (int64_t k = 0; k < 4 * 32 + 16; ++k) out[6 * npan + 2 + k] = tr[(size_t)(6 * npan + k)];
+  for (int64_t k = 0; k < 4 * 32 + 16 + 32; ++k) out[6 * npan + 2 + k] = tr[(size_t)(6 * npan + k)];
+  int st2[2] = {0, 0};  // the refinement's status and sweeps
+  CK(cudaMemcpy(st2, h->d_info + 2, sizeof st2, cudaMemcpyDeviceToHost));
+  out[ntr + 2] = st2[0];
+  out[ntr + 3] = st2[1];
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaEventDestroy(e2);

@@ -731,6 +731,8 @@ __global__ void __launch_bounds__(kRT, 1) patch_refine_kernel(const PatchJob* __
       }
       rn = patch_residual(J, xs, red);  // block_sum orders the x / xs writes before it
       stamp(trk, 3);
+      if (tr && tid == 0 && k < kTraceSweeps)  // trace: the residual after each sweep, relative to |r0|
+        tr[4 * kTraceSweeps + 16 + k] = __double_as_longlong(rn / r0);
       if (!isfinite(rn)) {
         status = MAFEM_NAN_DETECTED;
         break;

@@ -478,13 +478,15 @@ class Solver:
         """FP32 form: per-panel phase stamps (ns) of the batched one-CTA factorisation
         of the resident state, as an (npan, 6) array, and the factor / refine kernel
         times in ms."""
-        cap = 6 * 4096 + 146
+        cap = 6 * 4096 + 182
         buf = (C.c_int64 * cap)()
         npan = lib().mafem_trace_patch_solve(self.h, time, dt, buf, cap)
         _raise(0 if npan >= 0 else npan, self.h)
-        a = np.ctypeslib.as_array(buf)[: 6 * npan + 146].copy()
+        a = np.ctypeslib.as_array(buf)[: 6 * npan + 182].copy()
         self.last_refine_trace = a[6 * npan + 2: 6 * npan + 130].reshape(32, 4)
-        self.last_solve_phases = a[6 * npan + 130:]
+        self.last_solve_phases = a[6 * npan + 130: 6 * npan + 146]
+        self.last_refine_residuals = a[6 * npan + 146: 6 * npan + 178].view(np.float64)
+        self.last_refine_status = (int(a[6 * npan + 180]), int(a[6 * npan + 181]))
         return a[: 6 * npan].reshape(npan, 6), a[6 * npan] / 1e6, a[6 * npan + 1] / 1e6
 
     def solve_band(self, band, rhs):
