@@ -133,6 +133,7 @@ struct mafem_handle {
   double* d_dir_val = nullptr;          // their values
   int* d_rstate = nullptr;              // refinement state {done, sweeps, status} (FP32 form)
   int* h_rstate = nullptr;              // its pinned host copy
+  bool no_async = false;                // the next iteration waits for its solve (a redo)
   std::unique_ptr<StateWriter> writer;  // state files, created by the first write
   double* d_snap = nullptr;             // device snapshots: nsnap x [xms | cps]
   int nsnap = 0;
@@ -837,6 +838,45 @@ static int check_info(mafem_handle* h) {
   return MAFEM_OK;
 }
 
+// FP32 form: FP64 iterative refinement of K x = rhs with the FP32 factors, run
+// on the device with a device-side stopping test.  refine_begin sets x = 0,
+// res = rhs and the handle's refinement state {done, sweeps, status};
+// refine_sweeps enqueues `count` sweeps (d = LU^-1 res, x += d, res = rhs - A0 x
+// in FP64), each ending with a check kernel that updates the state; the kernels
+// of a sweep read `done` first and return at once once it is set.  The stopping
+// rule: |rhs - A0 x| <= tol |rhs| (this solver is also the fallback of the
+// batched solve when that one stalls on an ill-conditioned tangent, where a
+// small correction says nothing about the error of x); stall after the fourth
+// sweep if |r| > |r_prev| / 2; max_refine sweeps at most.
+static void refine_begin(mafem_handle* h, const double* rhs_dev) {
+  const int64_t n = h->nmdf;
+  cudaMemsetAsync(h->d_x, 0, n * sizeof(double), h->st);
+  launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part, h->d_out + 4,
+                              h->st);  // res = rhs, |rhs|
+  launch_refine_init(h->d_out + 4, h->d_rstate, h->d_out + 12, h->st);
+  h->launches += 3;
+}
+static void refine_sweeps(mafem_handle* h, const double* rhs_dev, int count) {
+  const int64_t n = h->nmdf;
+  int* gate = h->d_rstate;
+  for (int k = 0; k < count; ++k) {
+    launch_copy_gated(n, h->d_res, h->d_dx, gate, h->st);
+    if (h->last_blk) {
+      blk_fwd_solve<float>(h, h->d_dx, gate);
+      blk_back_solve<float>(h, h->d_dx, gate);
+    } else {  // full partial pivoting: single-CTA substitutions (ungated: they only rewrite d_dx)
+      band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
+      band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
+      h->launches += 2;
+    }
+    launch_axpy_norms(n, h->d_dx, h->d_x, h->d_part, h->d_out + 8, h->st, gate);
+    launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part, h->d_out + 3,
+                                h->st, gate);
+    launch_refine_check(h->d_out + 3, h->d_out + 8, gate, h->d_out + 12, h->refine_tol, h->max_refine, h->st);
+    h->launches += 6;
+  }
+}
+
 // Solve K x = rhs (rhs in d_x on entry for the plain form; x in d_x on exit).
 // Factors the band if needed.  Returns the number of refinement sweeps in *sweeps.
 static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps) {
@@ -870,43 +910,13 @@ static int factor_and_solve(mafem_handle* h, const double* rhs_dev, int* sweeps)
     if (rc) return rc;
   }
   cudaEventRecord(h->ev[2], h->st);
-  // The sweeps run on the device with a device-side stopping test: every sweep
-  // (d = LU^-1 res, x += d, res = rhs - A0 x in FP64) ends with a check kernel
-  // that sets the handle's refinement state {done, sweeps, status}; the
-  // kernels of later sweeps see `done` and return at once.  Sweeps are
-  // enqueued kRefineChunk at a time and the host reads the state once per
-  // chunk -- one wait where the solve stops within a chunk -- instead of once
-  // per sweep.  The stopping rule: |rhs - A0 x| <= tol |rhs| (this solver is
-  // also the fallback of the batched solve when that one stalls on an
-  // ill-conditioned tangent, where a small correction says nothing about the
-  // error of x); stall after the fourth sweep if |r| > |r_prev| / 2.
   constexpr int kRefineChunk = 3;
-  int* gate = h->d_rstate;
-  CK(cudaMemsetAsync(h->d_x, 0, n * sizeof(double), h->st));
-  launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part, h->d_out + 4,
-                              h->st);  // res = rhs, |rhs|
-  launch_refine_init(h->d_out + 4, gate, h->d_out + 12, h->st);
-  h->launches += 3;
+  refine_begin(h, rhs_dev);
   int state[3] = {0, 0, MAFEM_OK};
   for (int chunk = 0; !state[0]; ++chunk) {
-    for (int k = 0; k < kRefineChunk; ++k) {
-      launch_copy_gated(n, h->d_res, h->d_dx, gate, h->st);
-      if (h->last_blk) {
-        blk_fwd_solve<float>(h, h->d_dx, gate);
-        blk_back_solve<float>(h, h->d_dx, gate);
-      } else {  // full partial pivoting: single-CTA substitutions (ungated: they only rewrite d_dx)
-        band_forward<float, double>((const float*)h->d_band, h->L, h->d_perm, h->rmax, h->d_dx, h->st);
-        band_backward<float, double>((const float*)h->d_band, h->L, h->d_dx, h->st);
-        h->launches += 2;
-      }
-      launch_axpy_norms(n, h->d_dx, h->d_x, h->d_part, h->d_out + 8, h->st, gate);
-      launch_band_residual<float>((const float*)h->d_band0, h->L, h->d_x, rhs_dev, h->d_res, h->d_part,
-                                  h->d_out + 3, h->st, gate);
-      launch_refine_check(h->d_out + 3, h->d_out + 8, gate, h->d_out + 12, h->refine_tol, h->max_refine, h->st);
-      h->launches += 6;
-    }
+    refine_sweeps(h, rhs_dev, kRefineChunk);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(h->h_rstate, gate, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(h->h_rstate, h->d_rstate, 3 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     std::memcpy(state, h->h_rstate, sizeof state);
     if (!state[0] && state[1] >= h->max_refine) break;  // cannot happen: the check stops at max_sweeps
@@ -995,6 +1005,11 @@ static bool residual_finite(mafem_handle* h) {
   return std::isfinite(nr[0]);
 }
 
+// Refinement sweeps enqueued per Newton iteration of the FP32 form when the
+// iteration runs without a host wait (the refinement stops within 2-5 sweeps
+// on the benchmark tangents at the default tolerance).
+constexpr int kAsyncSweeps = 8;
+
 // ---- a time step as step_begin / iter_enqueue / iter_finish: mafem_time_step
 // runs them for one handle, mafem_batch_step interleaves many handles ----
 
@@ -1021,12 +1036,25 @@ static int iter_enqueue(mafem_handle* h) {
   if (rc) return rc;
   cudaEventRecord(h->ev[1], h->st);
   h->ss_sweeps = 0;
-  h->ss_async = h->precision == MAFEM_PLAIN_FP64 && h->use_blk && h->lu_path != MAFEM_LU_FULL;
-  if (h->ss_async) {
+  h->ss_async = h->use_blk && h->lu_path != MAFEM_LU_FULL && !h->no_async;
+  if (h->ss_async && h->precision == MAFEM_PLAIN_FP64) {
     CK(cudaMemcpyAsync(h->d_x, h->d_r, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
     if ((rc = factor_enqueue(h, h->d_x)) != MAFEM_OK) return rc;
     cudaEventRecord(h->ev[2], h->st);
     blk_back_solve<double>(h, h->d_x);
+  } else if (h->ss_async) {
+    // FP32 form without a host wait: factor, then a fixed number of gated
+    // refinement sweeps (those after convergence return at once); a node block
+    // without a usable pivot, or a refinement that did not converge within
+    // them, leaves the state unchanged and iter_finish redoes or reports it
+    CK(cudaMemcpyAsync(h->d_band0, h->d_band, (size_t)h->L.ldb * n * sizeof(float), cudaMemcpyDeviceToDevice,
+                       h->st));
+    if ((rc = factor_enqueue(h, nullptr)) != MAFEM_OK) return rc;
+    cudaEventRecord(h->ev[2], h->st);
+    refine_begin(h, h->d_r);
+    refine_sweeps(h, h->d_r, std::min(h->max_refine, kAsyncSweeps));
+    launch_refine_seal(h->d_rstate, h->st);
+    h->launches += 1;
   } else if ((rc = factor_and_solve(h, h->d_r, &h->ss_sweeps)) != MAFEM_OK) {
     // a singular or stalled solve of a non-finite system: report the NaN (the
     // residual itself is not finite), as the other paths do
@@ -1037,11 +1065,14 @@ static int iter_enqueue(mafem_handle* h) {
     return rc;
   }
   cudaEventRecord(h->ev[3], h->st);
-  launch_newton_update(h->P, h->pp, h->ss_dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st, h->d_info, h->d_info + 1);
+  const bool fp32_async = h->ss_async && h->precision != MAFEM_PLAIN_FP64;
+  launch_newton_update(h->P, h->pp, h->ss_dt, h->d_x, h->d_r, h->d_part, h->d_out, h->st, h->d_info,
+                       h->d_info + 1, fp32_async ? h->d_rstate + 3 : nullptr);
   h->launches += 2;
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(h->h_out, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CK(cudaMemcpyAsync(h->h_out + 5, h->d_info, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  if (fp32_async) CK(cudaMemcpyAsync(h->h_rstate, h->d_rstate, 4 * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   cudaEventRecord(h->ev[4], h->st);
   return MAFEM_OK;
 }
@@ -1132,6 +1163,28 @@ static int iter_finish(mafem_handle* h) {
     if (rc) return rc;
     CK(cudaEventSynchronize(h->ev[4]));
     accum_times(h);
+  }
+  if (h->ss_async && h->precision != MAFEM_PLAIN_FP64 && info[0] == 0 && info[1] == 0) {
+    int rs[4];
+    std::memcpy(rs, h->h_rstate, sizeof rs);
+    h->ss_sweeps = rs[1];
+    if (rs[3]) {  // the update was skipped: the refinement did not succeed within its sweeps
+      if (rs[2] == MAFEM_NAN_DETECTED) {
+        h->err = "non-finite refinement residual or correction";
+        return MAFEM_NAN_DETECTED;
+      }
+      // still converging (or stalled): redo the iteration with the waiting
+      // solver, which runs up to max_refine sweeps and reports a stall
+      ++h->fallbacks;
+      const int sw = h->ss_sweeps;
+      h->no_async = true;
+      const int rc = iter_enqueue(h);
+      h->no_async = false;
+      if (rc) return rc;
+      CK(cudaEventSynchronize(h->ev[4]));
+      accum_times(h);
+      h->ss_sweeps += sw;
+    }
   }
   mafem_step_stats& S = h->ss_S;
   const int iter = h->ss_iter;

@@ -91,9 +91,10 @@ __global__ void predictor_kernel(DevPatch P, PhysParams pp, double dt) {
 // host redoes the iteration or reports the failure.
 __global__ void newton_update_kernel(DevPatch P, PhysParams pp, double dt, const double* __restrict__ x,
                                      const double* __restrict__ r, double* __restrict__ part,
-                                     const int* __restrict__ skip, const int* __restrict__ skip2) {
+                                     const int* __restrict__ skip, const int* __restrict__ skip2,
+                                     const int* __restrict__ skip3) {
   __shared__ double s_du[32], s_r[32];
-  const bool hold = (skip && *skip) || (skip2 && *skip2);
+  const bool hold = (skip && *skip) || (skip2 && *skip2) || (skip3 && *skip3);
   double du2 = 0.0, r2 = 0.0;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P.nmdf; q += (int64_t)gridDim.x * blockDim.x) {
     r2 += r[q] * r[q];
@@ -262,9 +263,10 @@ void launch_predictor(const DevPatch& P, const PhysParams& pp, double dt, cudaSt
 }
 int newton_update_blocks(int64_t nmdf) { return (int)min64(256, (nmdf + 255) / 256); }
 void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
-                          double* part, double* out, cudaStream_t st, const int* skip, const int* skip2) {
+                          double* part, double* out, cudaStream_t st, const int* skip, const int* skip2,
+                          const int* skip3) {
   const int blocks = newton_update_blocks(P.nmdf);
-  newton_update_kernel<<<blocks, 256, 0, st>>>(P, pp, dt, x, r, part, skip, skip2);
+  newton_update_kernel<<<blocks, 256, 0, st>>>(P, pp, dt, x, r, part, skip, skip2, skip3);
   newton_norm_kernel<<<1, 32, 0, st>>>(part, blocks, P.nmdf, out);
 }
 int band_residual_blocks(int64_t n) { return (int)min64(304, (n + 255) / 256); }
@@ -306,6 +308,7 @@ __global__ void refine_check_kernel(const double* __restrict__ rn, const double*
                                     double* __restrict__ nrm, double tol, int max_sweeps) {
   if (threadIdx.x != 0 || blockIdx.x != 0 || st[0]) return;
   const double r = *rn, d = dxn[0], xv = dxn[1];
+  // (refine_init_kernel clears st[0..2]; st[3] is written by refine_seal_kernel)
   const int k = st[1] + 1;
   st[1] = k;
   if (!isfinite(r) || !isfinite(d) || !isfinite(xv)) {
@@ -332,6 +335,11 @@ void launch_refine_check(const double* rn, const double* dxn, int* st, double* n
                          cudaStream_t s) {
   refine_check_kernel<<<1, 32, 0, s>>>(rn, dxn, st, nrm, tol, max_sweeps);
 }
+// st[3] = 1 unless the refinement has stopped with MAFEM_OK (the Newton update's skip word)
+__global__ void refine_seal_kernel(int* __restrict__ st) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) st[3] = (st[0] && st[2] == MAFEM_OK) ? 0 : 1;
+}
+void launch_refine_seal(int* st, cudaStream_t s) { refine_seal_kernel<<<1, 32, 0, s>>>(st); }
 void launch_copy_gated(int64_t n, const double* src, double* dst, const int* gate, cudaStream_t s) {
   const int blocks = (int)min64(304, (n + 255) / 256);
   copy_gated_kernel<<<blocks, 256, 0, s>>>(n, src, dst, gate);

@@ -128,7 +128,7 @@ void launch_dirichlet_scale(double* cps, const int* idx, const double* val, int 
 int newton_update_blocks(int64_t nmdf);
 void launch_newton_update(const DevPatch& P, const PhysParams& pp, double dt, const double* x, const double* r,
                           double* part, double* out, cudaStream_t st, const int* skip = nullptr,
-                          const int* skip2 = nullptr);
+                          const int* skip2 = nullptr, const int* skip3 = nullptr);
 int band_residual_blocks(int64_t n);
 template <class T>
 void launch_band_residual(const T* a0, const BandLayout& L, const double* x, const double* r, double* res,
@@ -144,6 +144,8 @@ void launch_refine_init(const double* r0, int* st, double* nrm, cudaStream_t s);
 void launch_refine_check(const double* rn, const double* dxn, int* st, double* nrm, double tol, int max_sweeps,
                          cudaStream_t s);
 void launch_copy_gated(int64_t n, const double* src, double* dst, const int* gate, cudaStream_t s);
+// st[3] = 1 unless the refinement has stopped with MAFEM_OK.
+void launch_refine_seal(int* st, cudaStream_t s);
 
 template <class T>
 size_t apply_smem_bytes(const BandLayout& L, int threads);
