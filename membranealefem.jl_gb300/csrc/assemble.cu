@@ -303,7 +303,9 @@ __global__ void refine_init_kernel(const double* __restrict__ r0, int* __restric
 }
 // After each sweep: stop on |r| <= tol |r0| (MAFEM_OK), a non-finite norm
 // (MAFEM_NAN_DETECTED), a stall -- |r| > |r_prev| / 2 after the fourth sweep --
-// or max_sweeps (MAFEM_REFINE_STALLED).
+// or max_sweeps (MAFEM_REFINE_STALLED, or MAFEM_OK when the last correction is
+// at most 1e-8 |x|: the residual has reached its rounding floor, which in a
+// late Newton iteration, where |r0| is itself tiny, lies above tol |r0|).
 __global__ void refine_check_kernel(const double* __restrict__ rn, const double* __restrict__ dxn, int* __restrict__ st,
                                     double* __restrict__ nrm, double tol, int max_sweeps) {
   if (threadIdx.x != 0 || blockIdx.x != 0 || st[0]) return;
@@ -317,7 +319,9 @@ __global__ void refine_check_kernel(const double* __restrict__ rn, const double*
   } else if (r <= tol * nrm[0]) {
     st[0] = 1;
   } else if ((k >= 4 && r > 0.5 * nrm[1]) || k >= max_sweeps) {
-    st[2] = MAFEM_REFINE_STALLED;
+    // no longer contracting: at the rounding floor (the last correction a
+    // small part of x) the solution is as accurate as the factors allow
+    st[2] = (d <= 1e-8 * xv) ? MAFEM_OK : MAFEM_REFINE_STALLED;
     st[0] = 1;
   }
   nrm[1] = r;

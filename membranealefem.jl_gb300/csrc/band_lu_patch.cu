@@ -280,21 +280,16 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
     for (int cb = rank * nch; cb < C; cb += NR * nch) {
       const int nc = min(nch, C - cb);
       const int ncp = (nc + 15) & ~15;  // the MMA's N
-      // U12 = Li P A12 and Y = Mi P A12: two threads per column (rows 0-15 and
-      // 16-31 of U12 / Y), each with the whole column in registers; Y goes to
-      // Yh / Yl split into TF32 parts (zero beyond nc).  Every load of the
-      // column comes before the barrier, every U12 store after it.
-      const bool job = tid < 2 * ncp;
-      const int c = job ? tid % ncp : 0, rh = job ? tid / ncp : 0;
-      const int64_t col = j1 + cb + c;
-      float* dst = ab + bix(L, j0, col);  // A(j0 + r, col) = dst[r]
-      float a[32];
+      // U12 = Li P A12 and Y = Mi P A12: one thread per column, the column in
+      // registers; Y goes to Yh / Yl split into TF32 parts (zero beyond nc)
+      for (int c = tid; c < ncp; c += kPT) {
+        const int64_t col = j1 + cb + c;
+        float* dst = ab + bix(L, j0, col);  // A(j0 + r, col) = dst[r]
+        float a[32];
 #pragma unroll
-      for (int k = 0; k < 32; ++k) a[k] = (job && c < nc && k < w) ? ldx<CG>(dst + sp[k]) : 0.0f;
-      __syncthreads();
-      if (job) {
+        for (int k = 0; k < 32; ++k) a[k] = (c < nc && k < w) ? ldx<CG>(dst + sp[k]) : 0.0f;
 #pragma unroll 2
-        for (int r = 16 * rh; r < 16 * rh + 16; ++r) {
+        for (int r = 0; r < 32; ++r) {
           float u = 0.0f, y = 0.0f;
           if (r < w) {  // block-uniform
             const float4* l4 = reinterpret_cast<const float4*>(Li + r * kIS);
@@ -362,38 +357,27 @@ __global__ void __launch_bounds__(kPT, 1) patch_factor_kernel(const PatchJob* __
       const int cs = min(ncp, grp * cpg), ce = min(ncp, cs + cpg);
       for (int t = 0; t < ntile; ++t) {
         const int b = t & 1;
-        const int row = w + t * kMT + 32 * q + lane;  // panel row of this thread
-        const bool live = row < R;
-        float* pa = ab + bix(L, j0 + (live ? row : 0), j1 + cb);  // + c * ldm: A(j0 + row, j1 + cb + c)
-        // this thread's A22 values, 32 columns at a time; the first 32 are
-        // loaded before the wait, so their L2 round trip overlaps the MMAs
-        float v[32];
-        auto load_v = [&](int c0) {
-#pragma unroll
-          for (int k = 0; k < 32; ++k)
-            v[k] = (live && c0 + k < ce && c0 + k < nc) ? ldx<CG>(pa + (int64_t)(c0 + k) * ldm) : 0.0f;
-        };
-        if (cs < ce) load_v(cs);
         mbar_wait_bounded(&bar_mma[b], ph_mma[b], err);  // tile t's products are in Tensor Memory
         if (tid == 0) {
           if (t + 2 < ntile) tma_tile(t + 2);  // buffer b is free: tile t's MMAs have completed
           if (t + 1 < ntile) mma_tile(t + 1);  // into the other accumulator, read back at t - 1
         }
         tc::fence_after();
+        const int row = w + t * kMT + 32 * q + lane;  // panel row of this thread
+        const bool live = row < R;
+        float* pa = ab + bix(L, j0 + (live ? row : 0), j1 + cb);  // + c * ldm: A(j0 + row, j1 + cb + c)
         const uint32_t dt = tmem + ((uint32_t)(32 * q) << 16) + b * kNCH;
-        for (int c0 = cs; c0 < ce; c0 += 32) {  // ce - c0 is a multiple of 8 (warp-uniform)
-          float d[4][8];
-          tc::ld8(dt + c0, d[0]);
-          if (c0 + 8 < ce) tc::ld8(dt + c0 + 8, d[1]);
-          if (c0 + 16 < ce) tc::ld8(dt + c0 + 16, d[2]);
-          if (c0 + 24 < ce) tc::ld8(dt + c0 + 24, d[3]);
+        for (int c0 = cs; c0 < ce; c0 += 16) {
+          float d0[8], d1[8];
+          tc::ld8(dt + c0, d0);
+          if (c0 + 8 < ce) tc::ld8(dt + c0 + 8, d1);
           tc::wait_ld();
+          float v[16];
 #pragma unroll
-          for (int k = 0; k < 32; ++k) d[k >> 3][k & 7] = v[k] - d[k >> 3][k & 7];
-          if (c0 + 32 < ce) load_v(c0 + 32);  // the next 32 columns' loads in flight during the stores
+          for (int k = 0; k < 16; ++k) v[k] = (live && c0 + k < ce && c0 + k < nc) ? ldx<CG>(pa + (int64_t)(c0 + k) * ldm) : 0.0f;
 #pragma unroll
-          for (int k = 0; k < 32; ++k)
-            if (live && c0 + k < ce && c0 + k < nc) pa[(int64_t)(c0 + k) * ldm] = d[k >> 3][k & 7];
+          for (int k = 0; k < 16; ++k)
+            if (live && c0 + k < ce && c0 + k < nc) pa[(int64_t)(c0 + k) * ldm] = v[k] - (k < 8 ? d0[k] : d1[k - 8]);
         }
         tc::fence_before();
         __syncthreads();  // accumulator b is read before the MMAs of tile t + 2 overwrite it
@@ -528,11 +512,19 @@ __device__ void patch_lu_solve(const PatchJob& J, float* v, float* bz, float (*p
           v[i] -= sacc;
         }
       }
-      // rows beyond kFwdRows slots (very wide bands): loaded on the spot
+      // rows beyond kFwdRows slots (very wide bands): loaded on the spot, 16 of
+      // the row's loads in flight at a time
       for (int64_t i = j1 + rt + (int64_t)kFwdRows * (kRT - 32); i < rend; i += kRT - 32) {
         const float* a = ab + bix(L, i, j0);
         float sacc = 0.0f;
-        for (int k = 0; k < w; ++k) sacc = fmaf(a[k * ldm], bz[k], sacc);
+#pragma unroll
+        for (int h = 0; h < 32; h += 16) {
+          float tk[16];
+#pragma unroll
+          for (int k = 0; k < 16; ++k) tk[k] = h + k < w ? a[(h + k) * ldm] : 0.0f;
+#pragma unroll
+          for (int k = 0; k < 16; ++k) sacc = fmaf(tk[k], bz[h + k], sacc);
+        }
         v[i] -= sacc;
       }
       fwd_load(p + 1);
@@ -569,9 +561,21 @@ __device__ void patch_lu_solve(const PatchJob& J, float* v, float* bz, float (*p
       const int c = warp + m * (kRT / 32);
       if (c < C) acc = fmaf(u[m], v[j1 + c], acc);
     }
-    if (lane < w) {  // columns beyond kBwdCols slots (very wide bands): loaded on the spot
+    if (lane < w) {  // columns beyond kBwdCols slots (very wide bands): loaded on the spot, four at a time in flight
       const float* ur = ab + bix(L, j0 + lane, j1);
-      for (int c = warp + kBwdCols * (kRT / 32); c < C; c += kRT / 32) acc = fmaf(ur[(int64_t)c * ldm], v[j1 + c], acc);
+      for (int c0 = warp + kBwdCols * (kRT / 32); c0 < C; c0 += 4 * (kRT / 32)) {
+        float tu[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const int c = c0 + m * (kRT / 32);
+          tu[m] = c < C ? ur[(int64_t)c * ldm] : 0.0f;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          const int c = c0 + m * (kRT / 32);
+          if (c < C) acc = fmaf(tu[m], v[j1 + c], acc);
+        }
+      }
     }
     part[warp][lane] = acc;
     bwd_load(p - 1);
@@ -744,7 +748,12 @@ __global__ void __launch_bounds__(kRT, 1) patch_refine_kernel(const PatchJob* __
         status = MAFEM_OK;
         break;
       }
-      if (k >= 3 && dn > 0.5 * prev_dn) break;  // stalled
+      if (k >= 3 && dn > 0.5 * prev_dn) {  // no longer contracting
+        // at the rounding floor (the correction a small part of x) the
+        // solution is as accurate as the factors allow: accept it
+        if (dn <= 1e-8 * xn) status = MAFEM_OK;
+        break;
+      }
       prev_dn = dn;
     }
   }
