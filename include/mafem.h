@@ -387,6 +387,12 @@ int mafem_set_refinement(mafem_handle* h, int32_t max_sweeps, double tol);
  * forms when the band is too wide for their shared-memory panels). */
 int mafem_set_lu_path(mafem_handle* h, int32_t path);
 
+/* Batched FP32 form: the CTAs (one thread-block cluster) that factor this
+ * handle's patch -- 1, 2 or 4; 0 (the default) chooses by band width: one CTA
+ * up to 256 trailing columns, two up to 512, four beyond.  Any choice gives the
+ * same factors; it trades the factorisation's latency against the SMs it holds. */
+int mafem_set_patch_ctas(mafem_handle* h, int32_t ctas);
+
 typedef struct mafem_kernel_times {
   double ms_assemble;         /* element kernel + gathers */
   double ms_panel, ms_apply;  /* summed device time of the LU's two kernels */

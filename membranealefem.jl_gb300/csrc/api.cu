@@ -117,6 +117,7 @@ struct mafem_handle {
   int* d_pull_list = nullptr;
   double* d_pull_r = nullptr;
   int lu_path = MAFEM_LU_AUTO;
+  int patch_nr = 0;  // CTAs per cluster of the batched FP32 factor (0: by band width)
   int fepoch = 0;          // epoch of the last persistent factorisation
   void* d_rdiag = nullptr;
   int64_t fallbacks = 0;
@@ -1241,8 +1242,11 @@ extern "C" int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas) {
 // clusters first, then those on two-CTA clusters, then the single-CTA ones,
 // each group largest first.  Returns the size of the first group in *n4 and of
 // the second in *n2.
+// CTAs that factor the handle's patch in the batched FP32 form
+static int patch_ctas(const mafem_handle* h) { return h->patch_nr ? h->patch_nr : patch_cluster_ctas(h->blk.kuf); }
+
 static void order_patch_jobs(std::vector<mafem_handle*>& hv, std::vector<int>& idx, int* n4, int* n2) {
-  auto nr = [&](int k) { return patch_cluster_ctas(hv[k]->blk.kuf); };
+  auto nr = [&](int k) { return patch_ctas(hv[k]); };
   auto cost = [&](int k) { return (double)hv[k]->blk.npan() * hv[k]->L.kl * hv[k]->blk.kuf; };
   std::sort(idx.begin(), idx.end(), [&](int a, int b) {
     if (nr(a) != nr(b)) return nr(a) > nr(b);
@@ -1404,7 +1408,7 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
           st[i] = MAFEM_ERR_CUDA;
           continue;
         }
-        if (i == pj[0]) h->launches += 2;  // the two batched launches, counted once
+        if (i == pj[0]) h->launches += patch_solve_launches(n4, n2, (int)pj.size());  // counted once
         const int rc = iter_enqueue_patch_end(h, b->bev);
         if (rc != MAFEM_OK) st[i] = rc;
       }
@@ -1703,7 +1707,7 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
         retire.push_back(q);
         continue;
       }
-      if (k == pj[0]) q->h->launches += 2;
+      if (k == pj[0]) q->h->launches += patch_solve_launches(n4, n2, (int)pj.size());
       const int rc = iter_enqueue_patch_end(q->h, lane->done);
       if (rc != MAFEM_OK) {
         q->status = rc;
@@ -1925,7 +1929,7 @@ extern "C" int mafem_trace_patch_solve(mafem_handle* h, double time, double dt, 
   cudaEventCreate(&e2);
   const int dyn = patch_solve_setup();
   cudaEventRecord(e0, h->st);
-  const int nr = patch_cluster_ctas(h->blk.kuf);  // as a batch would run it
+  const int nr = patch_ctas(h);  // as a batch would run it
   patch_solve_stage(d_job, d_ord, 1, nr, patch_factor_smem(h->L.kl), 0, 0, 0.0, h->st);
   cudaEventRecord(e1, h->st);
   patch_solve_stage(d_job, d_ord, 1, 1, 0, patch_refine_smem(h->L.n), h->max_refine, h->refine_tol, h->st);
@@ -2185,6 +2189,12 @@ extern "C" int mafem_set_lu_path(mafem_handle* h, int32_t path) {
   }
   h->lu_path = path;
   h->factored = false;
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_set_patch_ctas(mafem_handle* h, int32_t ctas) {
+  if (!h || (ctas != 0 && ctas != 1 && ctas != 2 && ctas != 4)) return MAFEM_ERR_ARG;
+  h->patch_nr = ctas;
   return MAFEM_OK;
 }
 

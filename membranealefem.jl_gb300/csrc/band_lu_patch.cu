@@ -512,19 +512,11 @@ __device__ void patch_lu_solve(const PatchJob& J, float* v, float* bz, float (*p
           v[i] -= sacc;
         }
       }
-      // rows beyond kFwdRows slots (very wide bands): loaded on the spot, 16 of
-      // the row's loads in flight at a time
+      // rows beyond kFwdRows slots (very wide bands): loaded on the spot
       for (int64_t i = j1 + rt + (int64_t)kFwdRows * (kRT - 32); i < rend; i += kRT - 32) {
         const float* a = ab + bix(L, i, j0);
         float sacc = 0.0f;
-#pragma unroll
-        for (int h = 0; h < 32; h += 16) {
-          float tk[16];
-#pragma unroll
-          for (int k = 0; k < 16; ++k) tk[k] = h + k < w ? a[(h + k) * ldm] : 0.0f;
-#pragma unroll
-          for (int k = 0; k < 16; ++k) sacc = fmaf(tk[k], bz[h + k], sacc);
-        }
+        for (int k = 0; k < w; ++k) sacc = fmaf(a[k * ldm], bz[k], sacc);
         v[i] -= sacc;
       }
       fwd_load(p + 1);
@@ -561,21 +553,9 @@ __device__ void patch_lu_solve(const PatchJob& J, float* v, float* bz, float (*p
       const int c = warp + m * (kRT / 32);
       if (c < C) acc = fmaf(u[m], v[j1 + c], acc);
     }
-    if (lane < w) {  // columns beyond kBwdCols slots (very wide bands): loaded on the spot, four at a time in flight
+    if (lane < w) {  // columns beyond kBwdCols slots (very wide bands): loaded on the spot
       const float* ur = ab + bix(L, j0 + lane, j1);
-      for (int c0 = warp + kBwdCols * (kRT / 32); c0 < C; c0 += 4 * (kRT / 32)) {
-        float tu[4];
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const int c = c0 + m * (kRT / 32);
-          tu[m] = c < C ? ur[(int64_t)c * ldm] : 0.0f;
-        }
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const int c = c0 + m * (kRT / 32);
-          if (c < C) acc = fmaf(tu[m], v[j1 + c], acc);
-        }
-      }
+      for (int c = warp + kBwdCols * (kRT / 32); c < C; c += kRT / 32) acc = fmaf(ur[(int64_t)c * ldm], v[j1 + c], acc);
     }
     part[warp][lane] = acc;
     bwd_load(p - 1);
@@ -840,6 +820,11 @@ cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int nj
   return cudaGetLastError();
 }
 
+int patch_solve_launches(int n4, int n2, int njobs) {
+  const int groups = (n4 > 0) + (n2 > 0) + (njobs - n4 - n2 > 0);
+  return groups + (groups > 1 ? 2 : 1);  // the factor launches and one refinement per stream
+}
+
 cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int n4, int n2, int njobs, size_t smem_factor,
                         size_t smem_refine, int max_sweeps, double tol, cudaStream_t st, cudaStream_t st2,
                         cudaEvent_t ev_fork, cudaEvent_t ev_join) {
@@ -847,7 +832,9 @@ cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int n4, int 
   cudaError_t e = cudaSuccess;
   // the groups in launch order: four-CTA clusters, two-CTA clusters, single
   // CTAs; the first non-empty group on st, the others one after the other on
-  // st2 beside it (their chains are the shorter ones)
+  // st2 beside it (their chains are the shorter ones).  Each stream refines its
+  // own patches as soon as their factors are done, so the refinement of one
+  // group overlaps the factorisations of the other.
   const int cnt[3] = {n4, n2, njobs - n4 - n2}, nrs[3] = {4, 2, 1};
   int first = 0;
   while (first < 3 && cnt[first] == 0) ++first;
@@ -861,11 +848,19 @@ cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int n4, int 
     if (cnt[g] == 0) continue;
     e = launch_factor(d_jobs, d_order + off, cnt[g], nrs[g], smem_factor, g == first ? st : st2);
     off += cnt[g];
+    if (g == first && e == cudaSuccess) {
+      patch_refine_kernel<<<cnt[g], kRT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
+      e = cudaGetLastError();
+    }
+  }
+  if (fork && e == cudaSuccess) {
+    patch_refine_kernel<<<njobs - cnt[first], kRT, smem_refine, st2>>>(d_jobs, d_order + cnt[first], max_sweeps,
+                                                                        tol);
+    e = cudaGetLastError();
   }
   if (fork && e == cudaSuccess) e = cudaEventRecord(ev_join, st2);
   if (fork && e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_join, 0);
   if (e != cudaSuccess) return e;
-  patch_refine_kernel<<<njobs, kRT, smem_refine, st>>>(d_jobs, d_order, max_sweeps, tol);
   return cudaGetLastError();
 }
 

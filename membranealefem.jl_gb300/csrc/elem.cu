@@ -105,9 +105,12 @@ struct Coef {
       : kb(P(pp.kb)), kg(P(pp.kg)), zv(P(pp.zv)), pn(P(pp.pn)), adb_zv(P(pp.adb / pp.zv)), am(P(pp.am)) {}
 };
 
-// Row accumulators: the tangent pass adds column q of the element block (and,
-// in the plain form, the primal value of row q); the residual pass adds the
-// primal value of every row into a per-task array.
+// Row accumulators.  A residual row at one Gauss point is linear in node b's
+// basis values (N, N_,α, N_,αβ): lin() receives the row's coefficient duals
+// c[s] and the basis values phi[s] of node b and adds sum_s phi[s] c[s].  The
+// tangent pass adds the tangent part to column q of the element block (and, in
+// the plain form, the primal of row q alone); the residual pass adds the
+// primal of every row into a per-task array.
 template <class P, class T, bool WANT_R>
 struct AccTan {
   T* Ks;
@@ -117,10 +120,29 @@ struct AccTan {
     if (WANT_R && row == q) rsum += val.v;
     Ks[row * ldk + q] += val.d;
   }
+  template <int NS>
+  __device__ __forceinline__ void lin(int row, const Dual<P, T> (&c)[NS], const P (&phi)[NS]) {
+    T d = T(phi[0]) * c[0].d;
+#pragma unroll
+    for (int s = 1; s < NS; ++s) d += T(phi[s]) * c[s].d;
+    Ks[row * ldk + q] += d;
+    if (WANT_R && row == q) {
+      P v = phi[0] * c[0].v;
+#pragma unroll
+      for (int s = 1; s < NS; ++s) v += phi[s] * c[s].v;
+      rsum += v;
+    }
+  }
 };
 struct AccRes {
   double* R;  // [row]
-  __device__ __forceinline__ void operator()(int row, Dual<double, Nil> val) { R[row] += val.v; }
+  template <int NS>
+  __device__ __forceinline__ void lin(int row, const Dual<double, Nil> (&c)[NS], const double (&phi)[NS]) {
+    double v = phi[0] * c[0].v;
+#pragma unroll
+    for (int s = 1; s < NS; ++s) v += phi[s] * c[s].v;
+    R[row] += v;
+  }
 };
 // boundary rows are velocity rows only: R[b*3 + i] for row vd[i] + ndf*b
 struct AccResV {
@@ -132,6 +154,39 @@ struct AccResV {
   }
 };
 
+// Primal values of one (element, area Gauss point) that every tangent
+// direction shares, formed once: a_α and x_,αβ (sums over the 9 nodes of the
+// mesh positions) and the interpolants of the 8 unknowns -- u N for u = 0..7,
+// u N_,1 and u N_,2 for u = 0..5 (zero for an unknown the motion lacks).
+constexpr int kPreA = 0, kPreX = 6, kPreN = 15, kPreD0 = 23, kPreD1 = 29, kPre = 35;
+template <class P>
+__device__ __forceinline__ P gp_pre_value(int j, const PhysParams& pp, const P* X, const P* C, const P* f) {
+  const P* wts;
+  const P* src;
+  int stride;
+  if (j < kPreX) {  // a[i][α] = sum_b N_,α[b] x[b][i]
+    wts = f + 10 + 9 * (j & 1);
+    src = X + (j >> 1);
+    stride = 3;
+  } else if (j < kPreN) {  // xab[i][k] = sum_b N_,k[b] x[b][i]
+    const int i = (j - kPreX) / 3, k = j - kPreX - 3 * i;
+    wts = f + 28 + 9 * k;
+    src = X + i;
+    stride = 3;
+  } else {
+    const int u = j < kPreD0 ? j - kPreN : j < kPreD1 ? j - kPreD0 : j - kPreD1;
+    const int d = pp.dof_of[u];
+    if (d < 0) return P(0);  // get_dof_cps zero-fills absent unknowns (GeoDynStress.jl:190-205)
+    wts = f + (j < kPreD0 ? 1 : j < kPreD1 ? 10 : 19);
+    src = C + d;
+    stride = 8;
+  }
+  P s = 0;
+#pragma unroll
+  for (int b = 0; b < 9; ++b) s += wts[b] * src[b * stride];
+  return s;
+}
+
 // ---- element kernel --------------------------------------------------------------
 // motion is a template parameter; the dof maps are runtime (PhysParams).
 enum { STATIC_ = 1, EUL_ = 2, LAG_ = 3, ALEV_ = 4, ALEVB_ = 5 };
@@ -139,8 +194,8 @@ enum { STATIC_ = 1, EUL_ = 2, LAG_ = 3, ALEV_ = 4, ALEVB_ = 5 };
 // One area Gauss point: calc_elem_dof_residuals' GP body (FiniteElement.jl:284-321)
 // with geo_dyn_stress (GeoDynStress.jl:91-178) inlined, on dual numbers.
 template <class P, class T, int MOTION, class Acc>
-__device__ __forceinline__ void area_gp(const PhysParams& pp, const Coef<P>& cf, const P* X, const P* C, const P* f,
-                                        int as, int js, int us, P dt, Acc& acc) {
+__device__ __forceinline__ void area_gp(const PhysParams& pp, const Coef<P>& cf, const P* pre, const P* f, int as,
+                                        int js, int us, P dt, Acc& acc) {
   const int ndf = pp.ndf;
   const P w = f[0];
   const P* N = f + 1;
@@ -149,23 +204,16 @@ __device__ __forceinline__ void area_gp(const PhysParams& pp, const Coef<P>& cf,
   const P* dd[3] = {f + 28, f + 37, f + 46};
   const T sN = T(N[as]), sd0 = T(dN0[as]), sd1 = T(dN1[as]);
 
-  // geometry: a_α, x_,αβ (x itself is not used by the residual)
+  // geometry: a_α, x_,αβ (x itself is not used by the residual); the seed of a
+  // mesh-motion direction is ∂xms[as, js] = Δt
   Dual<P, T> a[3][2], xab[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    P s0 = 0, s1 = 0, t0 = 0, t1 = 0, t2 = 0;
-#pragma unroll
-    for (int b = 0; b < 9; ++b) {
-      P xb = X[b * 3 + i];
-      s0 += dN0[b] * xb; s1 += dN1[b] * xb;
-      t0 += dd[0][b] * xb; t1 += dd[1][b] * xb; t2 += dd[2][b] * xb;
-    }
     T g = (i == js) ? T(dt) : T(0);
-    a[i][0] = mk<P, T>(s0, g * sd0);
-    a[i][1] = mk<P, T>(s1, g * sd1);
-    xab[i][0] = mk<P, T>(t0, g * T(dd[0][as]));
-    xab[i][1] = mk<P, T>(t1, g * T(dd[1][as]));
-    xab[i][2] = mk<P, T>(t2, g * T(dd[2][as]));
+    a[i][0] = mk<P, T>(pre[kPreA + 2 * i], g * sd0);
+    a[i][1] = mk<P, T>(pre[kPreA + 2 * i + 1], g * sd1);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) xab[i][k] = mk<P, T>(pre[kPreX + 3 * i + k], g * T(dd[k][as]));
   }
   Dual<P, T> a11 = a[0][0] * a[0][0] + a[1][0] * a[1][0] + a[2][0] * a[2][0];
   Dual<P, T> a12 = a[0][0] * a[0][1] + a[1][0] * a[1][1] + a[2][0] * a[2][1];
@@ -199,23 +247,19 @@ __device__ __forceinline__ void area_gp(const PhysParams& pp, const Coef<P>& cf,
   Dual<P, T> H = (i11 * bf[0] + i12 * bf[2] + i12 * bf[2] + i22 * bf[1]) * P(0.5);
   Dual<P, T> K = (bf[0] * bf[1] - bf[2] * bf[2]) * idet;
 
-  // dynamics (get_dof_cps zero-fills absent unknowns, GeoDynStress.jl:190-205)
-  auto interp = [&](int u, const P* wts, T swt) -> Dual<P, T> {
-    int d = pp.dof_of[u];
-    P s = 0;
-    if (d >= 0) {
-#pragma unroll
-      for (int b = 0; b < 9; ++b) s += wts[b] * C[b * 8 + d];
-    }
+  // dynamics: interpolants of unknown u (pre-formed), seeded when u is this
+  // direction's unknown; kind 0: N, 1: N_,1, 2: N_,2
+  auto interp = [&](int u, int kind, T swt) -> Dual<P, T> {
+    const P s = pre[(kind == 0 ? kPreN : kind == 1 ? kPreD0 : kPreD1) + u];
     return mk<P, T>(s, (u == us) ? swt : T(0));
   };
   Dual<P, T> dv[3][2];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    dv[i][0] = interp(i, dN0, sd0);
-    dv[i][1] = interp(i, dN1, sd1);
+    dv[i][0] = interp(i, 1, sd0);
+    dv[i][1] = interp(i, 2, sd1);
   }
-  Dual<P, T> lam = interp(6, N, sN);
+  Dual<P, T> lam = interp(6, 0, sN);
 
   // π^αβ = ζv sym(a^αᵀ v_,α a⁻¹)  (GeoDynStress.jl:148-149)
   auto visc = [&](Dual<P, T> g[3][2], Dual<P, T>& p11, Dual<P, T>& p12, Dual<P, T>& p22) {
@@ -257,18 +301,18 @@ __device__ __forceinline__ void area_gp(const PhysParams& pp, const Coef<P>& cf,
     Dual<P, T> dvm[3][2];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      dvm[i][0] = interp(3 + i, dN0, sd0);
-      dvm[i][1] = interp(3 + i, dN1, sd1);
+      dvm[i][0] = interp(3 + i, 1, sd0);
+      dvm[i][1] = interp(3 + i, 2, sd1);
     }
     Dual<P, T> m11, m12, m22;
     visc(dvm, m11, m12, m22);
     sm0 = i11 * cb - bu11 * hb + m11;  // GeoDynStress.jl:156-159
     sm1 = i22 * cb - bu22 * hb + m22;
     sm2 = (i12 * cb - bu12 * hb + m12) * P(2);
-    pm_ = interp(7, N, sN);
+    pm_ = interp(7, 0, sN);
     Dual<P, T> nd = cst<P, T>(P(0));
 #pragma unroll
-    for (int i = 0; i < 3; ++i) nd = nd + n[i] * (interp(3 + i, N, sN) - interp(i, N, sN));
+    for (int i = 0; i < 3; ++i) nd = nd + n[i] * (interp(3 + i, 0, sN) - interp(i, 0, sN));
     nd_ = nd;
   }
   Dual<P, T> nv;
@@ -276,56 +320,97 @@ __device__ __forceinline__ void area_gp(const PhysParams& pp, const Coef<P>& cf,
     Dual<P, T> v[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      v[i] = interp(i, N, sN);
-      vmv[i] = interp(3 + i, N, sN);
+      v[i] = interp(i, 0, sN);
+      vmv[i] = interp(3 + i, 0, sN);
     }
     nv = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
   }
 
-  // residual rows (node-major packing of calc_elem_residual, FiniteElement.jl:225-239)
-  const int vo0 = pp.dof_of[0], vo1 = pp.dof_of[1], vo2 = pp.dof_of[2];
-  const int vd[3] = {vo0, vo1, vo2};
+  // Residual rows (node-major packing of calc_elem_residual,
+  // FiniteElement.jl:225-239).  Row (node b, dof) of this point is linear in
+  // node b's basis values -- with nn_k(b) = N_,k[b] - Γ^α_k N_,α[b],
+  //   r_v,i = a_i,1 c1 + a_i,2 c2 + n_i (nn·M) J w - n_i pn N J w,
+  //   c1 = (σ11 N_,1 + σ12 N_,2) J w, c2 = (σ22 N_,2 + σ12 N_,1) J w,
+  // and likewise for the mesh, pressure and λ rows -- so each row's
+  // coefficients of (N_,1, N_,2, N_,11, N_,22, N_,12, N) are formed once per
+  // point and the node loop is a 6-term sum per row.
+  const int vd[3] = {pp.dof_of[0], pp.dof_of[1], pp.dof_of[2]};
   const int mo[3] = {pp.dof_of[3], pp.dof_of[4], pp.dof_of[5]};
   const int lo = pp.dof_of[6], po = pp.dof_of[7];
-  Dual<P, T> rl_c = J * tr - cf.adb_zv * lam;
-#pragma unroll 1
-  for (int b = 0; b < 9; ++b) {
-    Dual<P, T> nn0 = cst<P, T>(dd[0][b]) - (Gam[0][0] * dN0[b] + Gam[0][1] * dN1[b]);
-    Dual<P, T> nn1 = cst<P, T>(dd[1][b]) - (Gam[1][0] * dN0[b] + Gam[1][1] * dN1[b]);
-    Dual<P, T> nn2 = cst<P, T>(dd[2][b]) - (Gam[2][0] * dN0[b] + Gam[2][1] * dN1[b]);
-    Dual<P, T> cbm = (nn0 * M0 + nn1 * M1 + nn2 * M2) * JW;  // Bbᵀ𝗠 coefficient of n_i
-    Dual<P, T> c1 = (sg0 * dN0[b] + sg2 * (P(0.5) * dN1[b])) * JW;
-    Dual<P, T> c2 = (sg1 * dN1[b] + sg2 * (P(0.5) * dN0[b])) * JW;
+  auto phi6 = [&](int b, P (&ph)[6]) {
+    ph[0] = dN0[b];
+    ph[1] = dN1[b];
+    ph[2] = dd[0][b];
+    ph[3] = dd[1][b];
+    ph[4] = dd[2][b];
+    ph[5] = N[b];
+  };
+  const Dual<P, T> JWh = JW * P(0.5);
+  const Dual<P, T> MJ[3] = {M0 * JW, M1 * JW, M2 * JW};  // bending: nn·M J w = sum_k N_,k MJ_k - N_,α GM_α
+  const Dual<P, T> GM0 = Gam[0][0] * MJ[0] + Gam[1][0] * MJ[1] + Gam[2][0] * MJ[2];
+  const Dual<P, T> GM1 = Gam[0][1] * MJ[0] + Gam[1][1] * MJ[1] + Gam[2][1] * MJ[2];
+  {
+    const Dual<P, T> S0 = sg0 * JW, S1 = sg1 * JW, S2 = sg2 * JWh, PN = JW * cf.pn;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      if (vd[i] >= 0) {
-        Dual<P, T> rv = a[i][0] * c1 + a[i][1] * c2 + n[i] * cbm;
-        if (pp.pn != 0.0) rv = rv - n[i] * (N[b] * cf.pn) * JW;
-        acc(vd[i] + ndf * b, rv);
+      if (vd[i] < 0) continue;
+      const Dual<P, T> c[6] = {a[i][0] * S0 + a[i][1] * S2 - n[i] * GM0, a[i][0] * S2 + a[i][1] * S1 - n[i] * GM1,
+                               n[i] * MJ[0], n[i] * MJ[1], n[i] * MJ[2], -(n[i] * PN)};
+#pragma unroll 1
+      for (int b = 0; b < 9; ++b) {
+        P ph[6];
+        phi6(b, ph);
+        acc.lin(vd[i] + ndf * b, c, ph);
       }
     }
-    if (MOTION == ALEV_ || MOTION == ALEVB_) {
-      Dual<P, T> e1 = (sm0 * dN0[b] + sm2 * (P(0.5) * dN1[b])) * JW;
-      Dual<P, T> e2 = (sm1 * dN1[b] + sm2 * (P(0.5) * dN0[b])) * JW;
-      Dual<P, T> pnj = pm_ * JW * N[b];
+  }
+  if (MOTION == ALEV_ || MOTION == ALEVB_) {
+    const Dual<P, T> E0 = sm0 * JW, E1 = sm1 * JW, E2 = sm2 * JWh, PJ = pm_ * JW;
 #pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        Dual<P, T> rm = a[i][0] * e1 + a[i][1] * e2;
-        if (MOTION == ALEVB_) rm = rm + n[i] * cbm;
-        rm = rm - n[i] * pnj;
-        acc(mo[i] + ndf * b, rm);
+    for (int i = 0; i < 3; ++i) {
+      if (MOTION == ALEVB_) {  // the mesh rows carry the bending term too
+        const Dual<P, T> c[6] = {a[i][0] * E0 + a[i][1] * E2 - n[i] * GM0, a[i][0] * E2 + a[i][1] * E1 - n[i] * GM1,
+                                 n[i] * MJ[0], n[i] * MJ[1], n[i] * MJ[2], -(n[i] * PJ)};
+#pragma unroll 1
+        for (int b = 0; b < 9; ++b) {
+          P ph[6];
+          phi6(b, ph);
+          acc.lin(mo[i] + ndf * b, c, ph);
+        }
+      } else {
+        const Dual<P, T> c[3] = {a[i][0] * E0 + a[i][1] * E2, a[i][0] * E2 + a[i][1] * E1, -(n[i] * PJ)};
+#pragma unroll 1
+        for (int b = 0; b < 9; ++b) {
+          const P ph[3] = {dN0[b], dN1[b], N[b]};
+          acc.lin(mo[i] + ndf * b, c, ph);
+        }
       }
-      Dual<P, T> rp = -((JW * nd_) * N[b]) - pm_ * (N[b] * w * cf.adb_zv);
-      acc(po + ndf * b, rp);
     }
-    if (MOTION == EUL_) {
+    const Dual<P, T> c[1] = {-(JW * nd_) - pm_ * (w * cf.adb_zv)};
+#pragma unroll 1
+    for (int b = 0; b < 9; ++b) {
+      const P ph[1] = {N[b]};
+      acc.lin(po + ndf * b, c, ph);
+    }
+  }
+  if (MOTION == EUL_) {
 #pragma unroll
-      for (int i = 0; i < 3; ++i) {
-        Dual<P, T> rm = (vmv[i] - n[i] * nv) * JW * (N[b] * cf.am);
-        acc(mo[i] + ndf * b, rm);
+    for (int i = 0; i < 3; ++i) {
+      const Dual<P, T> c[1] = {(vmv[i] - n[i] * nv) * JW * cf.am};
+#pragma unroll 1
+      for (int b = 0; b < 9; ++b) {
+        const P ph[1] = {N[b]};
+        acc.lin(mo[i] + ndf * b, c, ph);
       }
     }
-    acc(lo + ndf * b, rl_c * (N[b] * w));
+  }
+  {
+    const Dual<P, T> c[1] = {(J * tr - cf.adb_zv * lam) * w};
+#pragma unroll 1
+    for (int b = 0; b < 9; ++b) {
+      const P ph[1] = {N[b]};
+      acc.lin(lo + ndf * b, c, ph);
+    }
   }
 }
 
@@ -427,12 +512,14 @@ __global__ void elem_kernel(DevPatch Pt, PhysParams pp, double time, double dt, 
   const int q = threadIdx.x - slot * nq;
   const int kk = blockIdx.x * EPB + slot;  // element (or list) index of this slot
   const int e = elist ? (kk < nlist ? elist[kk] : 0) : kk;
-  // per-slot shared memory: X[27], C[72], GP tables [9][kTab] in P; then the blocks
-  const size_t per_slot = 27 + 72 + 9 * kTab;
+  // per-slot shared memory: X[27], C[72], GP tables [9][kTab], the points'
+  // shared primal values [9][kPre] in P; then the blocks
+  const size_t per_slot = 27 + 72 + 9 * kTab + 9 * kPre;
   P* base = reinterpret_cast<P*>(smem_raw);
   P* X = base + slot * per_slot;
   P* C = X + 27;
   P* tab = C + 72;
+  P* pre = tab + 9 * kTab;
   T* Ks = reinterpret_cast<T*>(base + EPB * per_slot) + (size_t)slot * nq * ldk;
   const bool live = (slot < EPB) && (elist ? kk < nlist : e < Pt.numel);
 
@@ -450,6 +537,12 @@ __global__ void elem_kernel(DevPatch Pt, PhysParams pp, double time, double dt, 
     for (int k = q; k < nq * ldk; k += nq) Ks[k] = T(0.0);
   }
   __syncthreads();
+  if (live)
+    for (int k = q; k < 9 * kPre; k += nq) {
+      const int gp = k / kPre;
+      pre[k] = gp_pre_value<P>(k - gp * kPre, pp, X, C, tab + gp * kTab);
+    }
+  __syncthreads();
   if (live) {
     const int as = q / ndf, ds = q - as * ndf;
     const int us = pp.unk_of[ds];
@@ -459,7 +552,8 @@ __global__ void elem_kernel(DevPatch Pt, PhysParams pp, double time, double dt, 
     AccTan<P, T, WANT_R> acc{Ks, ldk, q, P(0)};
 
 #pragma unroll 1
-    for (int gp = 0; gp < 9; ++gp) area_gp<P, T, MOTION>(pp, cf, X, C, tab + gp * kTab, as, js, us, pdt, acc);
+    for (int gp = 0; gp < 9; ++gp)
+      area_gp<P, T, MOTION>(pp, cf, pre + gp * kPre, tab + gp * kTab, as, js, us, pdt, acc);
 
     // Dohrmann-Bochev projection (FiniteElement.jl:323-327): rλ += Gᵀ H⁻¹ G λ αdb/ζv,
     // and for ALEV/ALEVB rp += Gᵀ H⁻¹ G p αdb/ζv.  Linear in λ / p.
@@ -548,8 +642,11 @@ __global__ void __launch_bounds__(kResEPB * 9) elem_resid_kernel(DevPatch Pt, Ph
     const int el = tid / 9, gp = tid - 9 * el;
     if (el < ne) {
       const double* f = Pt.tab + ((size_t)Pt.uel[e0 + el] * 9 + gp) * kTab;
+      double pre[kPre];
+#pragma unroll
+      for (int j = 0; j < kPre; ++j) pre[j] = gp_pre_value<double>(j, pp, X + el * 27, C + el * 72, f);
       AccRes acc{R + (size_t)tid * nq};
-      area_gp<double, Nil, MOTION>(pp, cf, X + el * 27, C + el * 72, f, 0, -1, -1, dt, acc);
+      area_gp<double, Nil, MOTION>(pp, cf, pre, f, 0, -1, -1, dt, acc);
     }
   }
   __syncthreads();
@@ -621,7 +718,7 @@ __global__ void __launch_bounds__(kResEPB * 9) elem_resid_kernel(DevPatch Pt, Ph
 // ---- launchers -----------------------------------------------------------------------
 template <class P, class T>
 static size_t elem_smem(int nq, int epb) {
-  return (size_t)epb * (27 + 72 + 9 * kTab) * sizeof(P) + (size_t)epb * nq * (nq + 1) * sizeof(T);
+  return (size_t)epb * (27 + 72 + 9 * kTab + 9 * kPre) * sizeof(P) + (size_t)epb * nq * (nq + 1) * sizeof(T);
 }
 template <class T>
 size_t elem_smem_bytes(int nq, int epb) {

@@ -283,10 +283,13 @@ int patch_cluster_ctas(int kuf);
 // the refine kernel alone (smem_factor == 0).
 cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int njobs, int nr, size_t smem_factor,
                               size_t smem_refine, int max_sweeps, double tol, cudaStream_t st);
+// kernel launches patch_solve makes for these group sizes
+int patch_solve_launches(int n4, int n2, int njobs);
 // Factor and solve the jobs d_order[0 .. njobs): the first n4 on four-CTA
 // clusters, the next n2 on two-CTA clusters, the rest one CTA each -- the first
 // non-empty group on st, the others after one another on st2 (forked from and
-// joined to st with ev_fork / ev_join); then the refinement of all on st.
+// joined to st with ev_fork / ev_join); each stream refines its own jobs after
+// their factorisations.
 cudaError_t patch_solve(const PatchJob* d_jobs, const int* d_order, int n4, int n2, int njobs, size_t smem_factor,
                         size_t smem_refine, int max_sweeps, double tol, cudaStream_t st, cudaStream_t st2,
                         cudaEvent_t ev_fork, cudaEvent_t ev_join);

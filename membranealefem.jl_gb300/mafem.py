@@ -166,6 +166,7 @@ def lib():
         L.mafem_launch_count.argtypes = [vp]
         L.mafem_launch_count.restype = C.c_int64
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
+        L.mafem_set_patch_ctas.argtypes = [vp, C.c_int32]
         L.mafem_set_refinement.argtypes = [vp, C.c_int32, C.c_double]
         L.mafem_set_wait_test.argtypes = [vp, C.c_int32, C.c_int32]
         L.mafem_set_dirichlet_scale.argtypes = [vp, C.c_double]
@@ -516,6 +517,11 @@ class Solver:
     def set_lu_path(self, path: int) -> None:
         """Select the banded LU: LU_AUTO (default), LU_PANELS or LU_FULL."""
         _raise(lib().mafem_set_lu_path(self.h, path), self.h)
+
+    def set_patch_ctas(self, ctas: int) -> None:
+        """Batched FP32 form: CTAs (1, 2 or 4) of the cluster that factors this
+        patch; 0 chooses by band width."""
+        _raise(lib().mafem_set_patch_ctas(self.h, ctas), self.h)
 
     def profile_factor(self, time: float, dt: float) -> dict:
         """Per-kernel device time of one assembly + factorisation of the resident state."""
