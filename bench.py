@@ -247,7 +247,7 @@ def run_gb300(args, rank, world, local, dist):
             s.time_step_resident(t, dt)
         cu.flush_l2()
         cu.sync()
-        flat, fit, fref = [], [], []
+        flat, fit, fref, fph = [], [], [], [0.0, 0.0, 0.0]
         for _ in range(args.steps):
             t += dt
             h0 = time.perf_counter()
@@ -256,11 +256,15 @@ def run_gb300(args, rank, world, local, dist):
             flat.append((time.perf_counter() - h0) * 1e3)
             fit.append(st["newton_iters"])
             fref.append(st["refine_iters"])
+            for k, key in enumerate(("ms_assemble", "ms_factor", "ms_solve")):
+                fph[k] += st[key]
             cu.flush_l2()
         x32, c32 = s.download()
     lam = mesh.dofs[6] - 1
     vel = [d for d in range(mesh.ndf) if d != lam]
     out["fp32"] = dict(total_ms=float(sum(flat)), lat=flat, iters=fit, refine=fref,
+                       phase_ms_per_iter={k: v / max(1, sum(fit)) for k, v in
+                                          zip(("assemble", "factor", "refinement"), fph)},
                        err_x=float(np.abs(x32 - x_fp64).max() / np.abs(x_fp64).max()),
                        err_v=float(np.abs(c32[:, vel] - c_fp64[:, vel]).max() / np.abs(c_fp64[:, vel]).max()),
                        err_lam=float(np.abs(c32[:, lam] - c_fp64[:, lam]).max() / np.abs(c_fp64[:, lam]).max()))
@@ -824,6 +828,7 @@ def main():
                                   "refine_tol": FP32_REFINE_TOL,
                                   "newton_iters_per_step": statistics.mean(r["fp32"]["iters"]),
                                   "refine_sweeps_per_step": statistics.mean(r["fp32"]["refine"]),
+                                  "phase_ms_per_iter": r["fp32"]["phase_ms_per_iter"],
                                   "rel_err_xms": r["fp32"]["err_x"], "rel_err_vel": r["fp32"]["err_v"],
                                   "rel_err_lambda": r["fp32"]["err_lam"]},
         "mesh": r["mesh"],

@@ -393,6 +393,18 @@ int mafem_set_lu_path(mafem_handle* h, int32_t path);
  * same factors; it trades the factorisation's latency against the SMs it holds. */
 int mafem_set_patch_ctas(mafem_handle* h, int32_t ctas);
 
+/* Autotuner of the batched FP32 factorisation: measure (CUDA events, on a
+ * synthetic band of this handle's shape written over its band, so call it
+ * between steps and with the GPU otherwise idle) the time of factoring this
+ * patch on 1, 2 and 4 CTAs, once per device and patch shape, cached for the
+ * process.  mafem_batch_create measures every shape of its patches; each
+ * batched round (mafem_batch_step, mafem_server_round) then picks per shape
+ * the cluster size that minimises the round's estimated makespan, max(longest
+ * factorisation, summed CTA-time / SMs).  Shapes without times keep the
+ * width rule of mafem_set_patch_ctas.  MAFEM_ERR_UNSUPPORTED for a handle the
+ * batched FP32 form does not serve. */
+int mafem_autotune_patch(mafem_handle* h);
+
 typedef struct mafem_kernel_times {
   double ms_assemble;         /* element kernel + gathers */
   double ms_panel, ms_apply;  /* summed device time of the LU's two kernels */

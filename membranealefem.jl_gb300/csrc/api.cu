@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -18,6 +19,7 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <thread>
 #include <vector>
 
@@ -117,7 +119,8 @@ struct mafem_handle {
   int* d_pull_list = nullptr;
   double* d_pull_r = nullptr;
   int lu_path = MAFEM_LU_AUTO;
-  int patch_nr = 0;  // CTAs per cluster of the batched FP32 factor (0: by band width)
+  int patch_nr = 0;  // CTAs per cluster of the batched FP32 factor (0: chosen per round)
+  int round_nr = 0;  // the cluster size the autotuner chose for this round (0: by band width)
   int fepoch = 0;          // epoch of the last persistent factorisation
   void* d_rdiag = nullptr;
   int64_t fallbacks = 0;
@@ -1242,8 +1245,121 @@ extern "C" int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas) {
 // clusters first, then those on two-CTA clusters, then the single-CTA ones,
 // each group largest first.  Returns the size of the first group in *n4 and of
 // the second in *n2.
-// CTAs that factor the handle's patch in the batched FP32 form
-static int patch_ctas(const mafem_handle* h) { return h->patch_nr ? h->patch_nr : patch_cluster_ctas(h->blk.kuf); }
+// CTAs that factor the handle's patch in the batched FP32 form: the caller's
+// choice, else the autotuner's for this round, else by band width
+static int patch_ctas(const mafem_handle* h) {
+  return h->patch_nr ? h->patch_nr : h->round_nr ? h->round_nr : patch_cluster_ctas(h->blk.kuf);
+}
+
+// ---- autotuner of the batched FP32 factorisation's cluster sizes ----------------------
+// The time of factoring one patch on 1, 2 and 4 CTAs is measured once per
+// device and patch shape (synthetic band, CUDA events) and cached for the
+// process.  Each round then picks a cluster size per shape: more CTAs shorten a
+// patch's factorisation but cost more SM-time (on a 48 x 48 patch about 1.5x
+// faster on 2 CTAs and 2.4x on 4), so a round with many patches wants small
+// clusters and a round with few large ones big clusters.
+namespace {
+using PatchShape = std::tuple<int, int64_t, int, int, int>;  // device, n, kl, kuf, panels
+std::mutex g_tune_mu;
+std::map<PatchShape, std::array<float, 3>> g_tune;  // ms on 1, 2, 4 CTAs
+int g_num_sms = 0;
+PatchShape patch_shape(const mafem_handle* h) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return PatchShape{dev, h->L.n, h->L.kl, h->blk.kuf, h->blk.npan()};
+}
+}  // namespace
+
+// Measure the cluster-size times of h's patch shape if not cached yet, with
+// h's job (d_jobs[slot]) on stream st; d_tmp: one device int.  The job's band is
+// overwritten (the next assembly rewrites it).
+static int patch_tune(mafem_handle* h, const PatchJob* d_jobs, int slot, int* d_tmp, cudaStream_t st) {
+  const PatchShape key = patch_shape(h);
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    if (g_tune.count(key)) return MAFEM_OK;
+  }
+  std::array<float, 3> ms{};
+  CK(cudaMemcpyAsync(d_tmp, &slot, sizeof(int), cudaMemcpyHostToDevice, st));
+  const int nrs[3] = {1, 2, 4};
+  for (int k = 0; k < 3; ++k) {
+    const cudaError_t e = patch_time_factor(d_jobs, d_tmp, nrs[k], patch_factor_smem(h->L.kl), st, &ms[k]);
+    if (e != cudaSuccess) {
+      h->err = std::string("factorisation autotuning: ") + cudaGetErrorString(e);
+      return MAFEM_ERR_CUDA;
+    }
+  }
+  CK(cudaMemsetAsync(h->d_info, 0, 4 * sizeof(int), st));
+  CK(cudaStreamSynchronize(st));
+  h->factored = false;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tune[key] = ms;
+  if (!g_num_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  return MAFEM_OK;
+}
+
+// Cluster size per patch shape for the round's jobs hv[idx]: the choice in
+// {1, 2, 4} per shape that minimises the estimated makespan
+//   max(longest factorisation, sum of jobs x CTAs x time / SMs)
+// (exhaustive over up to 8 shapes, the rest by band width).  Patches whose
+// caller fixed the size, or whose shape has no times, keep theirs.
+static void choose_patch_ctas(std::vector<mafem_handle*>& hv, const std::vector<int>& idx) {
+  std::map<PatchShape, int> count;
+  std::vector<std::pair<PatchShape, std::array<float, 3>>> shapes;
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    for (int k : idx) {
+      mafem_handle* h = hv[k];
+      h->round_nr = 0;
+      if (h->patch_nr) continue;
+      const PatchShape key = patch_shape(h);
+      auto it = g_tune.find(key);
+      if (it == g_tune.end()) continue;
+      if (count[key]++ == 0 && shapes.size() < 8) shapes.push_back(*it);
+    }
+  }
+  if (shapes.empty() || g_num_sms <= 0) return;
+  const int ns = (int)shapes.size();
+  const int nrs[3] = {1, 2, 4};
+  std::vector<int> pick(ns, 0), best(ns, 0);
+  double best_t = INFINITY;
+  int combos = 1;
+  for (int c = 0; c < ns; ++c) combos *= 3;
+  for (int code = 0; code < combos; ++code) {
+    int x = code;
+    double lg[3] = {0.0, 0.0, 0.0}, work = 0.0;  // longest factorisation per group (1, 2, 4 CTAs)
+    for (int c = 0; c < ns; ++c) {
+      pick[c] = x % 3;
+      x /= 3;
+      const double t = shapes[c].second[pick[c]];
+      lg[pick[c]] = std::max(lg[pick[c]], t);
+      work += count[shapes[c].first] * nrs[pick[c]] * t;
+    }
+    // patch_solve runs the first non-empty group (4, 2, 1 CTAs) on one stream
+    // and the others one after the other on a second
+    const int first = lg[2] > 0.0 ? 2 : lg[1] > 0.0 ? 1 : 0;
+    double rest = 0.0;
+    for (int g = 0; g < 3; ++g)
+      if (g != first) rest += lg[g];
+    const double est = std::max(std::max(lg[first], rest), work / g_num_sms);
+    if (est < best_t - 1e-9) {
+      best_t = est;
+      best = pick;
+    }
+  }
+  std::map<PatchShape, int> nr;
+  for (int c = 0; c < ns; ++c) nr[shapes[c].first] = nrs[best[c]];
+  for (int k : idx) {
+    mafem_handle* h = hv[k];
+    if (h->patch_nr) continue;
+    auto it = nr.find(patch_shape(h));
+    if (it != nr.end()) h->round_nr = it->second;
+  }
+}
 
 static void order_patch_jobs(std::vector<mafem_handle*>& hv, std::vector<int>& idx, int* n4, int* n2) {
   auto nr = [&](int k) { return patch_ctas(hv[k]); };
@@ -1334,6 +1450,14 @@ extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ct
       set_global_error(std::string("mafem_batch_create: ") + cudaGetErrorString(e));
       return MAFEM_ERR_CUDA;
     }
+    for (int i = 0; i < n; ++i) {  // the autotuner's times of every patch shape not yet measured
+      if (b->slot[i] < 0) continue;
+      const int rc = patch_tune(b->hs[i], b->d_jobs, b->slot[i], b->d_order, b->bst);
+      if (rc != MAFEM_OK) {
+        set_global_error("mafem_batch_create: " + b->hs[i]->err);
+        return rc;
+      }
+    }
     b->patch_on = true;
   }
   *out = b.release();
@@ -1384,6 +1508,7 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
     }
     if (!pj.empty()) {
       int n4 = 0, n2 = 0;
+      choose_patch_ctas(b->hs, pj);
       order_patch_jobs(b->hs, pj, &n4, &n2);
       // one launch serves every patch: the strictest tolerance and the largest sweep cap among them
       b->max_sweeps = 1;
@@ -1679,6 +1804,7 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
     std::vector<mafem_handle*> hv(s->active.size());
     for (size_t k = 0; k < s->active.size(); ++k) hv[k] = s->active[k]->h;
     int n4 = 0, n2 = 0;
+    choose_patch_ctas(hv, pj);
     order_patch_jobs(hv, pj, &n4, &n2);
     size_t smf = 0, smr = 0;
     int max_sw = 1;
@@ -2190,6 +2316,25 @@ extern "C" int mafem_set_lu_path(mafem_handle* h, int32_t path) {
   h->lu_path = path;
   h->factored = false;
   return MAFEM_OK;
+}
+
+extern "C" int mafem_autotune_patch(mafem_handle* h) {
+  if (!h) return MAFEM_ERR_ARG;
+  if (!h->patch_ok) {
+    h->err = "the batched FP32 form does not serve this handle";
+    return MAFEM_ERR_UNSUPPORTED;
+  }
+  PatchJob* d_job = nullptr;
+  int* d_tmp = nullptr;
+  cudaError_t e = cudaMalloc(&d_job, sizeof(PatchJob));
+  if (e == cudaSuccess) e = cudaMalloc(&d_tmp, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_job, &h->job, sizeof(PatchJob), cudaMemcpyHostToDevice, h->st);
+  int rc = e == cudaSuccess ? patch_tune(h, d_job, 0, d_tmp, h->st) : MAFEM_ERR_CUDA;
+  if (e != cudaSuccess) h->err = std::string("mafem_autotune_patch: ") + cudaGetErrorString(e);
+  cudaStreamSynchronize(h->st);
+  if (d_job) cudaFree(d_job);
+  if (d_tmp) cudaFree(d_tmp);
+  return rc;
 }
 
 extern "C" int mafem_set_patch_ctas(mafem_handle* h, int32_t ctas) {

@@ -820,6 +820,48 @@ cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int nj
   return cudaGetLastError();
 }
 
+// ---- autotuning: the factorisation's time per cluster size -------------------------
+// A synthetic band of the job's shape: entries of the band uniform in [-1, 1)
+// (a hash of i and j), the diagonal kl + ku + 2 (diagonally dominant, so every
+// node block keeps its own pivots), the pivoting fill rows zero.  The
+// factorisation's time does not depend on the values.
+__global__ void patch_fill_synthetic_kernel(const PatchJob* __restrict__ jobs, const int* __restrict__ order) {
+  const PatchJob& J = jobs[order[0]];
+  const BandLayout L = J.L;
+  const int64_t total = L.ldb * L.n;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = idx / L.ldb, i = j + (idx - j * L.ldb) - L.off;
+    float v = 0.0f;
+    if (i >= 0 && i < L.n && i - j <= L.kl && j - i <= L.ku) {
+      uint32_t h = (uint32_t)i * 73856093u ^ (uint32_t)j * 19349663u;
+      h ^= h >> 13;
+      h *= 0x5bd1e995u;
+      h ^= h >> 15;
+      v = i == j ? (float)(L.kl + L.ku + 2) : (float)(h & 0xffffu) * (1.0f / 32768.0f) - 1.0f;
+    }
+    J.band[idx] = v;
+  }
+}
+
+cudaError_t patch_time_factor(const PatchJob* d_jobs, const int* d_order1, int nr, size_t smem, cudaStream_t st,
+                              float* ms) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {  // the second run is timed
+    patch_fill_synthetic_kernel<<<1024, 256, 0, st>>>(d_jobs, d_order1);
+    e = cudaEventRecord(e0, st);
+    if (e == cudaSuccess) e = launch_factor(d_jobs, d_order1, 1, nr, smem, st);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  }
+  if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  return e;
+}
+
 int patch_solve_launches(int n4, int n2, int njobs) {
   const int groups = (n4 > 0) + (n2 > 0) + (njobs - n4 - n2 > 0);
   return groups + (groups > 1 ? 2 : 1);  // the factor launches and one refinement per stream

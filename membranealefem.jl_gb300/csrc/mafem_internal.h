@@ -283,6 +283,11 @@ int patch_cluster_ctas(int kuf);
 // the refine kernel alone (smem_factor == 0).
 cudaError_t patch_solve_stage(const PatchJob* d_jobs, const int* d_order, int njobs, int nr, size_t smem_factor,
                               size_t smem_refine, int max_sweeps, double tol, cudaStream_t st);
+// Time (ms, CUDA events) of factoring job d_order1[0] on a cluster of nr CTAs,
+// on a synthetic band of its shape written over the job's band (which the
+// next assembly rewrites); synchronises st.
+cudaError_t patch_time_factor(const PatchJob* d_jobs, const int* d_order1, int nr, size_t smem, cudaStream_t st,
+                              float* ms);
 // kernel launches patch_solve makes for these group sizes
 int patch_solve_launches(int n4, int n2, int njobs);
 // Factor and solve the jobs d_order[0 .. njobs): the first n4 on four-CTA

@@ -167,6 +167,7 @@ def lib():
         L.mafem_launch_count.restype = C.c_int64
         L.mafem_set_lu_path.argtypes = [vp, C.c_int32]
         L.mafem_set_patch_ctas.argtypes = [vp, C.c_int32]
+        L.mafem_autotune_patch.argtypes = [vp]
         L.mafem_set_refinement.argtypes = [vp, C.c_int32, C.c_double]
         L.mafem_set_wait_test.argtypes = [vp, C.c_int32, C.c_int32]
         L.mafem_set_dirichlet_scale.argtypes = [vp, C.c_double]
@@ -522,6 +523,12 @@ class Solver:
         """Batched FP32 form: CTAs (1, 2 or 4) of the cluster that factors this
         patch; 0 chooses by band width."""
         _raise(lib().mafem_set_patch_ctas(self.h, ctas), self.h)
+
+    def autotune_patch(self) -> None:
+        """Measure (once per device and patch shape) the batched FP32 factorisation
+        of this patch on 1, 2 and 4 CTAs for the round-by-round autotuner; call
+        between steps with the GPU otherwise idle."""
+        _raise(lib().mafem_autotune_patch(self.h), self.h)
 
     def profile_factor(self, time: float, dt: float) -> dict:
         """Per-kernel device time of one assembly + factorisation of the resident state."""
