@@ -127,6 +127,7 @@ struct mafem_handle {
   // batched FP32 form (band_lu_patch.cu): the handle's job, usable when its band fits
   float* d_inv = nullptr;
   double* d_zbuf = nullptr;  // npan x 32: z = U11^-1 y1 per panel (cooperative forward substitution)
+  double* d_pinv = nullptr;  // npan x 2 x 32 x 32: L11^-1, U11^-1 per panel (cooperative substitutions)
   bool patch_ok = false;
   bool ss_patch = false;  // the iteration in progress ran through a batch's patch solve
   PatchJob job{};
@@ -275,6 +276,7 @@ static int64_t footprint(const mafem_mesh_desc* d, int precision, int64_t kl) {
   b += d->numnp * (3 + d->ndf) * 8 + d->nmdf * 8 * 6;                           // state + vectors
   b += ((d->nmdf + nb - 1) / std::max(nb, 1)) * ((int64_t)nb + kl) * 4;           // panel permutations
   b += d->nmdf * (esz + 4);                                                      // pivot reciprocals, blocks
+  b += (d->nmdf / 24 + 1) * 2 * 32 * 32 * 8;                                     // panel triangle inverses
   return b;
 }
 
@@ -501,6 +503,7 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
       h->use_blk = true;
       AL(h->d_flags, (size_t)h->blk.npan());
       AL(h->d_zbuf, (size_t)h->blk.npan() * kBlkW);
+      AL(h->d_pinv, (size_t)h->blk.npan() * 2 * kBlkW * kBlkW);
       cudaMemset(h->d_flags, 0, (size_t)h->blk.npan() * sizeof(int));
       h->bwd_grid = precision == MAFEM_PLAIN_FP64 ? blk_backward_grid<double, double>() : blk_backward_grid<double, float>();
       h->bwd_max = h->bwd_grid;
@@ -698,6 +701,17 @@ static int assemble(mafem_handle* h, double time, double dt, bool both_bands = f
 // the fallback.
 // Launch the node-block factorisation (persistent kernel, or per-panel launches)
 // without waiting for it; `info` tells later whether a block had no usable pivot.
+// The panels' triangle inverses for the cooperative substitutions, stream-ordered
+// after a node-block factorisation.
+static void blk_after_factor(mafem_handle* h) {
+  if (!h->d_pinv) return;
+  if (h->precision == MAFEM_PLAIN_FP64)
+    blk_inverses<double, double>((const double*)h->d_band, h->L, h->blk, (const double*)h->d_rdiag, h->d_pinv, h->st);
+  else
+    blk_inverses<double, float>((const float*)h->d_band, h->L, h->blk, (const float*)h->d_rdiag, h->d_pinv, h->st);
+  h->launches += 1;
+}
+
 static int factor_enqueue(mafem_handle* h, double* x) {
   const bool fp64 = h->precision == MAFEM_PLAIN_FP64;
   CK(cudaMemsetAsync(h->d_info, 0, sizeof(int), h->st));
@@ -723,6 +737,7 @@ static int factor_enqueue(mafem_handle* h, double* x) {
                                                h->d_info, nullptr, h->st, h->st2, h->ev_pool.data(), nullptr);
     h->launches += nl;
   }
+  blk_after_factor(h);
   CK(cudaGetLastError());
   h->factored = true;
   h->last_blk = true;
@@ -797,7 +812,7 @@ template <class T>
 static void blk_back_solve(mafem_handle* h, double* y, const int* gate = nullptr) {
   if (h->bwd_grid > 0) {
     ++h->epoch;
-    if (blk_backward<double, T>((const T*)h->d_band, h->L, h->blk, (const T*)h->d_rdiag, y, h->d_flags, h->epoch,
+    if (blk_backward<double, T>((const T*)h->d_band, h->L, h->blk, h->d_pinv, y, h->d_flags, h->epoch,
                                 h->d_info + 1, h->bwd_grid, h->st, h->wait_test, gate) == 0) {
       h->launches += 1;
       return;
@@ -815,7 +830,7 @@ template <class T>
 static void blk_fwd_solve(mafem_handle* h, double* y, const int* gate = nullptr) {
   if (h->bwd_grid > 0) {
     ++h->epoch;
-    if (blk_forward_coop<double, T>((const T*)h->d_band, h->L, h->blk, h->d_perm, (const T*)h->d_rdiag, y, h->d_zbuf,
+    if (blk_forward_coop<double, T>((const T*)h->d_band, h->L, h->blk, h->d_perm, h->d_pinv, y, h->d_zbuf,
                                     h->d_flags, h->epoch, h->d_info + 1, h->bwd_grid, h->st, h->wait_test,
                                     gate) == 0) {
       h->launches += 1;
@@ -2017,6 +2032,7 @@ extern "C" int mafem_trace_factor(mafem_handle* h, double time, double dt, int64
                       : blk_lu_factor_persist<float>((float*)h->d_band, h->L, h->blk, h->pers, h->fepoch, h->d_perm,
                                                      (float*)h->d_rdiag, h->d_info, nullptr, h->d_info + 1, h->st,
                                                      d_tr);
+  blk_after_factor(h);
   h->factored = true;
   h->last_blk = true;
   CK(cudaMemcpyAsync(out, d_tr, sizeof(long long) * 12 * npan, cudaMemcpyDeviceToHost, h->st));
@@ -2367,6 +2383,7 @@ extern "C" int mafem_profile_factor(mafem_handle* h, double time, double dt, maf
     else
       blk_lu_factor<float>((float*)h->d_band, h->L, h->blk, h->d_perm, (float*)h->d_rdiag, h->d_info, nullptr, h->st,
                            nullptr, nullptr, ev.data());
+    blk_after_factor(h);
   } else if (fp64) {
     band_lu_factor<double>((double*)h->d_band, h->L, h->d_ipiv, h->d_perm, h->rmax, h->d_info, h->d_x,
                            h->apply_threads, h->apply_blocks, h->st, nullptr, nullptr, ev.data());

@@ -320,6 +320,57 @@ __global__ void __launch_bounds__(1024) blk_backward_kernel(const T* __restrict_
 }
 
 // ---------------------------------------------------------------------------
+// Explicit inverses of every panel's diagonal triangles for the cooperative
+// substitutions: Li = L11^-1 (unit lower) and Ui = U11^-1 (upper, 1 / U(k, k)
+// from rdiag), 32 x 32 each with element (i, k) at k * 32 + i, zero outside
+// the panel's w x w block; inv[p] = Li then Ui.  One warp per panel (four per
+// CTA), lane c
+// forming column c of both by substitution.  With them the step of a
+// substitution that lies on its critical path -- the panel's two triangles --
+// is two 32-term dot products per lane with independent shuffles instead of
+// two 32-step dependent chains.
+template <class T, class V>
+__global__ void __launch_bounds__(128) blk_inverses_kernel(const T* __restrict__ ab, BandLayout L,
+                                                           const int* __restrict__ ps, int npan,
+                                                           const T* __restrict__ rdiag, V* __restrict__ inv) {
+  __shared__ V S[4][32][33];  // per warp: S[c][i] = A(j0 + i, j0 + c) of its panel
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int p = blockIdx.x * 4 + warp;
+  if (p >= npan) return;  // warp-uniform; only warp-level synchronisation below
+  const int64_t j0 = ps[p];
+  const int w = (int)(ps[p + 1] - j0);
+  for (int c = 0; c < 32; ++c) S[warp][c][lane] = (c < w && lane < w) ? V(ab[bix(L, j0 + lane, j0 + c)]) : V(0);
+  const V rd = lane < w ? V(rdiag[j0 + lane]) : V(0);
+  __syncwarp();
+  V* Li = inv + (size_t)p * 2 * kBlkW * kBlkW;
+  V* Ui = Li + kBlkW * kBlkW;
+  V x[32];
+  // column `lane` of L11^-1: L11 x = e_lane, forward
+#pragma unroll
+  for (int i = 0; i < 32; ++i) x[i] = i == lane ? V(1) : V(0);
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    const V xk = x[k];
+#pragma unroll
+    for (int i = k + 1; i < 32; ++i) x[i] = fma(-S[warp][k][i], xk, x[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) Li[lane * 32 + i] = (lane < w && i < w) ? x[i] : V(0);
+  // column `lane` of U11^-1: U11 x = e_lane, backward
+#pragma unroll
+  for (int i = 0; i < 32; ++i) x[i] = i == lane ? V(1) : V(0);
+#pragma unroll
+  for (int k = 31; k >= 0; --k) {
+    const V xk = x[k] * __shfl_sync(kFull, rd, k);
+    x[k] = xk;
+#pragma unroll
+    for (int i = 0; i < k; ++i) x[i] = fma(-S[warp][k][i], xk, x[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) Ui[lane * 32 + i] = (lane < w && i < w) ? x[i] : V(0);
+}
+
+// ---------------------------------------------------------------------------
 // Back substitution on many SMs: one cooperative launch, panel q handled by
 // CTA (npan - 1 - q) mod gridDim.x.  A CTA accumulates U(q rows, c) x(c) over
 // the columns of the panels above it as their flags appear (most are done
@@ -334,11 +385,11 @@ __global__ void __launch_bounds__(1024) blk_backward_kernel(const T* __restrict_
 template <class T, class V>
 __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restrict__ ab, BandLayout L, int kuf,
                                                                 const int* __restrict__ ps, int npan,
-                                                                const T* __restrict__ rdiag, V* y, int* flags,
+                                                                const V* __restrict__ inv, V* y, int* flags,
                                                                 int epoch, int* err, WaitTest wt,
                                                                 const int* gate) {
   __shared__ V part[8][33];
-  __shared__ V Us[32][33];
+  __shared__ V Uis[32 * 32];  // U11^-1 of the panel, element (i, k) at k * 32 + i
   __shared__ int s_ok;
   if (gate && *gate) return;  // every CTA reads the same word: all return (refinement already stopped)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -346,10 +397,8 @@ __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restr
     const int64_t j0 = ps[q], j1 = ps[q + 1];
     const int w = (int)(j1 - j0);
     const int64_t jend = min64b(L.n, j1 + kuf);
-    for (int k = tid; k < w * w; k += 256) {
-      const int c = k / w, i = k - c * w;
-      Us[c][i] = i < c ? V(ab[bix(L, j0 + i, j0 + c)]) : (i == c ? V(rdiag[j0 + c]) : V(0));
-    }
+    const V* Ui = inv + (size_t)q * 2 * kBlkW * kBlkW + kBlkW * kBlkW;
+    for (int k = tid; k < kBlkW * kBlkW; k += 256) Uis[k] = __ldcg(Ui + k);
     int pl = q + 1;  // last panel with columns in [j1, jend)
     while (pl + 1 < npan && ps[pl + 1] < jend) ++pl;
     V acc = V(0);
@@ -364,21 +413,12 @@ __global__ void __launch_bounds__(256) blk_backward_coop_kernel(const T* __restr
     if (warp == 0) {
       const V sum = ((part[0][lane] + part[1][lane]) + (part[2][lane] + part[3][lane])) +
                     ((part[4][lane] + part[5][lane]) + (part[6][lane] + part[7][lane]));  // tree: 3 dependent adds
-      // U11 x = v with this lane's row in registers, pre-scaled by 1/U(lane, lane)
-      // (unit diagonal): each step of the chain is one shuffle and one FMA
-      const V rl = lane < w ? Us[lane][lane] : V(0);  // 1 / U(lane, lane)
-      V Ur[32];
+      // x1 = U11^-1 (y1 - U12 x2): one dot product per lane, the shuffles independent
+      const V v = lane < w ? __ldcg(y + j0 + lane) - sum : V(0);
+      V x = V(0);
 #pragma unroll
-      for (int k = 0; k < 32; ++k) Ur[k] = (k < w && lane < k) ? Us[k][lane] * rl : V(0);
-      V v = lane < w ? (__ldcg(y + j0 + lane) - sum) * rl : V(0);
-#pragma unroll
-      for (int k = 31; k >= 0; --k) {
-        if (k < w) {
-          const V xk = __shfl_sync(kFull, v, k);
-          if (lane < k) v = fma(-Ur[k], xk, v);
-        }
-      }
-      if (lane < w) __stcg(y + j0 + lane, v);
+      for (int k = 0; k < 32; ++k) x = fma(Uis[k * 32 + lane], __shfl_sync(kFull, v, k), x);
+      if (lane < w) __stcg(y + j0 + lane, x);
       __threadfence();
       __syncwarp();
       if (lane == 0 && npan - 1 - q != wt.withhold) st_release(flags + q, epoch);
@@ -401,11 +441,11 @@ template <class T, class V>
 __global__ void __launch_bounds__(256) blk_forward_coop_kernel(const T* __restrict__ ab, BandLayout L,
                                                                const int* __restrict__ ps, int npan,
                                                                const int* __restrict__ perm_all,
-                                                               const T* __restrict__ rdiag, V* b, V* zbuf,
+                                                               const V* __restrict__ inv, V* b, V* zbuf,
                                                                int* flags, int epoch, int* err, WaitTest wt,
                                                                const int* gate) {
   __shared__ V part[8][33];
-  __shared__ V Ls[32][33];
+  __shared__ V Is[2 * 32 * 32];  // L11^-1 then U11^-1 of the panel, element (i, k) at k * 32 + i
   __shared__ V accs[32];
   __shared__ int s_ok;
   if (gate && *gate) return;
@@ -413,10 +453,8 @@ __global__ void __launch_bounds__(256) blk_forward_coop_kernel(const T* __restri
   for (int p = blockIdx.x; p < npan; p += gridDim.x) {
     const int64_t j0 = ps[p], j1 = ps[p + 1];
     const int w = (int)(j1 - j0);
-    for (int k = tid; k < w * w; k += 256) {
-      const int c = k / w, i = k - c * w;
-      Ls[c][i] = V(ab[bix(L, j0 + i, j0 + c)]);
-    }
+    const V* Ip = inv + (size_t)p * 2 * kBlkW * kBlkW;
+    for (int k = tid; k < 2 * kBlkW * kBlkW; k += 256) Is[k] = __ldcg(Ip + k);
     int pf = p;  // earliest panel whose rows reach j0
     while (pf > 0 && ps[pf] + L.kl > j0) --pf;
     V acc = V(0);
@@ -436,19 +474,14 @@ __global__ void __launch_bounds__(256) blk_forward_coop_kernel(const T* __restri
                    ((part[4][lane] + part[5][lane]) + (part[6][lane] + part[7][lane]));
       __syncwarp();
       const int pr = lane < w ? perm_all[(size_t)p * kBlkW + lane] : 0;
-      V x = lane < w ? __ldcg(b + j0 + pr) - accs[pr] : V(0);
-      for (int k = 0; k < w; ++k) {  // L11 (unit lower)
-        const V xk = __shfl_sync(kFull, x, k);
-        if (lane > k && lane < w) x -= Ls[k][lane] * xk;
-      }
-      const V y1 = x;
-      V v = x;
-      for (int k = w - 1; k >= 0; --k) {  // U11, 1 / U(k, k) from rdiag
-        V yk = lane == k ? v * V(rdiag[j0 + k]) : V(0);
-        yk = __shfl_sync(kFull, yk, k);
-        if (lane == k) v = yk;
-        if (lane < k) v -= Ls[k][lane] * yk;
-      }
+      const V x = lane < w ? __ldcg(b + j0 + pr) - accs[pr] : V(0);
+      // y1 = L11^-1 P b1, z = U11^-1 y1: dot products with independent shuffles
+      V y1 = V(0);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) y1 = fma(Is[k * 32 + lane], __shfl_sync(kFull, x, k), y1);
+      V v = V(0);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) v = fma(Is[kBlkW * kBlkW + k * 32 + lane], __shfl_sync(kFull, y1, k), v);
       if (lane < w) {
         __stcg(b + j0 + lane, y1);
         __stcg(zbuf + (size_t)p * kBlkW + lane, v);
@@ -601,12 +634,16 @@ void blk_forward(const T* ab, const BandLayout& L, const BlkPlan& B, const int* 
   blk_forward_kernel<T, V><<<1, 1024, sm, st>>>(ab, L, B.d_ps, B.npan(), perm_all, rdiag, b);
 }
 template <class V, class T>
-int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, int* flags, int epoch,
+void blk_inverses(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* inv, cudaStream_t st) {
+  blk_inverses_kernel<T, V><<<(B.npan() + 3) / 4, 128, 0, st>>>(ab, L, B.d_ps, B.npan(), rdiag, inv);
+}
+template <class V, class T>
+int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const V* inv, V* y, int* flags, int epoch,
                  int* err, int grid, cudaStream_t st, WaitTest wt, const int* gate) {
   const int npan = B.npan();
   int kuf = B.kuf;
   const int* ps = B.d_ps;
-  void* args[] = {(void*)&ab,    (void*)&L,     (void*)&kuf, (void*)&ps, (void*)&npan, (void*)&rdiag,
+  void* args[] = {(void*)&ab,    (void*)&L,     (void*)&kuf, (void*)&ps, (void*)&npan, (void*)&inv,
                   (void*)&y,     (void*)&flags, (void*)&epoch, (void*)&err, (void*)&wt,  (void*)&gate};
   const cudaError_t e = cudaLaunchCooperativeKernel((const void*)blk_backward_coop_kernel<T, V>,
                                                     dim3(std::min(grid, npan)), dim3(256), args, 0, st);
@@ -619,12 +656,12 @@ void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const
 }
 // cooperative forward substitution; returns 0, or -1 if the launch was refused
 template <class V, class T>
-int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
+int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const V* inv, V* b,
                      V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st, WaitTest wt,
                      const int* gate) {
   const int npan = B.npan();
   const int* ps = B.d_ps;
-  void* args[] = {(void*)&ab,    (void*)&L,    (void*)&ps,    (void*)&npan,  (void*)&perm_all, (void*)&rdiag,
+  void* args[] = {(void*)&ab,    (void*)&L,    (void*)&ps,    (void*)&npan,  (void*)&perm_all, (void*)&inv,
                   (void*)&b,     (void*)&zbuf, (void*)&flags, (void*)&epoch, (void*)&err, (void*)&wt, (void*)&gate};
   const cudaError_t e = cudaLaunchCooperativeKernel((const void*)blk_forward_coop_kernel<T, V>,
                                                     dim3(std::min(grid, npan)), dim3(256), args, 0, st);
@@ -650,9 +687,13 @@ template void blk_forward<double, double>(const double*, const BandLayout&, cons
                                           double*, cudaStream_t);
 template void blk_forward<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*, const float*,
                                          double*, cudaStream_t);
+template void blk_inverses<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*, double*,
+                                           cudaStream_t);
+template void blk_inverses<double, float>(const float*, const BandLayout&, const BlkPlan&, const float*, double*,
+                                          cudaStream_t);
 template int blk_backward<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*, double*,
                                           int*, int, int*, int, cudaStream_t, WaitTest, const int*);
-template int blk_backward<double, float>(const float*, const BandLayout&, const BlkPlan&, const float*, double*, int*,
+template int blk_backward<double, float>(const float*, const BandLayout&, const BlkPlan&, const double*, double*, int*,
                                          int, int*, int, cudaStream_t, WaitTest, const int*);
 template void blk_backward_1cta<double, double>(const double*, const BandLayout&, const BlkPlan&, const double*,
                                                 double*, cudaStream_t);
@@ -663,8 +704,8 @@ template int blk_backward_grid<double, float>();
 template int blk_forward_coop<double, double>(const double*, const BandLayout&, const BlkPlan&, const int*,
                                               const double*, double*, double*, int*, int, int*, int, cudaStream_t,
                                               WaitTest, const int*);
-template int blk_forward_coop<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*, const float*,
-                                             double*, double*, int*, int, int*, int, cudaStream_t, WaitTest,
-                                             const int*);
+template int blk_forward_coop<double, float>(const float*, const BandLayout&, const BlkPlan&, const int*,
+                                             const double*, double*, double*, int*, int, int*, int, cudaStream_t,
+                                             WaitTest, const int*);
 
 }  // namespace mafem

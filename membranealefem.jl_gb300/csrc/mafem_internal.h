@@ -200,8 +200,12 @@ struct WaitTest {
   int limit = 0;
   int withhold = -1;
 };
+// Explicit inverses of the stored panels' L11 and U11 (inv: npan x 2 x 32 x
+// 32 in V) for the cooperative substitutions; run after each factorisation.
 template <class V, class T>
-int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* y, int* flags, int epoch,
+void blk_inverses(const T* ab, const BandLayout& L, const BlkPlan& B, const T* rdiag, V* inv, cudaStream_t st);
+template <class V, class T>
+int blk_backward(const T* ab, const BandLayout& L, const BlkPlan& B, const V* inv, V* y, int* flags, int epoch,
                  int* err, int grid, cudaStream_t st, WaitTest wt = WaitTest(), const int* gate = nullptr);
 template <class V, class T>
 int blk_backward_grid();
@@ -209,7 +213,7 @@ int blk_backward_grid();
 // cooperative launch, in place on b; zbuf: npan x 32 scratch; flags/epoch as
 // for blk_backward.  Returns 0, or -1 if the cooperative launch was refused.
 template <class V, class T>
-int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const T* rdiag, V* b,
+int blk_forward_coop(const T* ab, const BandLayout& L, const BlkPlan& B, const int* perm_all, const V* inv, V* b,
                      V* zbuf, int* flags, int epoch, int* err, int grid, cudaStream_t st, WaitTest wt = WaitTest(),
                      const int* gate = nullptr);
 // Persistent cooperative factorisation (band_lu_persist.cu): launch shape and

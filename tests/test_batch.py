@@ -191,8 +191,10 @@ def test_64x64_patch_in_the_batched_fp32_solve():
     """A 64 x 64 ALEVB patch (half bandwidth 1055) is factored by the batched
     one-patch-per-cluster FP32 solve (its panel and the tensor-core chunk
     buffers fit one CTA's shared memory); one ramped step of it within 1e-8,
-    and of the plain FP64 path within 1e-9, of the oracle's step."""
-    p, q = params_pair(M.ALEVB, M.F_PULL, 64, 64, pull_speed=0.3, pull_centre=1)
+    and of the plain FP64 path within 1e-9, of the oracle's step.  Pull speed
+    0.1: at 0.3 this fine graded patch loses Newton convergence in its first
+    step at dt 0.01 (plain FP64 as well)."""
+    p, q = params_pair(M.ALEVB, M.F_PULL, 64, 64, pull_speed=0.1, pull_centre=1)
     mesh = M.Mesh(p)
     assert mesh.half_bw == 1055
     xms, cps = state(p, mesh, seed=64, amp=0.0)
