@@ -342,7 +342,25 @@ def _relmax(a, b):
     return float(np.abs(a - b).max() / max(float(np.abs(b).max()), 1e-300))
 
 
-def run_batched(steps=None, wl=BATCH):
+def _baseline_sample(patches, per_class):
+    """Indices of the plain FP64 one-at-a-time baseline: every patch (per_class
+    = 0), or the first per_class patches of each (size, motion) class, with the
+    class counts that scale their times up to the whole set."""
+    classes = {}
+    for k, (p, _, _, _) in enumerate(patches):
+        classes.setdefault((p.num1el, p.motion), []).append(k)
+    if per_class <= 0:
+        return list(range(len(patches))), {k: 1.0 for k in range(len(patches))}
+    pick, weight = [], {}
+    for ks in classes.values():
+        sel = ks[:per_class]
+        for k in sel:
+            pick.append(k)
+            weight[k] = len(ks) / len(sel)
+    return sorted(pick), weight
+
+
+def run_batched(steps=None, wl=BATCH, baseline_per_class=0, continuous=True):
     """The batching workload, every patch for `steps` time steps (the
     workload's 30 by default) from the same seeded initial states:
     (a) plain FP64, one patch after another, each factorisation on all SMs --
@@ -354,15 +372,21 @@ def run_batched(steps=None, wl=BATCH):
     (c) the same FP32 form under continuous batching (mafem_server), every
         patch advancing through its steps on its own.
     Host wall clock around the steps, device synchronised on both sides;
-    patch time-steps/s.  No patch is left out: a failed patch-step is counted."""
+    patch time-steps/s.  No patch is left out of (b): a failed patch-step is
+    counted.  baseline_per_class > 0 times (a) on the first baseline_per_class
+    patches of every (size, motion) class and scales each class's time by its
+    patch count (a stratified estimate of the whole set's time; the errors of
+    (b) are then taken on those patches)."""
     import mafem as M
     cu = Cudart()
     steps = steps or wl["steps"]
     patches = batch_patches(M, wl)
     dt = wl["dt"]
+    base_idx, base_w = _baseline_sample(patches, baseline_per_class)
     # (a) plain FP64, one at a time
-    seq_ms, seq_state, seq_fail = 0.0, [], 0
-    for p, mesh, x0, c0 in patches:
+    seq_ms, seq_state, seq_fail = 0.0, {}, 0
+    for pk in base_idx:
+        p, mesh, x0, c0 = patches[pk]
         with M.Solver(mesh, p, M.PLAIN_FP64) as s:
             s.set_launch_ctas(0)
             s.upload(x0, c0)
@@ -378,8 +402,8 @@ def run_batched(steps=None, wl=BATCH):
                 except (M.NewtonNotConverged, M.MafemError):
                     seq_fail += 1
             cu.sync()
-            seq_ms += (time.perf_counter() - h0) * 1e3
-            seq_state.append(s.download())
+            seq_ms += base_w[pk] * (time.perf_counter() - h0) * 1e3
+            seq_state[pk] = s.download()
     # (b) the FP32 form batched, refinement to FP32_REFINE_TOL per linear solve
     # (Newton's FP64 criterion decides convergence)
     fsolvers = [M.Solver(mesh, p, M.FP32_REFINE) for p, mesh, _, _ in patches]
@@ -388,27 +412,74 @@ def run_batched(steps=None, wl=BATCH):
             s.upload(x0, c0)
             s.set_refinement(30, FP32_REFINE_TOL)
         with M.Batch(fsolvers) as b:
-            t, f_lat, f_fails, f_iters, f_sweeps = 0.0, [], 0, 0, 0
+            t, f_lat, f_fails, f_iters, f_sweeps, f_rounds, f_phase = 0.0, [], 0, 0, 0, 0, [0.0, 0.0, 0.0]
+            f_launch = 0
             for k in range(steps):
                 t += dt
                 cu.sync()
                 h0 = time.perf_counter()
                 for s in fsolvers:  # the pull's ramp, stream-ordered before the step
                     s.set_dirichlet_scale(min(1.0, (k + 1) / wl["ramp"]))
+                l0 = b.stats()["kernel_launches"]
                 status, st = b.step(t, dt)
+                f_launch += b.stats()["kernel_launches"] - l0
                 cu.sync()
                 f_lat.append((time.perf_counter() - h0) * 1e3)
                 f_fails += sum(1 for x in status if x != M.OK)
                 f_iters += sum(x["newton_iters"] for x in st)
                 f_sweeps += sum(x["refine_iters"] for x in st)
+                f_rounds += max(x["newton_iters"] for x in st)
+                for x in st:
+                    f_phase[0] += x["ms_assemble"]
+                    f_phase[1] += x["ms_factor"]
+                    f_phase[2] += x["ms_solve"]
+            b_stats = b.stats()
         f_err, forces = 0.0, []
-        for s, (xs, cs) in zip(fsolvers, seq_state):
-            xf, cf = s.download()
-            f_err = max(f_err, _relmax(xf, xs), _relmax(cf, cs))
+        for k, s in enumerate(fsolvers):
+            if k in seq_state:
+                xf, cf = s.download()
+                f_err = max(f_err, _relmax(xf, seq_state[k][0]), _relmax(cf, seq_state[k][1]))
             forces.append(float(s.pull_force()[2]))
+        bstats = b_stats
     finally:
         for s in fsolvers:
             s.close()
+    n = len(patches)
+    f_ms = sum(f_lat)
+    one = {"value": n * steps / (seq_ms / 1e3), "unit": "patch time-steps/s", "failed_patch_steps": seq_fail,
+           "form": "plain FP64, one patch after another",
+           "timed": "every patch" if len(base_idx) == n else
+                    "the first %d patches of each (size, motion) class (%d of %d), each class's time scaled by its "
+                    "patch count" % (baseline_per_class, len(base_idx), n)}
+    out = {"workload": wl["name"], "patches": n, "steps": steps,
+           "value": n * steps / (f_ms / 1e3), "unit": "patch time-steps/s",
+           "form": "FP32 tangent + batched FP32 LU (tcgen05 3xTF32 trailing update) + FP64 refinement to %g per "
+                   "solve, mafem_batch_step with batched rounds replayed from CUDA graphs" % FP32_REFINE_TOL,
+           "speedup_vs_plain_fp64_one_at_a_time": seq_ms / f_ms,
+           "p50_batch_step_ms": None, "p99_batch_step_ms": None,
+           "max_rel_err_vs_plain_fp64": f_err, "rel_err_patches": len(seq_state), "failed_patch_steps": f_fails,
+           "newton_iters_per_patch_step": f_iters / (n * steps), "refine_sweeps_per_patch_step": f_sweeps / (n * steps),
+           "rounds": f_rounds, "kernel_launches": f_launch,
+           "launches_per_round": f_launch / max(f_rounds, 1),
+           "graph_replays": bstats["graph_launches"], "graph_captures": bstats["graph_captures"],
+           "round_phase_ms": {"assemble": f_phase[0] / max(f_iters, 1), "factor_refine": f_phase[1] / max(f_iters, 1),
+                              "update": f_phase[2] / max(f_iters, 1),
+                              "note": "device time of the round's phases, averaged over the patches' iterations"},
+           "one_at_a_time": one}
+    flat = sorted(f_lat)
+
+    def pct(a, q):
+        return a[min(len(a) - 1, int(q * len(a)))]
+    out["p50_batch_step_ms"] = pct(flat, 0.5)
+    out["p99_batch_step_ms"] = pct(flat, 0.99)
+    sizes = {}
+    for p, _, _, _ in patches:
+        sizes[p.num1el] = sizes.get(p.num1el, 0) + 1
+    fz = np.array(forces)
+    out["pull_force_z_after"] = {"min": float(fz.min()), "median": float(np.median(fz)), "max": float(fz.max())}
+    out["size_histogram"] = {str(k): v for k, v in sorted(sizes.items())}
+    if not continuous:
+        return out
     # (c) continuous batching of the same FP32 solves
     with M.Server() as srv:
         ids = [srv.submit(mesh, p, x0, c0, steps, dt, precision=M.FP32_REFINE, refine_tol=FP32_REFINE_TOL,
@@ -427,38 +498,17 @@ def run_batched(steps=None, wl=BATCH):
         c_wall = time.perf_counter() - h0
         c_stats = srv.stats()
     c_err, c_fail = 0.0, 0
-    for k, (xs, cs) in enumerate(seq_state):
+    for k in range(n):
         stt, xc, cc = got[k]
         c_fail += stt != M.OK
-        c_err = max(c_err, _relmax(xc, xs), _relmax(cc, cs))
-    n = len(patches)
-    f_ms = sum(f_lat)
-    flat = sorted(f_lat)
-
-    def pct(a, q):
-        return a[min(len(a) - 1, int(q * len(a)))]
-    sizes = {}
-    for p, _, _, _ in patches:
-        sizes[p.num1el] = sizes.get(p.num1el, 0) + 1
-    fz = np.array(forces)
-    return {"workload": wl["name"], "patches": n, "steps": steps,
-            "value": n * steps / (f_ms / 1e3), "unit": "patch time-steps/s",
-            "form": "FP32 tangent + batched FP32 LU (tcgen05 3xTF32 trailing update) + FP64 refinement to %g per "
-                    "solve, mafem_batch_step" % FP32_REFINE_TOL,
-            "speedup_vs_plain_fp64_one_at_a_time": seq_ms / f_ms,
-            "p50_batch_step_ms": pct(flat, 0.5), "p99_batch_step_ms": pct(flat, 0.99),
-            "max_rel_err_vs_plain_fp64": f_err, "failed_patch_steps": f_fails,
-            "newton_iters_per_patch_step": f_iters / (n * steps), "refine_sweeps_per_patch_step": f_sweeps / (n * steps),
-            "one_at_a_time": {"value": n * steps / (seq_ms / 1e3), "unit": "patch time-steps/s",
-                              "failed_patch_steps": seq_fail, "form": "plain FP64, one patch after another"},
-            "continuous": {"value": n * steps / c_wall, "unit": "patch time-steps/s",
-                           "speedup_vs_plain_fp64_one_at_a_time": (n * steps / c_wall) / (n * steps / (seq_ms / 1e3)),
-                           "p50_step_ms": c_stats["p50_step_ms"], "p99_step_ms": c_stats["p99_step_ms"],
-                           "max_rel_err_vs_plain_fp64": c_err, "failed_patches": c_fail,
-                           "form": "the FP32 form under continuous batching (mafem_server), all patches submitted "
-                                   "at once"},
-            "pull_force_z_after": {"min": float(fz.min()), "median": float(np.median(fz)), "max": float(fz.max())},
-            "size_histogram": {str(k): v for k, v in sorted(sizes.items())}}
+        if k in seq_state:
+            c_err = max(c_err, _relmax(xc, seq_state[k][0]), _relmax(cc, seq_state[k][1]))
+    out["continuous"] = {"value": n * steps / c_wall, "unit": "patch time-steps/s",
+                         "speedup_vs_plain_fp64_one_at_a_time": (n * steps / c_wall) / (n * steps / (seq_ms / 1e3)),
+                         "p50_step_ms": c_stats["p50_step_ms"], "p99_step_ms": c_stats["p99_step_ms"],
+                         "max_rel_err_vs_plain_fp64": c_err, "failed_patches": c_fail,
+                         "form": "the FP32 form under continuous batching (mafem_server), all patches submitted at once"}
+    return out
 
 
 SERVE = dict(name="serving workload: Poisson arrivals of tether-pull solves, n in {8,16,32,64} elements per side "
@@ -469,17 +519,19 @@ SERVE = dict(name="serving workload: Poisson arrivals of tether-pull solves, n i
              steps=(20, 100), dt=0.01, ramp=30)
 
 
-def serve_requests(M, wl=SERVE):
-    """The request sample: (Params, Mesh, xms, cps, steps, arrival offset at rate 1/s)."""
+def serve_requests(M, wl=SERVE, requests=None, step_scale=1.0):
+    """The request sample: (Params, Mesh, xms, cps, steps, arrival offset at rate 1/s);
+    the first `requests` of the seeded stream, each request's step count scaled
+    by step_scale (at least 1)."""
     rng = np.random.default_rng(wl["seed"])
     out = []
     t = 0.0
-    for k in range(wl["requests"]):
+    for k in range(requests or wl["requests"]):
         n = int(rng.choice(wl["sizes"], p=wl["probs"]))
         kb = float(np.exp(rng.uniform(np.log(0.5), np.log(2.0))))
         lam0 = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
         f = float(rng.uniform(2.0, 10.0))
-        steps = int(rng.integers(wl["steps"][0], wl["steps"][1] + 1))
+        steps = max(1, int(round(step_scale * int(rng.integers(wl["steps"][0], wl["steps"][1] + 1)))))
         t += float(rng.exponential(1.0))
         motion = M.LAG if k % 2 == 0 else M.ALEVB
         p = M.Params(motion=motion, scenario=M.F_PULL, num1el=n, num2el=n, length=1.0, kb=kb, lambda0=lam0,
@@ -490,16 +542,17 @@ def serve_requests(M, wl=SERVE):
     return out
 
 
-def run_serving(wl=SERVE):
+def run_serving(wl=SERVE, requests=None, step_scale=1.0):
     """Continuous batching (mafem_server) of a Poisson stream of requests at each
     rate, every request in the FP32 form with batched solves, against the same
     requests solved one at a time with the plain FP64 path.  Per-step latency is
     the wall time from a step's first Newton iteration to its convergence;
     throughput is time steps per wall second from the first arrival to the last
-    result."""
+    result.  requests / step_scale bound the sample (the first requests of the
+    stream, their step counts scaled)."""
     import mafem as M
     cu = Cudart()
-    reqs = serve_requests(M, wl)
+    reqs = serve_requests(M, wl, requests, step_scale)
     dt = wl["dt"]
     # plain FP64, one at a time
     seq_s, ref, total_steps = 0.0, [], 0
@@ -523,7 +576,9 @@ def run_serving(wl=SERVE):
             ref.append(s.download() if ok else None)
         total_steps += steps
     out = {"workload": wl["name"], "requests": len(reqs),
-           "steps_per_request": "U{%d..%d}" % (wl["steps"][0], wl["steps"][1]), "time_steps": total_steps,
+           "steps_per_request": "U{%d..%d}" % (wl["steps"][0], wl["steps"][1]) +
+                                (" scaled by %g" % step_scale if step_scale != 1.0 else ""),
+           "time_steps": total_steps,
            "plain_fp64_one_at_a_time": {"value": total_steps / seq_s, "unit": "time-steps/s"}, "rates": {}}
     for rate in wl["rates"]:
         with M.Server() as srv:
@@ -599,9 +654,10 @@ def _pull_state(mesh, cps, vz, vx):
     return cps
 
 
-def run_precision64(wl=PREC64):
+def run_precision64(wl=PREC64, max_steps=0):
     """Per-step relative error of the FP32 form against plain FP64 on the precision
-    workload, and both forms' time-steps/s (device time of each Newton loop)."""
+    workload, and both forms' time-steps/s (device time of each Newton loop);
+    max_steps > 0 runs only the workload's first max_steps steps."""
     import mafem as M
     p = M.Params(motion=wl["motion"], scenario=M.F_PULL, num1el=wl["n"], num2el=wl["n"], length=1.0,
                  pull_speed=wl["pull_speed"], pull_centre=1)
@@ -617,7 +673,7 @@ def run_precision64(wl=PREC64):
         s64.upload(x0, c0)
         s32.upload(x0, c0)
         t = 0.0
-        for k in range(npull + ntr):
+        for k in range(npull + ntr if max_steps <= 0 else min(max_steps, npull + ntr)):
             for s in (s64, s32):
                 if k < npull:
                     s.set_dirichlet_scale((k + 1) / npull)
@@ -767,6 +823,10 @@ def main():
     ap.add_argument("--batch-steps", type=int, default=0, help="time steps of the batching workload (0: its 30)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-precision", action="store_true", help="skip the 64 x 64 precision measurement")
+    ap.add_argument("--full", action="store_true",
+                    help="the batching, serving and precision workloads in full (about half an hour): the plain "
+                         "FP64 baseline on every patch, continuous batching, every serving request's full step "
+                         "count, all 140 precision steps; by default each is a bounded sample")
     ap.add_argument("--case", choices=["fp32-patch32", "fp32-batch16"],
                     help="run a small profiling case instead of the bench (prints no bench line)")
     args = ap.parse_args()
@@ -843,11 +903,12 @@ def main():
         "mesh": r["mesh"],
     }
     if rank == 0 and not args.no_batch:
-        line["batched"] = run_batched(args.batch_steps)
+        line["batched"] = run_batched(args.batch_steps, baseline_per_class=0 if args.full else 2,
+                                      continuous=args.full)
     if rank == 0 and not args.no_serve:
-        line["serving"] = run_serving()
+        line["serving"] = run_serving(requests=None if args.full else 16, step_scale=1.0 if args.full else 0.1)
     if rank == 0 and not args.no_precision:
-        line["precision_64"] = run_precision64()
+        line["precision_64"] = run_precision64(max_steps=0 if args.full else 6)
     if rank == 0 and not args.no_cpu_baseline:
         ref = {}
         line["cpu_baseline"] = cpu_baseline(warmup=args.warmup, max_steps=2, state_out=ref)
@@ -865,7 +926,9 @@ def main():
                 "plain_fp64_one_at_a_time_patch_steps_per_s": b["one_at_a_time"]["value"],
                 "ratio": b["speedup_vs_plain_fp64_one_at_a_time"], "target_ratio": 10.0,
                 "p99_batch_step_ms": b["p99_batch_step_ms"], "max_rel_err_vs_plain_fp64": b["max_rel_err_vs_plain_fp64"],
-                "failed_patch_steps": b["failed_patch_steps"], "patches": b["patches"], "steps": b["steps"]}
+                "failed_patch_steps": b["failed_patch_steps"], "patches": b["patches"], "steps": b["steps"],
+                "launches_per_round": b["launches_per_round"], "graph_replays": b["graph_replays"],
+                "baseline_timed": b["one_at_a_time"]["timed"]}
         print(json.dumps(line))
 
 

@@ -264,6 +264,26 @@ int mafem_batch_destroy(mafem_batch* b);
  * patches instead (each with its own multi-CTA factorisation).  Returns 1 if
  * the batched solve is in use. */
 int mafem_batch_set_patch_solve(mafem_batch* b, int32_t on);
+/* Newton rounds of the batched solve's patches (no counterpart in the
+ * reference, whose time_step! advances one patch).  batched_assembly != 0 (the
+ * default): every round assembles all of those patches with one launch per
+ * kernel (the element kernels once per motion), factors and refines them
+ * (mafem_batch_set_patch_solve), then updates them and forms their Newton
+ * norms with one launch each, and reads all their results with one copy --
+ * a fixed number of launches per round, whatever the patch count.  They
+ * run the per-patch kernels' arithmetic on the same element-to-CTA map (the
+ * element kernels compiled separately, so a multiply-add may round
+ * differently).  graphs != 0 (the
+ * default): such a round is captured as a CUDA graph the first time its
+ * sequence of patches occurs and replayed from then on.  Returns MAFEM_OK. */
+int mafem_batch_set_rounds(mafem_batch* b, int32_t batched_assembly, int32_t graphs);
+typedef struct mafem_batch_stats {
+  int64_t graph_launches;   /* rounds replayed from a CUDA graph */
+  int64_t graph_captures;   /* rounds captured */
+  int64_t graphs_cached;    /* graphs held now */
+  int64_t kernel_launches;  /* kernels enqueued by the batch's handles and rounds */
+} mafem_batch_stats;
+int mafem_batch_get_stats(const mafem_batch* b, mafem_batch_stats* out);
 /* CTAs of this handle's persistent factorisation and back substitution (0: all
  * SMs); clamped to what the band needs.  Returns the CTAs the factorisation uses. */
 int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas);

@@ -1141,9 +1141,16 @@ enum { kIterAgain = -100, kIterDone = -101 };
 
 // Wait for the enqueued iteration and apply the Newton criterion: kIterAgain,
 // kIterDone (converged), or a status.
+static int iter_decide(mafem_handle* h);
 static int iter_finish(mafem_handle* h) {
   CK(cudaEventSynchronize(h->ev[4]));
   accum_times(h);
+  return iter_decide(h);
+}
+// The Newton criterion on the iteration's results in h_out (eps, |r|, the
+// non-finite flag and the info words), redoing the iteration with the
+// handle's own solver where the solve failed.
+static int iter_decide(mafem_handle* h) {
   if (!std::isfinite(h->h_out[1])) {  // the FP64 residual itself is not finite: nothing to redo
     h->err = "non-finite residual";
     return MAFEM_NAN_DETECTED;
@@ -1228,9 +1235,9 @@ static int iter_finish(mafem_handle* h) {
   return kIterAgain;
 }
 
-static void step_stats(mafem_handle* h, mafem_step_stats* stats) {
+static void step_stats(mafem_handle* h, mafem_step_stats* stats, cudaEvent_t end = nullptr) {
   float ms_t = 0;
-  cudaEventElapsedTime(&ms_t, h->ev[5], h->ev[4]);
+  cudaEventElapsedTime(&ms_t, h->ev[5], end ? end : h->ev[4]);
   h->ss_S.ms_total = ms_t;
   if (stats) *stats = h->ss_S;
 }
@@ -1390,6 +1397,103 @@ static void order_patch_jobs(std::vector<mafem_handle*>& hv, std::vector<int>& i
   }
 }
 
+// A batched round's host/device buffer: the items (patches of the round in
+// motion groups), then per kernel kind the CTA offsets off[0 .. m] --
+// 0 residual, 1 tangent, 2 band gather, 3 residual gather, 4 update, 5 predictor.
+namespace {
+constexpr int kOffKinds = 6;
+struct RoundLayout {
+  size_t off[kOffKinds];
+  size_t bytes;
+};
+RoundLayout round_layout(int m) {
+  RoundLayout R{};
+  size_t p = ((size_t)m * sizeof(AsmItem) + 15) & ~(size_t)15;
+  for (int t = 0; t < kOffKinds; ++t) {
+    R.off[t] = p;
+    p = (p + (size_t)(m + 1) * sizeof(int) + 15) & ~(size_t)15;
+  }
+  R.bytes = p;
+  return R;
+}
+constexpr int kOffDir = kOffKinds;  // 6: Dirichlet scaling (a seventh offset array)
+
+// One stream of batched Newton rounds (a batch has one, a server one per
+// solve lane): its streams, round buffers, result rows, timing events and the
+// CUDA graphs of the rounds it has run.
+struct RoundRunner {
+  cudaStream_t st = nullptr, st2 = nullptr;  // clusters / single CTAs of the factorisation
+  cudaEvent_t efork = nullptr, ejoin = nullptr;
+  cudaEvent_t rev[4] = {};  // start, assembled, solved, done
+  unsigned char* d_round = nullptr;
+  unsigned char* h_round = nullptr;  // pinned
+  AsmOut* d_outs = nullptr;
+  AsmOut* h_outs = nullptr;  // pinned
+  int* d_order = nullptr;
+  int* h_order = nullptr;  // pinned
+  int cap = 0;              // patches per round at most
+  bool graph_on = true;
+  std::map<std::vector<int64_t>, cudaGraphExec_t> graphs;
+  int64_t graph_launches = 0, graph_captures = 0;
+  std::vector<int> items_of;  // the last round's result rows: index of each row's handle
+  bool busy = false;
+
+  cudaError_t init(int max_patches) {
+    cap = max_patches;
+    const size_t rb = round_layout(cap).bytes + (size_t)(cap + 1) * sizeof(int) + 16;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&efork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ejoin, cudaEventDisableTiming);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) e = cudaEventCreate(&rev[k]);
+    if (e == cudaSuccess) e = cudaMalloc(&d_round, rb);
+    if (e == cudaSuccess) e = cudaMallocHost(&h_round, rb);
+    if (e == cudaSuccess) e = cudaMalloc(&d_outs, (size_t)cap * sizeof(AsmOut));
+    if (e == cudaSuccess) e = cudaMallocHost(&h_outs, (size_t)cap * sizeof(AsmOut));
+    if (e == cudaSuccess) e = cudaMalloc(&d_order, (size_t)cap * sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocHost(&h_order, (size_t)cap * sizeof(int));
+    return e;
+  }
+  ~RoundRunner() {
+    if (st) cudaStreamSynchronize(st);
+    if (st2) cudaStreamSynchronize(st2);
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    for (cudaEvent_t e : {efork, ejoin, rev[0], rev[1], rev[2], rev[3]})
+      if (e) cudaEventDestroy(e);
+    if (d_round) cudaFree(d_round);
+    if (h_round) cudaFreeHost(h_round);
+    if (d_outs) cudaFree(d_outs);
+    if (h_outs) cudaFreeHost(h_outs);
+    if (d_order) cudaFree(d_order);
+    if (h_order) cudaFreeHost(h_order);
+    if (st2) cudaStreamDestroy(st2);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+}  // namespace
+
+// The batched-round view of a handle's FP32 patch (its job in a round).
+static AsmJob asm_job(const mafem_handle* h) {
+  AsmJob a{};
+  a.P = h->P;
+  a.pp = h->pp;
+  a.L = h->L;
+  a.r_el = h->d_rel;
+  a.K_el = (float*)h->d_Kel;
+  a.band = (float*)h->d_band;
+  a.band0 = (float*)h->d_band0;
+  a.r = h->d_r;
+  a.x = h->d_x;
+  a.part = h->d_part;
+  a.out = h->d_out;
+  a.info = h->d_info;
+  a.dir_idx = h->d_dir_idx;
+  a.dir_val = h->d_dir_val;
+  a.n_dir = h->n_dir;
+  return a;
+}
+
 struct mafem_batch {
   std::vector<mafem_handle*> hs;
   // batched FP32 solve: the handles whose band fits one CTA (patch_ok)
@@ -1404,9 +1508,16 @@ struct mafem_batch {
   size_t smem_f = 0, smem_r = 0;
   int max_sweeps = 30;
   double tol = 1e-10;
+  // batched rounds of the FP32 patch jobs: one launch per kernel (per motion
+  // for the element kernels) per Newton round, indexed by slot like d_jobs
+  bool asm_on = false;
+  AsmJob* d_ajobs = nullptr;
+  std::unique_ptr<RoundRunner> rr;
   ~mafem_batch() {
     if (bst) cudaStreamSynchronize(bst);
     if (bst2) cudaStreamSynchronize(bst2);
+    rr.reset();
+    if (d_ajobs) cudaFree(d_ajobs);
     if (efork) cudaEventDestroy(efork);
     if (ejoin) cudaEventDestroy(ejoin);
     if (bst2) cudaStreamDestroy(bst2);
@@ -1417,6 +1528,7 @@ struct mafem_batch {
     if (bst) cudaStreamDestroy(bst);
   }
 };
+
 
 extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ctas, mafem_batch** out) {
   if (!out || n < 0 || (n > 0 && !hs) || ctas < 0) {
@@ -1474,6 +1586,22 @@ extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ct
       }
     }
     b->patch_on = true;
+    // the batched rounds' job table and runner
+    std::vector<AsmJob> aj;
+    for (int i = 0; i < n; ++i)
+      if (b->slot[i] >= 0) aj.push_back(asm_job(b->hs[i]));
+    e = batch_asm_setup();
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_ajobs, nj * sizeof(AsmJob));
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_ajobs, aj.data(), nj * sizeof(AsmJob), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+      b->rr = std::make_unique<RoundRunner>();
+      e = b->rr->init((int)nj);
+    }
+    if (e != cudaSuccess) {
+      set_global_error(std::string("mafem_batch_create: ") + cudaGetErrorString(e));
+      return MAFEM_ERR_CUDA;
+    }
+    b->asm_on = true;
   }
   *out = b.release();
   return MAFEM_OK;
@@ -1490,37 +1618,218 @@ extern "C" int mafem_batch_destroy(mafem_batch* b) {
   return MAFEM_OK;
 }
 
+// One batched Newton round of the FP32 patches hv[pj] (ordered for the
+// factorisation: the first n4 on four-CTA clusters, the next n2 on two; job
+// index slot_of[i], step-start flags start[i] and Dirichlet scale dscale[i]
+// per handle) on R's streams: the Dirichlet scaling and the predictor of the
+// patches that start a time step, the FP64 residual and FP32 tangent kernels
+// per motion, both band gathers and the residual gather, the batched factor /
+// refine (patch_solve), the Newton update and norms of every patch, and the
+// copy of the results to R.h_outs (row k: handle R.items_of[k]).  With
+// R.graph_on a round is captured as a CUDA graph the first time its sequence
+// of patches occurs and replayed from then on.  *launches: kernels per round.
+static cudaError_t run_round(RoundRunner& R, const PatchJob* d_jobs, const AsmJob* d_ajobs, size_t smem_f,
+                             size_t smem_r, const std::vector<mafem_handle*>& hv, const std::vector<int>& slot_of,
+                             const std::vector<int>& pj, int n4, int n2, int max_sweeps, double tol,
+                             const std::vector<int>& start, const std::vector<double>& dscale, int* launches) {
+  const int m = (int)pj.size();
+  if (m > R.cap) return cudaErrorInvalidValue;
+  const RoundLayout RL = round_layout(m);
+  const size_t dir_off = RL.bytes;  // the seventh offset array follows the layout
+  std::vector<int>& it = R.items_of;
+  it.assign(pj.begin(), pj.end());
+  auto gkey = [&](int i) { return std::make_pair(hv[i]->pp.motion, hv[i]->pp.nq); };
+  std::stable_sort(it.begin(), it.end(), [&](int a, int c) { return gkey(a) < gkey(c); });
+  AsmItem* items = reinterpret_cast<AsmItem*>(R.h_round);
+  int* off[kOffKinds + 1];
+  for (int t = 0; t < kOffKinds; ++t) off[t] = reinterpret_cast<int*>(R.h_round + RL.off[t]);
+  off[kOffDir] = reinterpret_cast<int*>(R.h_round + dir_off);
+  for (int t = 0; t <= kOffDir; ++t) off[t][0] = 0;
+  std::vector<int> groups{0};  // item ranges of one (motion, nq)
+  bool any_pred = false, any_dir = false;
+  for (int k = 0; k < m; ++k) {
+    const int i = it[k];
+    const mafem_handle* h = hv[i];
+    items[k].job = slot_of[i];
+    items[k].start = start[i];
+    items[k].time = h->ss_time;
+    items[k].dt = h->ss_dt;
+    items[k].dscale = dscale[i];
+    off[0][k + 1] = off[0][k] + batch_resid_ctas(h->numel);
+    off[1][k + 1] = off[1][k] + batch_tan_ctas(h->numel);
+    off[2][k + 1] = off[2][k] + batch_gather_ctas(h->L.n);
+    off[3][k + 1] = off[3][k] + batch_rgather_ctas(h->nmdf);
+    off[4][k + 1] = off[4][k] + newton_update_blocks(h->nmdf);
+    off[5][k + 1] = off[5][k] + ((start[i] & kStartPredict) ? batch_pred_ctas(h->numnp) : 0);
+    off[kOffDir][k + 1] = off[kOffDir][k] + ((start[i] & kStartDirichlet) ? batch_dir_ctas(h->n_dir) : 0);
+    any_pred |= (start[i] & kStartPredict) != 0;
+    any_dir |= (start[i] & kStartDirichlet) != 0 && h->n_dir > 0;
+    if (k + 1 < m && gkey(it[k + 1]) != gkey(it[k])) groups.push_back(k + 1);
+  }
+  groups.push_back(m);
+  const size_t bytes = dir_off + (size_t)(m + 1) * sizeof(int);
+  for (int k = 0; k < m; ++k) R.h_order[k] = slot_of[pj[k]];
+  const unsigned char* dr = R.d_round;
+  const AsmItem* d_items = reinterpret_cast<const AsmItem*>(dr);
+  auto d_off = [&](int t, int g0) {
+    return reinterpret_cast<const int*>(dr + (t == kOffDir ? dir_off : RL.off[t])) + g0;
+  };
+  const int ng = (int)groups.size() - 1;
+  *launches = (any_dir ? 1 : 0) + (any_pred ? 1 : 0) + 2 * ng + 2 + patch_solve_launches(n4, n2, m) + 2;
+
+  auto enqueue = [&](bool capturing) -> cudaError_t {
+    const unsigned fl = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    cudaStream_t st = R.st;
+    cudaError_t e = cudaMemcpyAsync(R.d_round, R.h_round, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(R.d_order, R.h_order, m * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(R.rev[0], st, fl);
+    if (e == cudaSuccess && any_dir) {
+      launch_batch_dirichlet(d_ajobs, d_items, d_off(kOffDir, 0), m, off[kOffDir][m], st);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && any_pred) {
+      launch_batch_predictor(d_ajobs, d_items, d_off(5, 0), m, off[5][m], st);
+      e = cudaGetLastError();
+    }
+    for (int g = 0; g < ng && e == cudaSuccess; ++g) {
+      const int g0 = groups[g], g1 = groups[g + 1];
+      const mafem_handle* h = hv[it[g0]];
+      e = launch_batch_resid(h->pp.motion, d_ajobs, d_items + g0, d_off(0, g0), g1 - g0, off[0][g1] - off[0][g0],
+                             h->pp.nq, st);
+      if (e == cudaSuccess)
+        e = launch_batch_tan(h->pp.motion, d_ajobs, d_items + g0, d_off(1, g0), g1 - g0, off[1][g1] - off[1][g0],
+                             h->pp.nq, st);
+    }
+    if (e == cudaSuccess) {
+      launch_batch_gather(d_ajobs, d_items, d_off(2, 0), m, off[2][m], st);
+      launch_batch_rgather(d_ajobs, d_items, d_off(3, 0), m, off[3][m], st);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(R.rev[1], st, fl);
+    if (e == cudaSuccess)
+      e = patch_solve(d_jobs, R.d_order, n4, n2, m, smem_f, smem_r, max_sweeps, tol, st, R.st2, R.efork, R.ejoin);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(R.rev[2], st, fl);
+    if (e == cudaSuccess) {
+      launch_batch_update(d_ajobs, d_items, d_off(4, 0), m, off[4][m], R.d_outs, st);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(R.h_outs, R.d_outs, m * sizeof(AsmOut), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaEventRecordWithFlags(R.rev[3], st, fl);
+    return e;
+  };
+
+  if (!R.graph_on) return enqueue(false);
+  // the graph's key: everything its nodes bake in (grids, copy sizes, kernel arguments)
+  // (a job's shape too: a slot of a server may hold another patch later)
+  std::vector<int64_t> key{m, n4, n2, max_sweeps, (int64_t)smem_f, (int64_t)smem_r};
+  int64_t tb;
+  std::memcpy(&tb, &tol, sizeof tb);
+  key.push_back(tb);
+  for (int k = 0; k < m; ++k) {
+    const mafem_handle* h = hv[it[k]];
+    key.push_back((int64_t)items[k].job * 4 + items[k].start);
+    key.push_back(((int64_t)h->numel << 32) | (uint32_t)h->numnp);
+    key.push_back((h->nmdf << 24) | ((int64_t)h->n_dir << 8) | (h->pp.motion << 4) | (h->ndf & 15));
+  }
+  for (int k = 0; k < m; ++k) key.push_back(R.h_order[k]);
+  auto found = R.graphs.find(key);
+  if (found == R.graphs.end()) {
+    if (R.graphs.size() >= 256) {
+      for (auto& g : R.graphs) cudaGraphExecDestroy(g.second);
+      R.graphs.clear();
+    }
+    cudaError_t e = cudaStreamBeginCapture(R.st, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const cudaError_t ee = enqueue(true);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(R.st, &graph);
+    cudaGraphExec_t exec = nullptr;
+    if (ee == cudaSuccess && e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (ee != cudaSuccess || e != cudaSuccess) {
+      cudaGetLastError();
+      R.graph_on = false;  // capture refused: plain stream launches from now on
+      return enqueue(false);
+    }
+    found = R.graphs.emplace(key, exec).first;
+    ++R.graph_captures;
+  }
+  ++R.graph_launches;
+  return cudaGraphLaunch(found->second, R.st);
+}
+
+// After R's round completed: each patch's results into its handle's h_out
+// (eps, |r|, the non-finite flag, the info words) and the round's phase times
+// into its step stats.
+static void round_results(RoundRunner& R, const std::vector<mafem_handle*>& hv) {
+  float ms_a = 0, ms_f = 0, ms_s = 0;
+  cudaEventElapsedTime(&ms_a, R.rev[0], R.rev[1]);
+  cudaEventElapsedTime(&ms_f, R.rev[1], R.rev[2]);
+  cudaEventElapsedTime(&ms_s, R.rev[2], R.rev[3]);
+  for (size_t k = 0; k < R.items_of.size(); ++k) {
+    mafem_handle* h = hv[R.items_of[k]];
+    const AsmOut& o = R.h_outs[k];
+    h->h_out[0] = o.out[0];
+    h->h_out[1] = o.out[1];
+    h->h_out[2] = o.out[2];
+    std::memcpy(h->h_out + 5, o.info, sizeof o.info);
+    h->ss_patch = true;
+    h->ss_async = false;
+    h->ss_sweeps = 0;
+    h->factored = false;
+    h->ss_S.ms_assemble += ms_a;
+    h->ss_S.ms_factor += ms_f;
+    h->ss_S.ms_solve += ms_s;
+  }
+}
+
 // One time step of every patch: predictor + Newton, the patches' iterations
-// interleaved -- every active patch's iteration k is enqueued (each handle on
-// its own stream) before any is waited for, so their kernels overlap.  FP32
-// patches whose band fits one CTA are factored and solved together: after
-// their assemblies, one launch factors all of them and one more solves and
-// refines all of them (one CTA per patch, largest first).
+// interleaved -- every active patch's iteration k is enqueued before any is
+// waited for, so their kernels overlap.  FP32 patches whose band fits the
+// batched solve run as batched rounds (batch_round: one launch per kernel for
+// all of them, replayed from a CUDA graph); the other patches run their own
+// iterations on their own streams beside them.
 extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const double* dts, int32_t* status,
                                 mafem_step_stats* stats) {
   if (!b || !times || !dts) return MAFEM_ERR_ARG;
   const int n = (int)b->hs.size();
+  const bool basm = b->asm_on && b->patch_on && b->rr;
   std::vector<int> active, st(n, MAFEM_OK);
+  std::vector<int> start(n, 0);
+  const std::vector<double> dscale(n, 1.0);
   for (int i = 0; i < n; ++i) {
     mafem_handle* h = b->hs[i];
-    launch_predictor(h->P, h->pp, dts[i], h->st);  // update_xms! (Analysis.jl:70)
-    h->launches += 1;
+    const bool bp = basm && b->slot[i] >= 0;
+    if (!bp) {
+      launch_predictor(h->P, h->pp, dts[i], h->st);  // update_xms! (Analysis.jl:70)
+      h->launches += 1;
+    }
     step_begin(h, times[i], dts[i]);
+    if (bp) {
+      start[i] = kStartPredict;  // the predictor runs in the step's first round
+      cudaStreamWaitEvent(b->rr->st, h->ev[5], 0);  // the caller's work on the handle's stream first
+    }
     active.push_back(i);
   }
   std::vector<int> pj;
+  std::vector<char> batched(n, 0);
   while (!active.empty()) {
     std::vector<int> next;
     pj.clear();
     for (int i : active) {
       mafem_handle* h = b->hs[i];
       const bool patch = b->patch_on && b->slot[i] >= 0;
+      if (patch && basm) {
+        pj.push_back(i);
+        continue;
+      }
       const int rc = patch ? iter_enqueue_patch_begin(h) : iter_enqueue(h);
       if (rc != MAFEM_OK)
         st[i] = rc;
       else if (patch)
         pj.push_back(i);
     }
+    bool round_ok = false;
     if (!pj.empty()) {
       int n4 = 0, n2 = 0;
       choose_patch_ctas(b->hs, pj);
@@ -1532,37 +1841,62 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
         b->max_sweeps = std::max(b->max_sweeps, b->hs[i]->max_refine);
         b->tol = std::min(b->tol, b->hs[i]->refine_tol);
       }
-      for (size_t k = 0; k < pj.size(); ++k) {
-        b->h_order[k] = b->slot[pj[k]];
-        cudaStreamWaitEvent(b->bst, b->hs[pj[k]]->ev[1], 0);
-      }
-      cudaError_t e = cudaMemcpyAsync(b->d_order, b->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice, b->bst);
-      if (e == cudaSuccess)
-        e = patch_solve(b->d_jobs, b->d_order, n4, n2, (int)pj.size(), b->smem_f, b->smem_r, b->max_sweeps, b->tol,
-                        b->bst, b->bst2, b->efork, b->ejoin);
-      if (e == cudaSuccess) e = cudaEventRecord(b->bev, b->bst);
-      for (int i : pj) {
-        mafem_handle* h = b->hs[i];
+      if (basm) {
+        int nl = 0;
+        cudaError_t e = run_round(*b->rr, b->d_jobs, b->d_ajobs, b->smem_f, b->smem_r, b->hs, b->slot, pj, n4, n2,
+                                  b->max_sweeps, b->tol, start, dscale, &nl);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b->rr->rev[3]);
+        for (int i : pj) start[i] = 0;
         if (e != cudaSuccess) {
-          h->err = std::string("batched FP32 solve: ") + cudaGetErrorString(e);
-          st[i] = MAFEM_ERR_CUDA;
-          continue;
+          for (int i : pj) {
+            b->hs[i]->err = std::string("batched round: ") + cudaGetErrorString(e);
+            st[i] = MAFEM_ERR_CUDA;
+          }
+        } else {
+          round_ok = true;
+          b->hs[pj[0]]->launches += nl;
+          round_results(*b->rr, b->hs);
+          for (int i : b->rr->items_of) batched[i] = 1;
         }
-        if (i == pj[0]) h->launches += patch_solve_launches(n4, n2, (int)pj.size());  // counted once
-        const int rc = iter_enqueue_patch_end(h, b->bev);
-        if (rc != MAFEM_OK) st[i] = rc;
+      } else {
+        for (size_t k = 0; k < pj.size(); ++k) {
+          b->h_order[k] = b->slot[pj[k]];
+          cudaStreamWaitEvent(b->bst, b->hs[pj[k]]->ev[1], 0);
+        }
+        cudaError_t e =
+            cudaMemcpyAsync(b->d_order, b->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice, b->bst);
+        if (e == cudaSuccess)
+          e = patch_solve(b->d_jobs, b->d_order, n4, n2, (int)pj.size(), b->smem_f, b->smem_r, b->max_sweeps,
+                          b->tol, b->bst, b->bst2, b->efork, b->ejoin);
+        if (e == cudaSuccess) e = cudaEventRecord(b->bev, b->bst);
+        for (int i : pj) {
+          mafem_handle* h = b->hs[i];
+          if (e != cudaSuccess) {
+            h->err = std::string("batched FP32 solve: ") + cudaGetErrorString(e);
+            st[i] = MAFEM_ERR_CUDA;
+            continue;
+          }
+          if (i == pj[0]) h->launches += patch_solve_launches(n4, n2, (int)pj.size());  // counted once
+          const int rc = iter_enqueue_patch_end(h, b->bev);
+          if (rc != MAFEM_OK) st[i] = rc;
+        }
       }
     }
     for (int i : active) {
       if (st[i] != MAFEM_OK) continue;
-      const int rc = iter_finish(b->hs[i]);
+      mafem_handle* h = b->hs[i];
+      const bool in_round = basm && round_ok && batched[i];
+      const int64_t fb = h->fallbacks;
+      const int rc = in_round ? iter_decide(h) : iter_finish(h);
       if (rc == kIterAgain) {
         next.push_back(i);
       } else {
         st[i] = rc == kIterDone ? MAFEM_OK : rc;
-        step_stats(b->hs[i], stats ? stats + i : nullptr);
+        // a batched patch's step ends with its round (or with its own redo of the last iteration)
+        step_stats(h, stats ? stats + i : nullptr, in_round && h->fallbacks == fb ? b->rr->rev[3] : nullptr);
       }
     }
+    std::fill(batched.begin(), batched.end(), 0);
     active.swap(next);
   }
   int first = MAFEM_OK;
@@ -1576,20 +1910,43 @@ extern "C" int mafem_batch_step(mafem_batch* b, const double* times, const doubl
   return first;
 }
 
+extern "C" int mafem_batch_set_rounds(mafem_batch* b, int32_t batched_assembly, int32_t graphs) {
+  if (!b) return MAFEM_ERR_ARG;
+  b->asm_on = batched_assembly != 0 && b->rr != nullptr;
+  if (b->rr) b->rr->graph_on = graphs != 0;
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_batch_get_stats(const mafem_batch* b, mafem_batch_stats* out) {
+  if (!b || !out) return MAFEM_ERR_ARG;
+  out->graph_launches = b->rr ? b->rr->graph_launches : 0;
+  out->graph_captures = b->rr ? b->rr->graph_captures : 0;
+  out->graphs_cached = b->rr ? (int64_t)b->rr->graphs.size() : 0;
+  int64_t l = 0;
+  for (const mafem_handle* h : b->hs) l += h->launches;
+  out->kernel_launches = l;
+  return MAFEM_OK;
+}
+
 // ---- serving: continuous batching of many solves ------------------------------------
 // Requests (a patch, its initial state, a number of time steps) are admitted
 // while their device footprint fits the server's HBM budget and run as one
-// continuous batch: every round starts a step for each admitted request that is
-// between steps and runs one Newton iteration of every admitted request -- the
-// FP32 ones through one batched factor/solve launch pair -- so requests at
-// different steps, and requests that arrived while others were running, share
-// the GPU.  A finished request's state is copied out and its memory freed at
-// once, which admits the next.  Each request computes exactly what
-// mafem_time_step computes on its handle: results do not depend on the mix.
+// continuous batch.  An FP32 request whose band fits the batched solve takes
+// a slot of the server's job tables and advances through batched Newton rounds
+// on one of kLanes solve lanes: a lane's round assembles, factors, refines and
+// updates its requests with one launch per kernel (run_round), and each
+// request that finishes an iteration goes into the next round of a free lane,
+// so small patches iterate while a large one is still in its round.  The
+// ready requests are grouped by the cost of their factorisation (groups within
+// a factor of 8), the costliest group first, one group per free lane.  Other
+// requests run their own iterations on their own streams beside the lanes.
+// A finished request's state is copied out and its memory freed at once,
+// which admits the next.  Each request computes exactly what mafem_time_step
+// computes on its handle: results do not depend on the mix.
 
 namespace {
 struct ServerReq {
-  enum State { IDLE, WAIT_SOLVE, FLIGHT };
+  enum State { IDLE, READY, LANE, FLIGHT };
   int64_t id = 0;
   mafem_request r{};
   std::vector<double> xms, cps;  // initial state, then the result
@@ -1600,24 +1957,19 @@ struct ServerReq {
   double t = 0.0;
   bool in_step = false;
   State state = IDLE;
+  int start = 0;         // step-start flags of the next lane round (kStartPredict | kStartDirichlet)
+  double dscale = 1.0;   // the ramp's Dirichlet scale of the step
   double t_start = 0.0;  // host seconds at the step's first iteration
   int status = MAFEM_OK;
   bool done = false;
   mafem_step_stats last{};
 };
-// One batched FP32 solve in flight: its streams (cluster and single-CTA
-// factorisations), completion event and job order.
-struct SolveLane {
-  cudaStream_t st = nullptr, st2 = nullptr;
-  cudaEvent_t done = nullptr, efork = nullptr, ejoin = nullptr;
-  int* d_order = nullptr;
-  int* h_order = nullptr;  // pinned
-  bool busy = false;
-};
 constexpr int kLanes = 4;
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
+// the factorisation cost of a patch, for the grouping of a lane's round
+double patch_cost(const mafem_handle* h) { return (double)h->blk.npan() * h->L.kl * h->blk.kuf; }
 }  // namespace
 
 struct mafem_server {
@@ -1629,14 +1981,17 @@ struct mafem_server {
   std::map<int64_t, ServerReq*> finished;
   std::vector<int> free_slots;
   PatchJob* d_jobs = nullptr;
-  PatchJob* h_jobs = nullptr;  // pinned staging of the job table
+  PatchJob* h_jobs = nullptr;  // pinned staging of the job tables
+  AsmJob* d_ajobs = nullptr;
+  AsmJob* h_ajobs = nullptr;
   cudaStream_t admin = nullptr;  // job-table uploads
-  SolveLane lanes[kLanes];
+  RoundRunner lanes[kLanes];
+  std::vector<ServerReq*> lane_reqs[kLanes];  // the requests of each lane's round in flight
   size_t smem_dyn = 0;
   std::vector<double> step_ms;  // wall latency of every completed step
   int64_t steps_done = 0, rounds = 0;
   ~mafem_server() {
-    for (SolveLane& l : lanes) {
+    for (RoundRunner& l : lanes) {
       if (l.st) cudaStreamSynchronize(l.st);
       if (l.st2) cudaStreamSynchronize(l.st2);
     }
@@ -1646,16 +2001,10 @@ struct mafem_server {
       delete q;
     }
     for (auto& kv : finished) delete kv.second;
-    for (SolveLane& l : lanes) {
-      if (l.d_order) cudaFree(l.d_order);
-      if (l.h_order) cudaFreeHost(l.h_order);
-      for (cudaEvent_t e : {l.done, l.efork, l.ejoin})
-        if (e) cudaEventDestroy(e);
-      if (l.st2) cudaStreamDestroy(l.st2);
-      if (l.st) cudaStreamDestroy(l.st);
-    }
     if (d_jobs) cudaFree(d_jobs);
     if (h_jobs) cudaFreeHost(h_jobs);
+    if (d_ajobs) cudaFree(d_ajobs);
+    if (h_ajobs) cudaFreeHost(h_ajobs);
     if (admin) cudaStreamDestroy(admin);
   }
 };
@@ -1674,16 +2023,12 @@ extern "C" int mafem_server_create(int64_t hbm_budget_bytes, int32_t max_active,
   const size_t m = (size_t)s->max_active;
   e = cudaMalloc(&s->d_jobs, m * sizeof(PatchJob));
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_jobs, m * sizeof(PatchJob));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_ajobs, m * sizeof(AsmJob));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_ajobs, m * sizeof(AsmJob));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->admin, cudaStreamNonBlocking);
-  for (SolveLane& l : s->lanes) {
-    if (e == cudaSuccess) e = cudaMalloc(&l.d_order, m * sizeof(int));
-    if (e == cudaSuccess) e = cudaMallocHost(&l.h_order, m * sizeof(int));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&l.st, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&l.st2, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.efork, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.ejoin, cudaEventDisableTiming);
-  }
+  for (RoundRunner& l : s->lanes)
+    if (e == cudaSuccess) e = l.init(s->max_active);
+  if (e == cudaSuccess) e = batch_asm_setup();
   if (e != cudaSuccess) {
     set_global_error(std::string("mafem_server_create: ") + cudaGetErrorString(e));
     return MAFEM_ERR_CUDA;
@@ -1739,12 +2084,29 @@ static void server_retire(mafem_server* s, ServerReq* q) {
   s->finished[q->id] = q;
 }
 
-// One pass of the event-driven loop: admit what fits; enqueue the next Newton
-// iteration of every request that is not waiting on the GPU (starting a time
-// step first if it is between steps); hand the FP32 requests whose assembly is
-// enqueued to a free solve lane as one batched launch; collect every request
-// whose iteration has completed.  Requests advance at their own pace: a small
-// patch runs several iterations while a large one runs one.
+// The Newton criterion on a request's completed iteration: the next iteration,
+// the next step, or the end of the request (pushed onto retire).
+static void server_after_iter(mafem_server* s, ServerReq* q, int rc, std::vector<ServerReq*>& retire,
+                              cudaEvent_t end) {
+  q->state = ServerReq::IDLE;
+  if (rc == kIterAgain) return;
+  if (rc == kIterDone) {
+    step_stats(q->h, &q->last, end);
+    s->step_ms.push_back((now_s() - q->t_start) * 1e3);
+    ++s->steps_done;
+    q->t += q->r.dt;
+    q->in_step = false;
+    if (++q->step < q->r.nsteps) return;
+    rc = MAFEM_OK;
+  }
+  q->status = rc;
+  retire.push_back(q);
+}
+
+// One pass of the event-driven loop: admit what fits; collect the completed
+// lane rounds and own iterations; start the next iteration of every request
+// that is not on the GPU (starting a time step first if it is between steps);
+// hand the ready FP32 requests to the free lanes as batched rounds.
 extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n_pending) {
   if (!s) return MAFEM_ERR_ARG;
   // admission, first come first served, while the footprint fits
@@ -1774,128 +2136,149 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
       q->slot = s->free_slots.back();
       s->free_slots.pop_back();
       s->h_jobs[q->slot] = h->job;
+      s->h_ajobs[q->slot] = asm_job(h);
       cudaMemcpyAsync(s->d_jobs + q->slot, s->h_jobs + q->slot, sizeof(PatchJob), cudaMemcpyHostToDevice, s->admin);
+      cudaMemcpyAsync(s->d_ajobs + q->slot, s->h_ajobs + q->slot, sizeof(AsmJob), cudaMemcpyHostToDevice, s->admin);
       cudaStreamSynchronize(s->admin);
     }
     s->active.push_back(q);
   }
   std::vector<ServerReq*> retire;
-  // the next iteration of every request not waiting on the GPU
-  const double t_now = now_s();
-  for (ServerReq* q : s->active) {
-    if (q->state != ServerReq::IDLE) continue;
-    if (!q->in_step) {  // predictor (Analysis.jl:70) + step_begin
-      if (q->r.ramp_steps > 0) {  // the Dirichlet values ramped over the request's first steps
-        const double sc = std::min(1.0, (double)(q->step + 1) / q->r.ramp_steps);
-        launch_dirichlet_scale(q->h->P.cps, q->h->d_dir_idx, q->h->d_dir_val, q->h->n_dir, sc, q->h->st);
-      }
-      launch_predictor(q->h->P, q->h->pp, q->r.dt, q->h->st);
-      q->h->launches += 1;
-      step_begin(q->h, q->t + q->r.dt, q->r.dt);
-      q->in_step = true;
-      q->t_start = t_now;
-    }
-    const int rc = q->slot >= 0 ? iter_enqueue_patch_begin(q->h) : iter_enqueue(q->h);
-    if (rc != MAFEM_OK) {
-      q->status = rc;
-      retire.push_back(q);
-      continue;
-    }
-    q->state = q->slot >= 0 ? ServerReq::WAIT_SOLVE : ServerReq::FLIGHT;
-  }
-  // the waiting FP32 requests as one batched solve on a free lane
-  for (SolveLane& l : s->lanes)
-    if (l.busy && cudaEventQuery(l.done) == cudaSuccess) l.busy = false;
-  std::vector<int> pj;
-  for (size_t k = 0; k < s->active.size(); ++k)
-    if (s->active[k]->state == ServerReq::WAIT_SOLVE && s->active[k]->status == MAFEM_OK) pj.push_back((int)k);
-  SolveLane* lane = nullptr;
-  for (SolveLane& l : s->lanes)
-    if (!l.busy) {
-      lane = &l;
-      break;
-    }
-  if (!pj.empty() && lane) {
-    std::vector<mafem_handle*> hv(s->active.size());
-    for (size_t k = 0; k < s->active.size(); ++k) hv[k] = s->active[k]->h;
-    int n4 = 0, n2 = 0;
-    choose_patch_ctas(hv, pj);
-    order_patch_jobs(hv, pj, &n4, &n2);
-    size_t smf = 0, smr = 0;
-    int max_sw = 1;
-    double tol = 1.0;
-    for (size_t k = 0; k < pj.size(); ++k) {
-      mafem_handle* h = s->active[pj[k]]->h;
-      lane->h_order[k] = s->active[pj[k]]->slot;
-      smf = std::max(smf, patch_factor_smem(h->L.kl));
-      smr = std::max(smr, patch_refine_smem(h->L.n));
-      max_sw = std::max(max_sw, h->max_refine);
-      tol = std::min(tol, h->refine_tol);
-      cudaStreamWaitEvent(lane->st, h->ev[1], 0);
-    }
-    cudaError_t e = cudaMemcpyAsync(lane->d_order, lane->h_order, pj.size() * sizeof(int), cudaMemcpyHostToDevice,
-                                    lane->st);
-    if (e == cudaSuccess)
-      e = patch_solve(s->d_jobs, lane->d_order, n4, n2, (int)pj.size(), smf, smr, max_sw, tol, lane->st, lane->st2,
-                      lane->efork, lane->ejoin);
-    if (e == cudaSuccess) e = cudaEventRecord(lane->done, lane->st);
-    lane->busy = true;
-    for (int k : pj) {
-      ServerReq* q = s->active[k];
-      if (e != cudaSuccess) {
-        q->h->err = std::string("batched FP32 solve: ") + cudaGetErrorString(e);
-        q->status = MAFEM_ERR_CUDA;
-        retire.push_back(q);
-        continue;
-      }
-      if (k == pj[0]) q->h->launches += patch_solve_launches(n4, n2, (int)pj.size());
-      const int rc = iter_enqueue_patch_end(q->h, lane->done);
-      if (rc != MAFEM_OK) {
-        q->status = rc;
-        retire.push_back(q);
-        continue;
-      }
-      q->state = ServerReq::FLIGHT;
-    }
-  }
-  // collect finished iterations
   bool progressed = false;
+  // completed lane rounds
+  for (int l = 0; l < kLanes; ++l) {
+    RoundRunner& L = s->lanes[l];
+    if (!L.busy) continue;
+    const cudaError_t qe = cudaEventQuery(L.rev[3]);
+    if (qe == cudaErrorNotReady) continue;
+    L.busy = false;
+    progressed = true;
+    std::vector<mafem_handle*> hv;
+    for (ServerReq* q : s->lane_reqs[l]) hv.push_back(q->h);
+    if (qe == cudaSuccess) round_results(L, hv);
+    for (ServerReq* q : s->lane_reqs[l]) {
+      const int64_t fb = q->h->fallbacks;
+      int rc = MAFEM_ERR_CUDA;
+      if (qe == cudaSuccess)
+        rc = iter_decide(q->h);
+      else
+        q->h->err = std::string("batched round: ") + cudaGetErrorString(qe);
+      server_after_iter(s, q, rc, retire, q->h->fallbacks == fb ? L.rev[3] : nullptr);
+    }
+    s->lane_reqs[l].clear();
+  }
+  // completed own iterations
   for (ServerReq* q : s->active) {
     if (q->state != ServerReq::FLIGHT || q->status != MAFEM_OK) continue;
     const cudaError_t qe = cudaEventQuery(q->h->ev[4]);
     if (qe == cudaErrorNotReady) continue;
     progressed = true;
-    q->state = ServerReq::IDLE;
     int rc = qe == cudaSuccess ? iter_finish(q->h) : MAFEM_ERR_CUDA;
     if (qe != cudaSuccess) q->h->err = std::string("iteration: ") + cudaGetErrorString(qe);
-    if (rc == kIterAgain) continue;
-    if (rc == kIterDone) {
-      step_stats(q->h, &q->last);
-      s->step_ms.push_back((now_s() - q->t_start) * 1e3);
-      ++s->steps_done;
-      q->t += q->r.dt;
-      q->in_step = false;
-      if (++q->step < q->r.nsteps) continue;
-      rc = MAFEM_OK;
+    server_after_iter(s, q, rc, retire, nullptr);
+  }
+  // the next iteration of every request not on the GPU
+  const double t_now = now_s();
+  for (ServerReq* q : s->active) {
+    if (q->state != ServerReq::IDLE || q->status != MAFEM_OK) continue;
+    if (std::find(retire.begin(), retire.end(), q) != retire.end()) continue;
+    mafem_handle* h = q->h;
+    if (!q->in_step) {  // predictor (Analysis.jl:70) + step_begin
+      const double sc = q->r.ramp_steps > 0 ? std::min(1.0, (double)(q->step + 1) / q->r.ramp_steps) : 1.0;
+      if (q->slot >= 0) {  // in the step's first lane round
+        q->start = kStartPredict | (q->r.ramp_steps > 0 ? kStartDirichlet : 0);
+        q->dscale = sc;
+      } else {
+        // the Dirichlet values ramped over the request's first steps
+        if (q->r.ramp_steps > 0) launch_dirichlet_scale(h->P.cps, h->d_dir_idx, h->d_dir_val, h->n_dir, sc, h->st);
+        launch_predictor(h->P, h->pp, q->r.dt, h->st);
+        h->launches += 1;
+      }
+      step_begin(h, q->t + q->r.dt, q->r.dt);
+      q->in_step = true;
+      q->t_start = t_now;
     }
-    q->status = rc;
-    retire.push_back(q);
+    if (q->slot >= 0) {
+      q->state = ServerReq::READY;
+      continue;
+    }
+    const int rc = iter_enqueue(h);
+    if (rc != MAFEM_OK) {
+      q->status = rc;
+      retire.push_back(q);
+      continue;
+    }
+    q->state = ServerReq::FLIGHT;
+  }
+  // the ready FP32 requests as batched rounds on the free lanes: groups of
+  // similar factorisation cost, the costliest first
+  std::vector<ServerReq*> ready;
+  for (ServerReq* q : s->active)
+    if (q->state == ServerReq::READY && q->status == MAFEM_OK) ready.push_back(q);
+  std::sort(ready.begin(), ready.end(), [](ServerReq* a, ServerReq* b) { return patch_cost(a->h) > patch_cost(b->h); });
+  size_t next = 0;
+  for (int l = 0; l < kLanes && next < ready.size(); ++l) {
+    RoundRunner& L = s->lanes[l];
+    if (L.busy) continue;
+    const double top = patch_cost(ready[next]->h);
+    size_t end = next + 1;
+    while (end < ready.size() && patch_cost(ready[end]->h) * 8.0 >= top) ++end;
+    std::vector<ServerReq*>& rq = s->lane_reqs[l];
+    rq.assign(ready.begin() + next, ready.begin() + end);
+    next = end;
+    const int m = (int)rq.size();
+    std::vector<mafem_handle*> hv(m);
+    std::vector<int> slot_of(m), start(m), pj(m);
+    std::vector<double> dscale(m);
+    size_t smf = 0, smr = 0;
+    int max_sw = 1;
+    double tol = 1.0;
+    for (int k = 0; k < m; ++k) {
+      ServerReq* q = rq[k];
+      mafem_handle* h = q->h;
+      hv[k] = h;
+      slot_of[k] = q->slot;
+      start[k] = q->start;
+      dscale[k] = q->dscale;
+      pj[k] = k;
+      smf = std::max(smf, patch_factor_smem(h->L.kl));
+      smr = std::max(smr, patch_refine_smem(h->L.n));
+      max_sw = std::max(max_sw, h->max_refine);
+      tol = std::min(tol, h->refine_tol);
+      if (q->start) cudaStreamWaitEvent(L.st, h->ev[5], 0);  // the handle's own work before the step
+    }
+    int n4 = 0, n2 = 0;
+    choose_patch_ctas(hv, pj);
+    order_patch_jobs(hv, pj, &n4, &n2);
+    int nl = 0;
+    cudaError_t e = run_round(L, s->d_jobs, s->d_ajobs, smf, smr, hv, slot_of, pj, n4, n2, max_sw, tol, start, dscale,
+                              &nl);
+    for (ServerReq* q : rq) q->start = 0;
+    if (e != cudaSuccess) {
+      for (ServerReq* q : rq) {
+        q->h->err = std::string("batched round: ") + cudaGetErrorString(e);
+        q->status = MAFEM_ERR_CUDA;
+        retire.push_back(q);
+      }
+      rq.clear();
+      continue;
+    }
+    hv[0]->launches += nl;
+    L.busy = true;
+    for (ServerReq* q : rq) q->state = ServerReq::LANE;
   }
   if (!retire.empty()) {
     std::vector<ServerReq*> keep;
     for (ServerReq* q : s->active)
       if (std::find(retire.begin(), retire.end(), q) == retire.end()) keep.push_back(q);
-    // A request retired on an error path may still be read by a batched solve
-    // in flight on some lane: wait for the lanes before its memory is freed.
-    // (A request whose iteration completed normally is past its lane's solve:
-    // its update waited on it.)
+    // A request retired on an error path may still be read by a round in
+    // flight on some lane: wait for the lanes before its memory is freed.
     bool drain = false;
     for (ServerReq* q : retire) drain |= q->status != MAFEM_OK && q->status != MAFEM_NEWTON_NOT_CONVERGED;
     if (drain)
-      for (SolveLane& l : s->lanes) {
-        cudaStreamSynchronize(l.st);
-        cudaStreamSynchronize(l.st2);
-        l.busy = false;
+      for (RoundRunner& L : s->lanes) {
+        cudaStreamSynchronize(L.st);
+        cudaStreamSynchronize(L.st2);
       }
     for (ServerReq* q : retire) {
       if (q->h) cudaStreamSynchronize(q->h->st);

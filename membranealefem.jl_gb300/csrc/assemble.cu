@@ -7,7 +7,7 @@
 // Here the scatter is inverted into a gather over the tensor-product
 // connectivity: element (e1, e2) owns nodes (e1..e1+2) x (e2..e2+2)
 // (Mesh.jl:582-589), so a band entry (i, j) receives contributions only from
-// the <= 2x2 elements that contain both node(i) and node(j), and each output
+// the <= 3x3 elements that contain both node(i) and node(j), and each output
 // is produced by exactly one thread -- no atomics, deterministic sums.
 
 #include <cuda_runtime.h>
@@ -15,12 +15,40 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "batch_common.cuh"
 #include "mafem_internal.h"
 
 namespace mafem {
 
 __host__ __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
 __host__ __device__ __forceinline__ int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
+
+// One thread per stored entry of band column j; entries outside the element
+// stencil (structural zeros, pivoting-fill rows, padding) are written as zero,
+// so the band needs no separate clearing pass.
+// Band entry (row j + s - off, column j): the sum of the <= 3 x 3 element
+// contributions, zero outside the element stencil.
+template <class T>
+__device__ __forceinline__ T band_entry(const DevPatch& P, int ndf, int nq, const BandLayout& L,
+                                        const T* __restrict__ K_el, int64_t j, int s1J, int s2J, int dj, int64_t s) {
+  const int64_t i = j + s - L.off;
+  T val = T(0);
+  if (i >= 0 && i < L.n && i - j >= -L.ku && i - j <= L.kl) {
+    const int NI = P.unk_node[i], di = P.unk_dof[i];
+    const int s1I = NI % P.num1np, s2I = NI / P.num1np;
+    if (abs(s1I - s1J) <= 2 && abs(s2I - s2J) <= 2) {
+      const int e1lo = max(max(s1I, s1J) - 2, 0), e1hi = min(min(s1I, s1J), P.num1el - 1);
+      const int e2lo = max(max(s2I, s2J) - 2, 0), e2hi = min(min(s2I, s2J), P.num2el - 1);
+      for (int e2 = e2lo; e2 <= e2hi; ++e2)
+        for (int e1 = e1lo; e1 <= e1hi; ++e1) {
+          const int e = e1 + P.num1el * e2;
+          const int a = (s1I - e1) + 3 * (s2I - e2), b = (s1J - e1) + 3 * (s2J - e2);
+          val += K_el[(size_t)e * nq * nq + (size_t)(b * ndf + dj) * nq + a * ndf + di];
+        }
+    }
+  }
+  return val;
+}
 
 // One thread per stored entry of band column j; entries outside the element
 // stencil (structural zeros, pivoting-fill rows, padding) are written as zero,
@@ -33,22 +61,7 @@ __global__ void band_gather_kernel(DevPatch P, int ndf, int nq, BandLayout L, co
     const int s1J = NJ % P.num1np, s2J = NJ / P.num1np;
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < L.ldb;
          s += (int64_t)gridDim.x * blockDim.x) {
-      const int64_t i = j + s - L.off;
-      T val = T(0);
-      if (i >= 0 && i < L.n && i - j >= -L.ku && i - j <= L.kl) {
-        const int NI = P.unk_node[i], di = P.unk_dof[i];
-        const int s1I = NI % P.num1np, s2I = NI / P.num1np;
-        if (abs(s1I - s1J) <= 2 && abs(s2I - s2J) <= 2) {
-          const int e1lo = max(max(s1I, s1J) - 2, 0), e1hi = min(min(s1I, s1J), P.num1el - 1);
-          const int e2lo = max(max(s2I, s2J) - 2, 0), e2hi = min(min(s2I, s2J), P.num2el - 1);
-          for (int e2 = e2lo; e2 <= e2hi; ++e2)
-            for (int e1 = e1lo; e1 <= e1hi; ++e1) {
-              const int e = e1 + P.num1el * e2;
-              const int a = (s1I - e1) + 3 * (s2I - e2), b = (s1J - e1) + 3 * (s2J - e2);
-              val += K_el[(size_t)e * nq * nq + (size_t)(b * ndf + dj) * nq + a * ndf + di];
-            }
-        }
-      }
+      const T val = band_entry<T>(P, ndf, nq, L, K_el, j, s1J, s2J, dj, s);
       ab[j * L.ldb + s] = val;
       if (ab2) ab2[j * L.ldb + s] = val;  // the unfactored copy the refinement multiplies by
     }
@@ -89,14 +102,12 @@ __global__ void predictor_kernel(DevPatch P, PhysParams pp, double dt) {
 // pivot, the batched solve failed, or a bounded wait ran out) the state is left
 // unchanged and only r² is summed (so a non-finite residual still shows); the
 // host redoes the iteration or reports the failure.
-__global__ void newton_update_kernel(DevPatch P, PhysParams pp, double dt, const double* __restrict__ x,
-                                     const double* __restrict__ r, double* __restrict__ part,
-                                     const int* __restrict__ skip, const int* __restrict__ skip2,
-                                     const int* __restrict__ skip3) {
+__device__ __forceinline__ void newton_update_body(const DevPatch& P, const PhysParams& pp, double dt,
+                                                   const double* __restrict__ x, const double* __restrict__ r,
+                                                   double* __restrict__ part, bool hold, int blk, int nblk) {
   __shared__ double s_du[32], s_r[32];
-  const bool hold = (skip && *skip) || (skip2 && *skip2) || (skip3 && *skip3);
   double du2 = 0.0, r2 = 0.0;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < P.nmdf; q += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t q = blk * (int64_t)blockDim.x + threadIdx.x; q < P.nmdf; q += (int64_t)nblk * blockDim.x) {
     r2 += r[q] * r[q];
     if (hold) continue;
     const double du = -x[q];
@@ -121,9 +132,17 @@ __global__ void newton_update_kernel(DevPatch P, PhysParams pp, double dt, const
       a += s_du[k];
       b += s_r[k];
     }
-    part[2 * blockIdx.x] = a;
-    part[2 * blockIdx.x + 1] = b;
+    part[2 * blk] = a;
+    part[2 * blk + 1] = b;
   }
+}
+
+__global__ void newton_update_kernel(DevPatch P, PhysParams pp, double dt, const double* __restrict__ x,
+                                     const double* __restrict__ r, double* __restrict__ part,
+                                     const int* __restrict__ skip, const int* __restrict__ skip2,
+                                     const int* __restrict__ skip3) {
+  const bool hold = (skip && *skip) || (skip2 && *skip2) || (skip3 && *skip3);
+  newton_update_body(P, pp, dt, x, r, part, hold, blockIdx.x, gridDim.x);
 }
 
 // Fixed-order final reduction: out[0] = ‖Δu‖₂ / nmdf (the Newton ε,
@@ -238,7 +257,141 @@ __global__ void sqrt_pair_kernel(const double* __restrict__ part, int nblk, doub
   }
 }
 
+// ---- batched kernels of a Newton round: every patch of the round in one launch ----------
+// Each patch gets exactly the CTAs (and the same CTA-to-work map) its own
+// launch would use: the gathers, the update and the norms sum in the same
+// order as the per-patch kernels.
+
+// Both bands of the FP32 form, kGatherCols columns per CTA.
+__global__ void __launch_bounds__(256, 4) batch_gather_kernel(const AsmJob* __restrict__ jobs,
+                                                           const AsmItem* __restrict__ items,
+                                                           const int* __restrict__ off, int m) {
+  __shared__ int s_k;
+  const int k = batch_item(off, m, &s_k);
+  const AsmJob& J = jobs[items[k].job];
+  const BandLayout L = J.L;
+  const int ndf = J.pp.ndf, nq = J.pp.nq;
+  const int64_t j0 = (int64_t)(off[0] + (int)blockIdx.x - off[k]) * kGatherCols;
+  for (int64_t j = j0; j < min64(j0 + kGatherCols, L.n); ++j) {
+    const int NJ = J.P.unk_node[j], dj = J.P.unk_dof[j];
+    const int s1J = NJ % J.P.num1np, s2J = NJ / J.P.num1np;
+    for (int64_t s = threadIdx.x; s < L.ldb; s += blockDim.x) {
+      const float val = band_entry<float>(J.P, ndf, nq, L, J.K_el, j, s1J, s2J, dj, s);
+      J.band[j * L.ldb + s] = val;
+      J.band0[j * L.ldb + s] = val;
+    }
+  }
+}
+
+// The residual, 256 unknowns per CTA; the patch's first CTA also zeroes its
+// info words for the round's solve.
+__global__ void __launch_bounds__(256) batch_rgather_kernel(const AsmJob* __restrict__ jobs,
+                                                            const AsmItem* __restrict__ items,
+                                                            const int* __restrict__ off, int m) {
+  __shared__ int s_k;
+  const int k = batch_item(off, m, &s_k);
+  const AsmJob& J = jobs[items[k].job];
+  const int blk = off[0] + (int)blockIdx.x - off[k];
+  if (blk == 0 && threadIdx.x < 4) J.info[threadIdx.x] = 0;
+  const int64_t i = (int64_t)blk * blockDim.x + threadIdx.x;
+  if (i >= J.P.nmdf) return;
+  const int ndf = J.pp.ndf, nq = J.pp.nq;
+  const int NI = J.P.unk_node[i], di = J.P.unk_dof[i];
+  const int s1 = NI % J.P.num1np, s2 = NI / J.P.num1np;
+  double acc = 0.0;
+  for (int e2 = max(s2 - 2, 0); e2 <= min(s2, J.P.num2el - 1); ++e2)
+    for (int e1 = max(s1 - 2, 0); e1 <= min(s1, J.P.num1el - 1); ++e1) {
+      const int e = e1 + J.P.num1el * e2;
+      const int a = (s1 - e1) + 3 * (s2 - e2);
+      acc += J.r_el[(size_t)e * nq + a * ndf + di];
+    }
+  J.r[i] = acc;
+}
+
+// Newton update of every patch; a patch whose solve failed (status or
+// wait-ran-out word set) keeps its state.
+__global__ void __launch_bounds__(256) batch_update_kernel(const AsmJob* __restrict__ jobs,
+                                                           const AsmItem* __restrict__ items,
+                                                           const int* __restrict__ off, int m) {
+  __shared__ int s_k;
+  const int k = batch_item(off, m, &s_k);
+  const AsmItem it = items[k];
+  const AsmJob& J = jobs[it.job];
+  const bool hold = J.info[2] != 0 || J.info[1] != 0;
+  newton_update_body(J.P, J.pp, it.dt, J.x, J.r, J.part, hold, off[0] + (int)blockIdx.x - off[k], off[k + 1] - off[k]);
+}
+
+// The fixed-order norms of newton_norm_kernel, one CTA per patch, copied with
+// the info words into outs[k] for the host.
+__global__ void batch_norm_kernel(const AsmJob* __restrict__ jobs, const AsmItem* __restrict__ items,
+                                  const int* __restrict__ off, int m, AsmOut* __restrict__ outs) {
+  const int k = blockIdx.x;
+  if (k >= m || threadIdx.x != 0) return;
+  const AsmJob& J = jobs[items[k].job];
+  const int nblk = off[k + 1] - off[k];
+  double a = 0, b = 0;
+  for (int t = 0; t < nblk; ++t) {
+    a += J.part[2 * t];
+    b += J.part[2 * t + 1];
+  }
+  AsmOut o;
+  o.out[0] = sqrt(a) / (double)J.P.nmdf;
+  o.out[1] = sqrt(b);
+  o.out[2] = (isfinite(a) && isfinite(b)) ? 0.0 : 1.0;
+  for (int t = 0; t < 3; ++t) J.out[t] = o.out[t];
+  for (int t = 0; t < 4; ++t) o.info[t] = J.info[t];
+  outs[k] = o;
+}
+
+// The scaled inhomogeneous Dirichlet values of the patches that start a time
+// step (mafem_set_dirichlet_scale's edit of the state).
+__global__ void __launch_bounds__(256) batch_dirichlet_kernel(const AsmJob* __restrict__ jobs,
+                                                              const AsmItem* __restrict__ items,
+                                                              const int* __restrict__ off, int m) {
+  __shared__ int s_k;
+  const int k = batch_item(off, m, &s_k);
+  const AsmItem it = items[k];
+  const AsmJob& J = jobs[it.job];
+  const int idx = (off[0] + (int)blockIdx.x - off[k]) * blockDim.x + threadIdx.x;
+  if ((it.start & kStartDirichlet) && idx < J.n_dir) J.P.cps[J.dir_idx[idx]] = it.dscale * J.dir_val[idx];
+}
+
+// update_xms! as the predictor of every patch (Analysis.jl:70).
+__global__ void __launch_bounds__(256) batch_predictor_kernel(const AsmJob* __restrict__ jobs,
+                                                              const AsmItem* __restrict__ items,
+                                                              const int* __restrict__ off, int m) {
+  __shared__ int s_k;
+  const int k = batch_item(off, m, &s_k);
+  const AsmItem it = items[k];
+  const AsmJob& J = jobs[it.job];
+  const int64_t idx = (int64_t)(off[0] + (int)blockIdx.x - off[k]) * blockDim.x + threadIdx.x;
+  if (!(it.start & kStartPredict) || idx >= 3LL * J.P.numnp) return;
+  const int j = (int)(idx / J.P.numnp), node = (int)(idx - (int64_t)j * J.P.numnp);
+  const int d = J.pp.mmo[j];
+  if (d >= 0) J.P.xms[idx] += it.dt * J.P.cps[(size_t)d * J.P.numnp + node];
+}
+
 // ---- launchers -------------------------------------------------------------------
+void launch_batch_gather(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas, cudaStream_t st) {
+  if (ctas > 0) batch_gather_kernel<<<ctas, 256, 0, st>>>(jobs, items, off, m);
+}
+void launch_batch_rgather(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas, cudaStream_t st) {
+  if (ctas > 0) batch_rgather_kernel<<<ctas, 256, 0, st>>>(jobs, items, off, m);
+}
+void launch_batch_update(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas, AsmOut* outs,
+                         cudaStream_t st) {
+  if (ctas <= 0) return;
+  batch_update_kernel<<<ctas, 256, 0, st>>>(jobs, items, off, m);
+  batch_norm_kernel<<<m, 32, 0, st>>>(jobs, items, off, m, outs);
+}
+void launch_batch_predictor(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
+                            cudaStream_t st) {
+  if (ctas > 0) batch_predictor_kernel<<<ctas, 256, 0, st>>>(jobs, items, off, m);
+}
+void launch_batch_dirichlet(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
+                            cudaStream_t st) {
+  if (ctas > 0) batch_dirichlet_kernel<<<ctas, 256, 0, st>>>(jobs, items, off, m);
+}
 template <class T>
 void launch_band_gather(const DevPatch& P, int ndf, int nq, const BandLayout& L, const T* K_el, T* ab,
                         cudaStream_t st, T* ab2) {

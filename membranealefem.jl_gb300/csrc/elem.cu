@@ -40,6 +40,7 @@
 #include <algorithm>
 #include <cstdint>
 
+#include "batch_common.cuh"
 #include "mafem_internal.h"
 
 namespace mafem {
@@ -502,15 +503,19 @@ __device__ __forceinline__ void bdry_gp(const PhysParams& pp, const P* X, const 
 // rows to r_el[k][q]; area_only: the area Gauss points alone
 // (calc_elem_dof_residuals without the Dohrmann-Bochev projection or boundary
 // terms, as PullForce.jl uses it); K_el may be null (no tangent written).
+// The element loop of one CTA (CTA number blk of the patch), shared by the
+// single-patch kernel and the batched kernel, which reads Pt / pp from a job
+// table into shared memory.
 template <class P, class T, bool WANT_R, int MOTION, int EPB>
-__global__ void elem_kernel(DevPatch Pt, PhysParams pp, double time, double dt, double* __restrict__ r_el,
-                            T* __restrict__ K_el, const int* __restrict__ elist, int nlist, int area_only) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void elem_body(const DevPatch& Pt, const PhysParams& pp, double time, double dt,
+                                          double* __restrict__ r_el, T* __restrict__ K_el,
+                                          const int* __restrict__ elist, int nlist, int area_only, int blk,
+                                          unsigned char* smem_raw) {
   const int nq = pp.nq, ndf = pp.ndf;
   const int ldk = nq + 1;
   const int slot = threadIdx.x / nq;
   const int q = threadIdx.x - slot * nq;
-  const int kk = blockIdx.x * EPB + slot;  // element (or list) index of this slot
+  const int kk = blk * EPB + slot;  // element (or list) index of this slot
   const int e = elist ? (kk < nlist ? elist[kk] : 0) : kk;
   // per-slot shared memory: X[27], C[72], GP tables [9][kTab], the points'
   // shared primal values [9][kPre] in P; then the blocks
@@ -609,6 +614,13 @@ __global__ void elem_kernel(DevPatch Pt, PhysParams pp, double time, double dt, 
   }
 }
 
+template <class P, class T, bool WANT_R, int MOTION, int EPB>
+__global__ void elem_kernel(DevPatch Pt, PhysParams pp, double time, double dt, double* __restrict__ r_el,
+                            T* __restrict__ K_el, const int* __restrict__ elist, int nlist, int area_only) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  elem_body<P, T, WANT_R, MOTION, EPB>(Pt, pp, time, dt, r_el, K_el, elist, nlist, area_only, blockIdx.x, smem_raw);
+}
+
 // FP64 residual of the FP32 form: primal only, one thread per (element, area
 // Gauss point).  Phase 1: each task adds its point's contribution to every
 // element row into its own shared array; phase 2: one thread per (element,
@@ -617,15 +629,14 @@ __global__ void elem_kernel(DevPatch Pt, PhysParams pp, double time, double dt, 
 // likewise, summed in (bc, point) order -- the plain form's order.
 constexpr int kResEPB = 16;  // elements per CTA: 144 threads
 template <int MOTION>
-__global__ void __launch_bounds__(kResEPB * 9) elem_resid_kernel(DevPatch Pt, PhysParams pp, double time, double dt,
-                                                                double* __restrict__ r_el) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void resid_body(const DevPatch& Pt, const PhysParams& pp, double time, double dt,
+                                           double* __restrict__ r_el, int blk, unsigned char* smem_raw) {
   const int nq = pp.nq, ndf = pp.ndf;
   double* X = reinterpret_cast<double*>(smem_raw);  // [kResEPB][27]
   double* C = X + kResEPB * 27;                       // [kResEPB][72]
   double* R = C + kResEPB * 72;                       // [kResEPB*9][nq], reused as [kResEPB*24][27]
   const int tid = threadIdx.x;
-  const int e0 = blockIdx.x * kResEPB;
+  const int e0 = blk * kResEPB;
   const int ne = min(kResEPB, Pt.numel - e0);
   for (int k = tid; k < ne * 27; k += blockDim.x) {
     const int el = k / 27, r = k - 27 * el, b = r / 3, i = r - 3 * b;
@@ -715,6 +726,50 @@ __global__ void __launch_bounds__(kResEPB * 9) elem_resid_kernel(DevPatch Pt, Ph
   }
 }
 
+template <int MOTION>
+__global__ void __launch_bounds__(kResEPB * 9) elem_resid_kernel(DevPatch Pt, PhysParams pp, double time, double dt,
+                                                                double* __restrict__ r_el) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  resid_body<MOTION>(Pt, pp, time, dt, r_el, blockIdx.x, smem_raw);
+}
+
+// ---- batched element kernels of the FP32 form: every patch of a round in one launch per motion ----
+// The CTA reads its patch's tables and parameters into shared memory, then runs
+// the single-patch kernel's body on its CTA number within the patch.
+constexpr int kTanEPB = 4;  // elements per CTA of the FP32 tangent kernel
+template <int MOTION>
+__global__ void __launch_bounds__(kResEPB * 9) batch_resid_kernel(const AsmJob* __restrict__ jobs,
+                                                                 const AsmItem* __restrict__ items,
+                                                                 const int* __restrict__ off, int m) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_k;
+  __shared__ __align__(16) DevPatch sP;
+  __shared__ __align__(16) PhysParams spp;
+  const int k = batch_item(off, m, &s_k);
+  const AsmItem it = items[k];
+  const AsmJob* J = jobs + it.job;
+  batch_copy(&sP, &J->P, (int)sizeof(DevPatch));
+  batch_copy(&spp, &J->pp, (int)sizeof(PhysParams));
+  __syncthreads();
+  resid_body<MOTION>(sP, spp, it.time, it.dt, J->r_el, off[0] + (int)blockIdx.x - off[k], smem_raw);
+}
+template <int MOTION>
+__global__ void batch_tan_kernel(const AsmJob* __restrict__ jobs, const AsmItem* __restrict__ items,
+                                 const int* __restrict__ off, int m) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_k;
+  __shared__ __align__(16) DevPatch sP;
+  __shared__ __align__(16) PhysParams spp;
+  const int k = batch_item(off, m, &s_k);
+  const AsmItem it = items[k];
+  const AsmJob* J = jobs + it.job;
+  batch_copy(&sP, &J->P, (int)sizeof(DevPatch));
+  batch_copy(&spp, &J->pp, (int)sizeof(PhysParams));
+  __syncthreads();
+  elem_body<float, float, false, MOTION, kTanEPB>(sP, spp, it.time, it.dt, nullptr, J->K_el, nullptr, 0, 0,
+                                                  off[0] + (int)blockIdx.x - off[k], smem_raw);
+}
+
 // ---- launchers -----------------------------------------------------------------------
 template <class P, class T>
 static size_t elem_smem(int nq, int epb) {
@@ -794,6 +849,55 @@ cudaError_t launch_elem<float>(const DevPatch& Pt, const PhysParams& pp, double 
       e = launch_resid_t<ALEVB_>(Pt, pp, time, dt, r_el, st);
       return e ? e : launch_elem_t<float, float, false, ALEVB_, 4>(Pt, pp, time, dt, r_el, K_el, st, nullptr, 0, 0);
   }
+}
+
+int batch_resid_ctas(int numel) { return (numel + kResEPB - 1) / kResEPB; }
+int batch_tan_ctas(int numel) { return (numel + kTanEPB - 1) / kTanEPB; }
+
+template <int MOTION>
+static cudaError_t batch_setup_t() {
+  cudaError_t e = cudaFuncSetAttribute(batch_resid_kernel<MOTION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)resid_smem(72));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(batch_tan_kernel<MOTION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)elem_smem<float, float>(72, kTanEPB));
+  return e;
+}
+cudaError_t batch_asm_setup() {
+  cudaError_t e = batch_setup_t<STATIC_>();
+  if (e == cudaSuccess) e = batch_setup_t<EUL_>();
+  if (e == cudaSuccess) e = batch_setup_t<LAG_>();
+  if (e == cudaSuccess) e = batch_setup_t<ALEV_>();
+  if (e == cudaSuccess) e = batch_setup_t<ALEVB_>();
+  return e;
+}
+
+cudaError_t launch_batch_resid(int motion, const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
+                               int nq, cudaStream_t st) {
+  if (ctas <= 0) return cudaSuccess;
+  const size_t sm = resid_smem(nq);
+  switch (motion) {
+    case MAFEM_STATIC: batch_resid_kernel<STATIC_><<<ctas, kResEPB * 9, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_EUL: batch_resid_kernel<EUL_><<<ctas, kResEPB * 9, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_LAG: batch_resid_kernel<LAG_><<<ctas, kResEPB * 9, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_ALEV: batch_resid_kernel<ALEV_><<<ctas, kResEPB * 9, sm, st>>>(jobs, items, off, m); break;
+    default: batch_resid_kernel<ALEVB_><<<ctas, kResEPB * 9, sm, st>>>(jobs, items, off, m); break;
+  }
+  return cudaGetLastError();
+}
+cudaError_t launch_batch_tan(int motion, const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
+                             int nq, cudaStream_t st) {
+  if (ctas <= 0) return cudaSuccess;
+  const size_t sm = elem_smem<float, float>(nq, kTanEPB);
+  const int thr = kTanEPB * nq;
+  switch (motion) {
+    case MAFEM_STATIC: batch_tan_kernel<STATIC_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_EUL: batch_tan_kernel<EUL_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_LAG: batch_tan_kernel<LAG_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_ALEV: batch_tan_kernel<ALEV_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    default: batch_tan_kernel<ALEVB_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+  }
+  return cudaGetLastError();
 }
 
 template size_t elem_smem_bytes<double>(int, int);

@@ -246,6 +246,72 @@ void blk_backward_1cta(const T* ab, const BandLayout& L, const BlkPlan& B, const
 }  // namespace mafem
 
 namespace mafem {
+// ---- batched assembly of the FP32 form (elem.cu, assemble.cu) -----------------------
+// A batch's Newton round assembles, updates and measures every patch of the
+// round with one launch per kernel (per motion for the element kernels): a
+// CTA finds its patch by the round's block offsets (off[k] <= CTA < off[k+1]
+// for item k) and reads the patch's tables from the job table.  Each patch is
+// cut into exactly the CTAs its single-patch launch would use: the same
+// arithmetic as the per-patch kernels (the element kernels are compiled
+// separately, so a multiply-add may round differently).
+struct AsmJob {
+  DevPatch P;
+  PhysParams pp;
+  BandLayout L;
+  double* r_el;  // [numel][nq] element residuals
+  float* K_el;   // [numel][nq][nq] element tangents
+  float* band;   // the band the factorisation overwrites
+  float* band0;  // its unfactored copy (refinement residual)
+  double* r;     // [nmdf] residual
+  double* x;     // [nmdf] the round's solution
+  double* part;  // per-CTA partial sums of the Newton update
+  double* out;   // [3] eps, |r|, non-finite flag
+  int* info;     // [4] zero-pivot column, wait ran out, solve status, sweeps
+  const int* dir_idx;     // [n_dir] inhomogeneous Dirichlet entries of cps (dof * numnp + node)
+  const double* dir_val;  // [n_dir] their values
+  int n_dir;
+  int pad;
+};
+enum { kStartPredict = 1, kStartDirichlet = 2 };  // AsmItem::start
+struct AsmItem {  // one patch of a round
+  int job;        // index into the job table
+  int start;      // first round of a time step: kStartPredict | kStartDirichlet (scale the Dirichlet values first)
+  double time, dt;
+  double dscale;  // the Dirichlet values' scale (kStartDirichlet)
+};
+struct AsmOut {  // one patch's results of a round, read by the host
+  double out[3];
+  int info[4];
+};
+constexpr int kGatherCols = 4;  // band columns per CTA of the batched gather
+// CTAs per patch of each batched kernel
+int batch_resid_ctas(int numel);
+int batch_tan_ctas(int numel);
+inline int batch_gather_ctas(int64_t n) { return (int)((n + kGatherCols - 1) / kGatherCols); }
+inline int batch_rgather_ctas(int64_t nmdf) { return (int)((nmdf + 255) / 256); }
+inline int batch_pred_ctas(int numnp) { return (3 * numnp + 255) / 256; }
+inline int batch_dir_ctas(int n_dir) { return (n_dir + 255) / 256; }
+// Sets the batched element kernels' shared-memory limits (once per process and device).
+cudaError_t batch_asm_setup();
+// The launches of one round.  items / off point at the round's slice (m items,
+// off[0 .. m]); each launch covers CTAs off[0] .. off[m] - 1.
+cudaError_t launch_batch_resid(int motion, const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
+                               int nq, cudaStream_t st);
+cudaError_t launch_batch_tan(int motion, const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
+                             int nq, cudaStream_t st);
+// Both bands and the residual; the residual gather also zeroes each patch's info words.
+void launch_batch_gather(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas, cudaStream_t st);
+void launch_batch_rgather(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas, cudaStream_t st);
+// Newton update of every patch (skipped for a patch whose solve failed) and the
+// fixed-order norms, written to the job's out and to outs[k].
+void launch_batch_update(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas, AsmOut* outs,
+                         cudaStream_t st);
+void launch_batch_predictor(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
+                            cudaStream_t st);
+// cps[dir_idx[k]] = dscale * dir_val[k] for the items that start a step with kStartDirichlet
+void launch_batch_dirichlet(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
+                            cudaStream_t st);
+
 // One patch's FP32 solve in the batched form (band_lu_patch.cu): device
 // pointers of the handle that owns them.
 struct PatchJob {

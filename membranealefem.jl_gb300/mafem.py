@@ -107,6 +107,14 @@ class _CRequest(C.Structure):
                 ("reserved", C.c_int32)]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [("graph_launches", C.c_int64), ("graph_captures", C.c_int64), ("graphs_cached", C.c_int64),
+                ("kernel_launches", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class ServerStats(C.Structure):
     _fields_ = [("steps_done", C.c_int64), ("rounds", C.c_int64), ("p50_step_ms", C.c_double),
                 ("p99_step_ms", C.c_double), ("max_step_ms", C.c_double), ("bytes_in_use", C.c_int64),
@@ -192,6 +200,8 @@ def lib():
         L.mafem_batch_step.argtypes = [vp, _PD, _PD, C.POINTER(C.c_int32), C.POINTER(StepStats)]
         L.mafem_batch_destroy.argtypes = [vp]
         L.mafem_batch_set_patch_solve.argtypes = [vp, C.c_int32]
+        L.mafem_batch_set_rounds.argtypes = [vp, C.c_int32, C.c_int32]
+        L.mafem_batch_get_stats.argtypes = [vp, C.POINTER(BatchStats)]
         L.mafem_server_create.argtypes = [C.c_int64, C.c_int32, C.POINTER(vp)]
         L.mafem_server_destroy.argtypes = [vp]
         L.mafem_server_submit.argtypes = [vp, C.POINTER(_CRequest), C.POINTER(C.c_int64)]
@@ -615,6 +625,17 @@ class Batch:
         if rc < 0:
             _raise(rc)
         return rc == 1
+
+    def set_rounds(self, batched_assembly: bool = True, graphs: bool = True):
+        """Newton rounds of the batched-solve patches: one launch per kernel for
+        all of them (default on), replayed from CUDA graphs (default on)."""
+        _raise(lib().mafem_batch_set_rounds(self.b, int(batched_assembly), int(graphs)))
+
+    def stats(self) -> dict:
+        """Graph replays and captures, graphs held, kernels enqueued."""
+        st = BatchStats()
+        _raise(lib().mafem_batch_get_stats(self.b, C.byref(st)))
+        return st.as_dict()
 
     def step(self, times, dts):
         """One time step of every patch; returns (statuses, list of step-stat dicts).

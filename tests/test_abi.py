@@ -34,7 +34,7 @@ def test_no_device_needed_for_host_calls():
 # ---- struct layouts: the ctypes mirrors against the header, compiled by gcc ----------
 _STRUCTS = {"mafem_params": "_CParams", "mafem_args": "_CArgs", "mafem_mesh_desc": "MeshDesc",
             "mafem_step_stats": "StepStats", "mafem_request": "_CRequest", "mafem_server_stats": "ServerStats",
-            "mafem_kernel_times": "KernelTimes"}
+            "mafem_kernel_times": "KernelTimes", "mafem_batch_stats": "BatchStats"}
 
 
 def test_struct_layouts_match_the_header(tmp_path):

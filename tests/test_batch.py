@@ -9,6 +9,7 @@ patches must still equal their runs alone.  Every patch matches the oracle
 (1e-9 plain FP64, 1e-8 FP32).  A patch whose Newton iteration fails reports its
 status without disturbing the others.
 """
+import numpy as np
 import pytest
 
 from _cases import M, O, params_pair, rel, state
@@ -215,3 +216,84 @@ def test_64x64_patch_in_the_batched_fp32_solve():
     xo, co = _oracle_steps(q, xms.copy(order="F"), cps.copy(order="F"), ramp=30, steps=1)
     assert rel(x1, xo) < 1e-8 and rel(c1, co) < 1e-8
     assert rel(x2, xo) < 1e-9 and rel(c2, co) < 1e-9
+
+
+# the batching workload's kind of patch: centre pull at a moderate speed, ramped
+# over 30 steps, from a flat start
+ROUND_CASES = [(M.LAG, 6, 6), (M.ALEVB, 7, 5), (M.LAG, 9, 9), (M.ALEVB, 10, 10), (M.LAG, 12, 8), (M.ALEVB, 16, 16),
+               (M.LAG, 5, 5), (M.ALEVB, 24, 24)]
+ROUND_RAMP = 30
+
+
+def _round_setup(motion, n1, n2):
+    p, q = params_pair(motion, M.F_PULL, n1, n2, pull_speed=0.2, pull_centre=1)
+    mesh = M.Mesh(p)
+    xms, cps = state(p, mesh, amp=0.0)
+    return p, q, mesh, xms, cps
+
+
+def _run_rounds(batched_assembly, graphs, cases=ROUND_CASES, steps=3):
+    solvers = []
+    try:
+        for motion, n1, n2 in cases:
+            p, _, mesh, xms, cps = _round_setup(motion, n1, n2)
+            s = M.Solver(mesh, p, M.FP32_REFINE)
+            s.upload(xms, cps)
+            solvers.append(s)
+        with M.Batch(solvers) as b:
+            assert b.set_patch_solve(True)
+            b.set_rounds(batched_assembly, graphs)
+            t, iters, launches = 0.0, [], 0
+            for k in range(steps):
+                t += DT
+                for s in solvers:
+                    s.set_dirichlet_scale(min(1.0, (k + 1) / ROUND_RAMP))
+                l0 = b.stats()["kernel_launches"]
+                status, st = b.step(t, DT)
+                launches += b.stats()["kernel_launches"] - l0
+                assert status == [M.OK] * len(cases)
+                iters.append([x["newton_iters"] for x in st])
+            stats = b.stats()
+            stats["kernel_launches"] = launches
+        return [s.download() for s in solvers], iters, stats
+    finally:
+        for s in solvers:
+            s.close()
+
+
+def test_batched_rounds_match_per_patch_kernels_and_replay_graphs():
+    """The batched Newton round (assembly, update and norms of every patch in
+    one launch per kernel) against the per-patch kernels: the same Newton
+    iteration counts and states within 1e-10 (the element kernels are compiled
+    separately, so a multiply-add may round differently); with CUDA-graph
+    replay bit-identical to the same rounds launched on the stream; the graphs
+    captured once per distinct round and replayed in later steps; every patch
+    within 1e-8 of the oracle."""
+    ref, it_ref, _ = _run_rounds(False, False)
+    got, it_got, st_plain = _run_rounds(True, False)
+    gra, it_gra, st_graph = _run_rounds(True, True)
+    assert it_got == it_ref and it_gra == it_ref
+    for (x0, c0), (x1, c1), (x2, c2) in zip(ref, got, gra):
+        assert rel(x1, x0) < 1e-10 and rel(c1, c0) < 1e-10
+        assert np.array_equal(x1, x2) and np.array_equal(c1, c2)
+    assert st_plain["graph_launches"] == 0
+    rounds = sum(max(r) for r in it_gra)
+    assert st_graph["graph_launches"] == rounds
+    assert 1 <= st_graph["graph_captures"] < rounds  # later steps replay the first step's rounds
+    for k, (motion, n1, n2) in enumerate(ROUND_CASES):
+        _, q, _, xms, cps = _round_setup(motion, n1, n2)
+        xo, co = _oracle_steps(q, xms.copy(order="F"), cps.copy(order="F"), ramp=ROUND_RAMP, steps=3)
+        assert rel(gra[k][0], xo) < 1e-8 and rel(gra[k][1], co) < 1e-8
+
+
+def test_batched_round_launches_do_not_grow_with_the_patch_count():
+    """Kernels enqueued per Newton round: a fixed number with batched rounds
+    (twice as many patches, the same launches per round up to one more
+    cluster-size group of the factorisation), one set per patch without them."""
+    def per_round(cases, on):
+        _, iters, st = _run_rounds(on, on, cases=cases, steps=1)
+        return st["kernel_launches"] / max(iters[0])
+    small = ROUND_CASES[:4]
+    large = ROUND_CASES[:4] + [(m, n1 + 1, n2) for m, n1, n2 in ROUND_CASES[:4]]
+    assert per_round(large, True) <= per_round(small, True) + 3
+    assert per_round(large, False) > 1.5 * per_round(small, False)
