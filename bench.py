@@ -825,8 +825,8 @@ def main():
     ap.add_argument("--no-precision", action="store_true", help="skip the 64 x 64 precision measurement")
     ap.add_argument("--full", action="store_true",
                     help="the batching, serving and precision workloads in full (about half an hour): the plain "
-                         "FP64 baseline on every patch, continuous batching, every serving request's full step "
-                         "count, all 140 precision steps; by default each is a bounded sample")
+                         "FP64 baseline on every patch, every serving request's full step count, all 140 precision "
+                         "steps; by default each is a bounded sample")
     ap.add_argument("--case", choices=["fp32-patch32", "fp32-batch16"],
                     help="run a small profiling case instead of the bench (prints no bench line)")
     args = ap.parse_args()
@@ -903,8 +903,7 @@ def main():
         "mesh": r["mesh"],
     }
     if rank == 0 and not args.no_batch:
-        line["batched"] = run_batched(args.batch_steps, baseline_per_class=0 if args.full else 2,
-                                      continuous=args.full)
+        line["batched"] = run_batched(args.batch_steps, baseline_per_class=0 if args.full else 2)
     if rank == 0 and not args.no_serve:
         line["serving"] = run_serving(requests=None if args.full else 16, step_scale=1.0 if args.full else 0.1)
     if rank == 0 and not args.no_precision:

@@ -292,13 +292,17 @@ int mafem_set_launch_ctas(mafem_handle* h, int32_t ctas);
  * A request is one solve: a patch (the mesh view, Params and args of
  * mafem_create), its initial state and a number of time steps.  The server
  * admits requests first come first served while their device footprint fits
- * its HBM budget and runs the admitted ones as one continuous batch: each
- * mafem_server_round starts a time step (predictor + time_step!) for every
- * admitted request between steps and runs one Newton iteration of every
- * admitted request, FP32-form requests through the batched one-CTA solve.  A
- * finished request's state is kept on the host and its device memory freed at
- * once.  Each request's results are those of mafem_time_step on its own handle,
- * whatever else runs beside it. */
+ * its HBM budget and runs the admitted ones as one continuous batch.  Each
+ * mafem_server_round collects the Newton iterations that have completed,
+ * starts the next iteration of every admitted request that is not on the GPU
+ * (a time step -- predictor + time_step! -- for one between steps), and hands
+ * the ready FP32-form requests to free solve lanes: a lane runs one batched
+ * Newton round of its requests (mafem_batch_set_rounds), the requests grouped
+ * by the cost of their factorisation so that small patches iterate while a
+ * large one is still in its round.  Other requests run their own iterations.
+ * A finished request's state is kept on the host and its device memory freed
+ * at once.  Each request's results are those of mafem_time_step on its own
+ * handle, whatever else runs beside it. */
 typedef struct mafem_server mafem_server;
 typedef struct mafem_request {
   const mafem_mesh_desc* mesh;  /* must stay valid until the request is admitted */
@@ -325,7 +329,7 @@ int mafem_server_create(int64_t hbm_budget_bytes, int32_t max_active, mafem_serv
 int mafem_server_destroy(mafem_server* s);
 /* Queue a request; MAFEM_ERR_ADMISSION if it can never fit the budget. */
 int mafem_server_submit(mafem_server* s, const mafem_request* r, int64_t* id);
-/* Admit what fits, then one Newton iteration of every admitted request. */
+/* Admit what fits, collect completed iterations, start the next ones (see above). */
 int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n_pending);
 /* A finished request's final state (xms, cps as in mafem_download_state; either
  * may be NULL) and status; the server then forgets it.  Returns 1 while it is

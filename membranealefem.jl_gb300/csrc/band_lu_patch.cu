@@ -674,11 +674,13 @@ __global__ void __launch_bounds__(kRT, 1) patch_refine_kernel(const PatchJob* __
   // trace: per sweep 4 stamps after J.trace's 6 per panel -- [0] sweep start,
   // [1] substitutions done, [2] x updated and norms formed, [3] residual done
   long long* tr = J.trace ? J.trace + (size_t)J.npan * 6 : nullptr;
-  // Stop when the last correction is small against x: |d| <= tol |x| bounds
-  // the forward error of x (about rho |d| with rho < 1 the sweep's
-  // contraction) whatever the conditioning, where a residual test would
-  // accept a large error in x on an ill-conditioned tangent.  The residual
-  // after the final sweep is then never needed.
+  // Stop when the error left in x is small against x.  After sweep k that
+  // error is about the next correction, rho |d_k| with rho = |d_k| / |d_k-1|
+  // the sweeps' contraction: stop once rho |d_k| <= tol |x| while the sweeps
+  // contract (rho <= 1/2), or once |d_k| <= tol |x| itself.  A bound on the
+  // forward error of x whatever the conditioning, where a residual test would
+  // accept a large error in x on an ill-conditioned tangent; the residual
+  // after the final sweep is never needed.
   int status = MAFEM_OK, sweeps = 0;
   double rn = r0, prev_dn = INFINITY;
   if (r0 > 0.0) {
@@ -709,7 +711,8 @@ __global__ void __launch_bounds__(kRT, 1) patch_refine_kernel(const PatchJob* __
         status = MAFEM_NAN_DETECTED;
         break;
       }
-      if (dn <= tol * xn) {
+      const double rho = dn / prev_dn;  // 0 after the first sweep (prev_dn infinite)
+      if (dn <= tol * xn || (k >= 1 && rho <= 0.5 && rho * dn <= tol * xn)) {
         status = MAFEM_OK;
         break;
       }
