@@ -144,17 +144,25 @@ class PatchLU:
         return z.astype(np.float64)
 
 
-def refine(lu: PatchLU, ab0: np.ndarray, kl: int, b: np.ndarray, tol: float = 1e-4, max_sweeps: int = 30):
-    """x with |last correction| <= tol |x|; returns (x, corrections |d_k| / |x|)."""
+def refine(lu: PatchLU, ab0: np.ndarray, kl: int, b: np.ndarray, tol: float = 1e-4, max_sweeps: int = 30,
+           predicted: bool = False):
+    """x with |last correction| <= tol |x|; returns (x, corrections |d_k| / |x|).
+    predicted=True: the batched kernel's rule (patch_refine_kernel) -- also stop
+    once the predicted next correction rho |d_k|, rho = |d_k| / |d_k-1|, is at
+    most tol |x| while the sweeps contract (rho <= 1/2)."""
     x = np.zeros(len(b))
     res = b.copy()
     hist = []
-    for _ in range(max_sweeps):
+    prev = np.inf
+    for k in range(max_sweeps):
         d = lu.solve(res)
         x += d
-        hist.append(float(np.linalg.norm(d) / max(np.linalg.norm(x), 1e-300)))
-        if hist[-1] <= tol:
+        dn, xn = float(np.linalg.norm(d)), float(np.linalg.norm(x))
+        hist.append(dn / max(xn, 1e-300))
+        rho = dn / prev
+        if dn <= tol * xn or (predicted and k >= 1 and rho <= 0.5 and rho * dn <= tol * xn):
             break
+        prev = dn
         res = b - band_matvec(ab0, kl, x)
     return x, hist
 

@@ -66,3 +66,27 @@ def test_double_float_residual_is_fp64_accurate():
         mag[i] += np.abs(a * x[jj])
     err = np.abs(df.astype(np.longdouble) - (b.astype(np.longdouble) - exact)).astype(np.float64)
     assert np.all(err <= 2.0**-40 * mag)
+
+
+@pytest.mark.parametrize("motion,n", [(M.ALEVB, 12), (M.LAG, 12), (M.ALEVB, 24)])
+@pytest.mark.parametrize("tol", [1e-4, 1e-8])
+def test_predicted_correction_stop_keeps_the_error_bound(motion, n, tol):
+    """The batched refinement's stopping rule (stop once rho |d_k| <= tol |x|
+    while the sweeps contract, rho = |d_k| / |d_k-1|): never more sweeps than
+    the plain |d_k| <= tol |x| rule, and the forward error of x against an FP64
+    band LU still within tol |x| (a factor 2 for the estimate of rho)."""
+    p, q = params_pair(motion, M.F_PULL, n, n, kb=0.5, pull_speed=0.01)
+    mesh, om = M.Mesh(p), O.Mesh(q)
+    xms, cps = state(p, mesh, seed=3, amp=1e-4)
+    om.update_xms(xms, cps, DT)
+    r, ab = om.calc_r_K(xms, cps, DT, DT, nthreads=2)
+    kl = om.half_bw
+    ab0 = ab.astype(np.float32).astype(np.float64)
+    lu = PM.PatchLU(ab0, kl, PM.node_blocks(om.ID_inv))
+    x_plain, h_plain = PM.refine(lu, ab0, kl, -r, tol=tol)
+    x_pred, h_pred = PM.refine(lu, ab0, kl, -r, tol=tol, predicted=True)
+    assert len(h_pred) <= len(h_plain)
+    f, piv, info = lapack.dgbtrf(np.asfortranarray(ab0.T), kl, kl)
+    assert info == 0
+    x64, _ = lapack.dgbtrs(f, kl, kl, -r, piv)
+    assert np.linalg.norm(x_pred - x64) <= 2 * tol * np.linalg.norm(x64)
