@@ -598,6 +598,23 @@ extern "C" int mafem_create(const mafem_mesh_desc* d, const mafem_params* p, con
       J.L = h->L;
       J.kuf = h->blk.kuf;
       J.npan = h->blk.npan();
+      J.num1np = (int)d->num1np;
+      J.num2np = (int)d->num2np;
+      // first unknown of every control point, when the unknowns are numbered
+      // control point by control point (the reference's ID numbering)
+      std::vector<int> nf((size_t)numnp + 1, 0);
+      bool mono = true;
+      for (int64_t q = 0; q < n; ++q) {
+        mono &= q == 0 || unk_node[q] >= unk_node[q - 1];
+        ++nf[(size_t)unk_node[q] + 1];
+      }
+      for (int v = 0; v < numnp; ++v) nf[(size_t)v + 1] += nf[v];
+      if (mono) {
+        int* d_nf = nullptr;
+        UP(d_nf, nf);
+        J.node_first = d_nf;
+        J.unk_node = d_un;
+      }
       h->patch_ok = patch_a21_map(J);
     }
   }

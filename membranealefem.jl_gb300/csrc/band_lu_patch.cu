@@ -581,21 +581,66 @@ __device__ void patch_lu_solve(const PatchJob& J, float* v, float* bz, float (*p
   __syncthreads();
 }
 
+// One column run [j0, j1) of a warp's double-float row sums (see patch_residual).
+__device__ __forceinline__ void residual_run(const float* a, int64_t ldm, const float2* xs, int64_t j0, int64_t j1,
+                                             float& sh, float& sl) {
+  int64_t j = j0;
+  for (; j + 8 <= j1; j += 8) {
+    float av[8];
+    float2 xv[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {  // all loads in flight
+      av[m] = a[(j + m) * ldm];
+      xv[m] = xs[j + m];
+    }
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      // explicit roundings: a contraction of p into t would break TwoSum
+      const float p = __fmul_rn(av[m], xv[m].x);
+      const float e = fmaf(av[m], xv[m].y, fmaf(av[m], xv[m].x, -p));
+      const float t = __fadd_rn(sh, p);
+      const float z = __fsub_rn(t, sh);
+      sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+      sh = t;
+    }
+  }
+  for (; j < j1; ++j) {
+    const float av = a[j * ldm];
+    const float2 xv = xs[j];
+    const float p = __fmul_rn(av, xv.x);
+    const float e = fmaf(av, xv.y, fmaf(av, xv.x, -p));
+    const float t = __fadd_rn(sh, p);
+    const float z = __fsub_rn(t, sh);
+    sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+    sh = t;
+  }
+}
+
 // res = rhs - A0 x (A0: the unfactored FP32 band); returns |res|.  The
 // products are formed on the FP32 pipe in double-float arithmetic: x = xh + xl
 // (two floats, split once per sweep), a xh = p + e exactly (FMA), and the row
 // sum kept as an unevaluated float pair (Knuth's TwoSum for the high part);
 // the pair's error (~2^-44 of the row's term magnitudes) is far below the
 // refinement tolerance, at a sixth of the cost of FP64 FMAs on this GPU.
+// A warp takes 32 rows and walks, in increasing order, only the columns their
+// control points couple to: an unknown of control point (s1, s2) couples only
+// to the unknowns of points (s1 +- 2, s2 +- 2) (biquadratic elements).  The
+// rows' points run from (s1a, s2a) to (s1b, s2b) in lexicographic order, so
+// grid row g is coupled to points [s1a - 2, W) through the points of grid row
+// s2a (if |g - s2a| <= 2), to [0, s1b + 2] through those of grid row s2b (if
+// |g - s2b| <= 2), and to the whole grid row through any grid row between
+// them: at most two runs per grid row.  The columns skipped hold stored
+// zeros, whose products leave the pair unchanged: the sums equal a walk of
+// the whole band window.
 __device__ double patch_residual(const PatchJob& J, const float2* xs, double* red) {
   const BandLayout L = J.L;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t ldm = L.ldb - 1;
   double ss = 0.0;
-  // A warp takes 32 rows and walks the columns j of their band window; with
-  // nb >= 32 every (i, j) it visits lies inside the band's storage, where the
-  // entries outside the band are stored zeros, so A0(i, j) = a[j * ldm + lane]
-  // with a at row rb of column 0 needs no guard but i < n.
+  // With nb >= 32 every (i, j) of the band window [rb - ku, rb + 32 + kl) lies
+  // inside the band's storage, where the entries outside the band are stored
+  // zeros, so A0(i, j) = a[j * ldm + lane] with a at row rb of column 0 needs
+  // no guard but i < n; the runs are clipped to that window.
   for (int64_t rb = (int64_t)warp * 32; rb < L.n; rb += kRT) {
     const int64_t i = rb + lane;
     const bool live = i < L.n;
@@ -603,35 +648,37 @@ __device__ double patch_residual(const PatchJob& J, const float2* xs, double* re
     const int64_t jhi = min64b(L.n, rb + 32 + L.kl);
     const float* a = J.band0 + L.off + (live ? i : rb);  // + j * ldm: A0(i, j)
     float sh = 0.0f, sl = 0.0f;
-    int64_t j = jlo;
-    for (; j + 8 <= jhi; j += 8) {
-      float av[8];
-      float2 xv[8];
-#pragma unroll
-      for (int m = 0; m < 8; ++m) {  // all loads in flight
-        av[m] = a[(j + m) * ldm];
-        xv[m] = xs[j + m];
+    if (J.node_first) {
+      const int W = J.num1np, H = J.num2np;
+      const int na = J.unk_node[rb], nb = J.unk_node[min64b(rb + 31, L.n - 1)];
+      const int s1a = na % W, s2a = na / W, s1b = nb % W, s2b = nb / W;
+      for (int g = max(s2a - 2, 0); g <= min(s2b + 2, H - 1); ++g) {
+        // the runs [c0, c1] (and [d0, d1] after it) of grid row g, in points
+        int c0 = 0, c1 = -1, d0 = 0, d1 = -1;
+        const bool fa = abs(g - s2a) <= 2, fb = abs(g - s2b) <= 2;
+        const bool fm = s2b - s2a >= 2 && g >= s2a - 1 && g <= s2b + 1;  // a grid row strictly between
+        if (s2a == s2b) {
+          c0 = max(s1a - 2, 0);
+          c1 = min(s1b + 2, W - 1);
+        } else if (fm || (fa && fb && s1b + 3 >= s1a - 2)) {
+          c1 = W - 1;
+        } else {
+          if (fb) c1 = min(s1b + 2, W - 1);  // [0, s1b + 2] comes first
+          if (fa) {
+            d0 = max(s1a - 2, 0);
+            d1 = W - 1;
+          }
+        }
+        for (int r = 0; r < 2; ++r) {
+          const int e0 = r ? d0 : c0, e1 = r ? d1 : c1;
+          if (e1 < e0) continue;
+          const int64_t j0 = max((int64_t)J.node_first[g * W + e0], jlo);
+          const int64_t j1 = min64b((int64_t)J.node_first[g * W + e1 + 1], jhi);
+          if (j0 < j1) residual_run(a, ldm, xs, j0, j1, sh, sl);
+        }
       }
-#pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        // explicit roundings: a contraction of p into t would break TwoSum
-        const float p = __fmul_rn(av[m], xv[m].x);
-        const float e = fmaf(av[m], xv[m].y, fmaf(av[m], xv[m].x, -p));
-        const float t = __fadd_rn(sh, p);
-        const float z = __fsub_rn(t, sh);
-        sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
-        sh = t;
-      }
-    }
-    for (; j < jhi; ++j) {
-      const float av = a[j * ldm];
-      const float2 xv = xs[j];
-      const float p = __fmul_rn(av, xv.x);
-      const float e = fmaf(av, xv.y, fmaf(av, xv.x, -p));
-      const float t = __fadd_rn(sh, p);
-      const float z = __fsub_rn(t, sh);
-      sl = __fadd_rn(sl, __fadd_rn(__fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
-      sh = t;
+    } else {
+      residual_run(a, ldm, xs, jlo, jhi, sh, sl);
     }
     if (live) {
       const double r = J.rhs[i] - ((double)sh + (double)sl);

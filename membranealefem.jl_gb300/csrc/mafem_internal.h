@@ -334,6 +334,11 @@ struct PatchJob {
   long long* trace;     // optional: 6 globaltimer stamps per panel (patch_factor_kernel)
   float* a21;           // split A21 of the current panel: [8][2 a21_rows][4] floats (TF32 hi rows, then lo rows)
   int a21_rows;         // rows per part, a multiple of 128 (patch_a21_rows)
+  // the tangent's sparsity for the refinement residual: unknowns couple only
+  // within 5 x 5 control points (biquadratic elements); null: walk the whole band
+  const int* unk_node;    // [n] control point of each unknown (non-decreasing)
+  const int* node_first;  // [numnp + 1] first unknown of each control point
+  int num1np, num2np;     // the control-point grid
 };
 // Rows per part of a patch's split-A21 buffer for half bandwidth kl.
 int patch_a21_rows(int kl);
