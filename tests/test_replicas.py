@@ -148,3 +148,25 @@ def test_rel_err_vs_oracle_report():
     rep = bench.rel_err_vs_oracle(fake, ref, wl)
     assert rep["steps"] == 3 and rep["bar"] == 1e-9
     assert max(rep["xms"], rep["velocities"], rep["lambda"]) < 1e-11, rep
+
+
+def test_stratified_baseline_sample_covers_every_class():
+    """The bounded bench's plain FP64 baseline on the batching workload: the
+    first patches of every (size, motion) class, weighted so that the weights
+    add up to each class's patch count (and to every patch with no sampling)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    import mafem as M
+    patches = bench.batch_patches(M, dict(bench.BATCH, patches=40))
+    classes = {}
+    for k, (p, _, _, _) in enumerate(patches):
+        classes.setdefault((p.num1el, p.motion), []).append(k)
+    idx, w = bench._baseline_sample(patches, 2)
+    assert sorted(idx) == idx and set(idx) == set(w)
+    for key, ks in classes.items():
+        picked = [k for k in idx if k in ks]
+        assert picked == ks[:2]
+        assert abs(sum(w[k] for k in picked) - len(ks)) < 1e-12
+    assert abs(sum(w.values()) - len(patches)) < 1e-9
+    idx_all, w_all = bench._baseline_sample(patches, 0)
+    assert idx_all == list(range(len(patches))) and all(v == 1.0 for v in w_all.values())
