@@ -434,6 +434,13 @@ def run_batched(steps=None, wl=BATCH, baseline_per_class=0, continuous=True):
                     f_phase[1] += x["ms_factor"]
                     f_phase[2] += x["ms_solve"]
             b_stats = b.stats()
+        tiles = {}
+        for (p, _, _, _), s in zip(patches, fsolvers):
+            key = "LAG" if p.motion == M.LAG else "ALEVB" if p.motion == M.ALEVB else str(p.motion)
+            if key not in tiles:
+                t = s.tangent_tile()
+                if t is not None:
+                    tiles[key] = {"elements_per_cta": t[0], "ms_2": t[1], "ms_4": t[2]}
         f_err, forces = 0.0, []
         for k, s in enumerate(fsolvers):
             if k in seq_state:
@@ -462,6 +469,7 @@ def run_batched(steps=None, wl=BATCH, baseline_per_class=0, continuous=True):
            "rounds": f_rounds, "kernel_launches": f_launch,
            "launches_per_round": f_launch / max(f_rounds, 1),
            "graph_replays": bstats["graph_launches"], "graph_captures": bstats["graph_captures"],
+           "tangent_tile_autotuned": tiles,
            "round_phase_ms": {"assemble": f_phase[0] / max(f_iters, 1), "factor_refine": f_phase[1] / max(f_iters, 1),
                               "update": f_phase[2] / max(f_iters, 1),
                               "note": "device time of the round's phases, averaged over the patches' iterations"},

@@ -428,6 +428,13 @@ int mafem_set_patch_ctas(mafem_handle* h, int32_t ctas);
  * width rule of mafem_set_patch_ctas.  MAFEM_ERR_UNSUPPORTED for a handle the
  * batched FP32 form does not serve. */
 int mafem_autotune_patch(mafem_handle* h);
+/* The batched rounds' FP32 tangent kernel evaluates 2 or 4 elements per CTA
+ * (no reference counterpart).  mafem_batch_create (and a server, when it
+ * admits the first FP32 request of a kind) times both on the first patch of
+ * each motion and element size, once per device, and every round uses the
+ * faster.  This returns that choice for h's kind of patch and the two
+ * measured times (ms); MAFEM_ERR_UNSUPPORTED before it was measured. */
+int mafem_tangent_tile(const mafem_handle* h, int32_t* epb, double* ms_2, double* ms_4);
 
 typedef struct mafem_kernel_times {
   double ms_assemble;         /* element kernel + gathers */

@@ -1400,6 +1400,36 @@ static void choose_patch_ctas(std::vector<mafem_handle*>& hv, const std::vector<
   }
 }
 
+// ---- autotuner of the batched FP32 tangent kernel's elements per CTA -------------------
+// Two or four elements per CTA: four share a CTA's launch overhead, two fit
+// more CTAs on an SM (the kernel holds over 100 registers per thread).  The
+// time of each is measured once per device, motion and element size on the
+// first patch of that kind (CUDA events, the fastest of three launches after
+// one untimed) and the faster is cached for the process.
+namespace {
+using TanShape = std::tuple<int, int, int>;  // device, motion, nq
+std::map<TanShape, int> g_tan_epb;           // guarded by g_tune_mu
+std::map<TanShape, std::array<float, 2>> g_tan_ms;  // ms with 2 and 4 elements per CTA
+TanShape tan_shape(const mafem_handle* h) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return TanShape{dev, h->pp.motion, h->pp.nq};
+}
+}  // namespace
+
+static int tan_epb(const mafem_handle* h) {
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  auto it = g_tan_epb.find(tan_shape(h));
+  return it == g_tan_epb.end() ? 4 : it->second;
+}
+
+// Tunes h's kind of patch if not cached yet, with h's job (slot of d_ajobs)
+// alone in a one-item round written to h_buf (pinned) and d_buf (at least
+// round_layout(1).bytes each) on stream st, which it synchronises.  The
+// patch's element tangents are overwritten (the next assembly rewrites them).
+static int tan_tune(mafem_handle* h, const AsmJob* d_ajobs, int slot, unsigned char* d_buf, unsigned char* h_buf,
+                    cudaStream_t st);
+
 static void order_patch_jobs(std::vector<mafem_handle*>& hv, std::vector<int>& idx, int* n4, int* n2) {
   auto nr = [&](int k) { return patch_ctas(hv[k]); };
   auto cost = [&](int k) { return (double)hv[k]->blk.npan() * hv[k]->L.kl * hv[k]->blk.kuf; };
@@ -1511,6 +1541,74 @@ static AsmJob asm_job(const mafem_handle* h) {
   return a;
 }
 
+static int tan_tune(mafem_handle* h, const AsmJob* d_ajobs, int slot, unsigned char* d_buf, unsigned char* h_buf,
+                    cudaStream_t st) {
+  const TanShape key = tan_shape(h);
+  {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    if (g_tan_epb.count(key)) return MAFEM_OK;
+  }
+  const RoundLayout RL = round_layout(1);
+  AsmItem* item = reinterpret_cast<AsmItem*>(h_buf);
+  item->job = slot;
+  item->start = 0;
+  item->time = h->ss_time;
+  item->dt = h->ss_dt > 0.0 ? h->ss_dt : 1e-3;
+  item->dscale = 1.0;
+  int* off = reinterpret_cast<int*>(h_buf + RL.off[1]);
+  const AsmItem* d_item = reinterpret_cast<const AsmItem*>(d_buf);
+  const int* d_off = reinterpret_cast<const int*>(d_buf + RL.off[1]);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CK(cudaEventCreate(&e0));
+  cudaError_t e = cudaEventCreate(&e1);
+  float best = INFINITY;
+  int best_epb = 4;
+  std::array<float, 2> times{INFINITY, INFINITY};
+  for (int epb : {4, 2}) {
+    if (e != cudaSuccess) break;
+    off[0] = 0;
+    off[1] = batch_tan_ctas(h->numel, epb);
+    e = cudaMemcpyAsync(d_buf, h_buf, RL.bytes, cudaMemcpyHostToDevice, st);
+    float t = INFINITY;
+    for (int r = 0; r < 4 && e == cudaSuccess; ++r) {
+      e = cudaEventRecord(e0, st);
+      if (e == cudaSuccess) e = launch_batch_tan(h->pp.motion, epb, d_ajobs, d_item, d_off, 1, off[1], h->pp.nq, st);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (e == cudaSuccess && r > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) t = std::min(t, ms);
+    }
+    times[epb == 2 ? 0 : 1] = t;
+    if (t < best) {
+      best = t;
+      best_epb = epb;
+    }
+  }
+  cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) {
+    h->err = std::string("tangent kernel autotuning: ") + cudaGetErrorString(e);
+    return MAFEM_ERR_CUDA;
+  }
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tan_epb[key] = best_epb;
+  g_tan_ms[key] = times;
+  return MAFEM_OK;
+}
+
+extern "C" int mafem_tangent_tile(const mafem_handle* h, int32_t* epb, double* ms_2, double* ms_4) {
+  if (!h) return MAFEM_ERR_ARG;
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  const TanShape key = tan_shape(h);
+  auto it = g_tan_epb.find(key);
+  if (it == g_tan_epb.end()) return MAFEM_ERR_UNSUPPORTED;
+  const std::array<float, 2>& t = g_tan_ms[key];
+  if (epb) *epb = it->second;
+  if (ms_2) *ms_2 = t[0];
+  if (ms_4) *ms_4 = t[1];
+  return MAFEM_OK;
+}
+
 struct mafem_batch {
   std::vector<mafem_handle*> hs;
   // batched FP32 solve: the handles whose band fits one CTA (patch_ok)
@@ -1614,6 +1712,14 @@ extern "C" int mafem_batch_create(mafem_handle* const* hs, int32_t n, int32_t ct
       b->rr = std::make_unique<RoundRunner>();
       e = b->rr->init((int)nj);
     }
+    for (int i = 0; i < n && e == cudaSuccess; ++i) {  // the tangent kernel's tile of every kind of patch
+      if (b->slot[i] < 0) continue;
+      const int rc = tan_tune(b->hs[i], b->d_ajobs, b->slot[i], b->rr->d_round, b->rr->h_round, b->rr->st);
+      if (rc != MAFEM_OK) {
+        set_global_error("mafem_batch_create: " + b->hs[i]->err);
+        return rc;
+      }
+    }
     if (e != cudaSuccess) {
       set_global_error(std::string("mafem_batch_create: ") + cudaGetErrorString(e));
       return MAFEM_ERR_CUDA;
@@ -1663,17 +1769,19 @@ static cudaError_t run_round(RoundRunner& R, const PatchJob* d_jobs, const AsmJo
   off[kOffDir] = reinterpret_cast<int*>(R.h_round + dir_off);
   for (int t = 0; t <= kOffDir; ++t) off[t][0] = 0;
   std::vector<int> groups{0};  // item ranges of one (motion, nq)
+  std::vector<int> epb(m);     // the tangent kernel's elements per CTA (the same within a group)
   bool any_pred = false, any_dir = false;
   for (int k = 0; k < m; ++k) {
     const int i = it[k];
     const mafem_handle* h = hv[i];
+    epb[k] = k > 0 && gkey(it[k - 1]) == gkey(i) ? epb[k - 1] : tan_epb(h);
     items[k].job = slot_of[i];
     items[k].start = start[i];
     items[k].time = h->ss_time;
     items[k].dt = h->ss_dt;
     items[k].dscale = dscale[i];
     off[0][k + 1] = off[0][k] + batch_resid_ctas(h->numel);
-    off[1][k + 1] = off[1][k] + batch_tan_ctas(h->numel);
+    off[1][k + 1] = off[1][k] + batch_tan_ctas(h->numel, epb[k]);
     off[2][k + 1] = off[2][k] + batch_gather_ctas(h->L.n);
     off[3][k + 1] = off[3][k] + batch_rgather_ctas(h->nmdf);
     off[4][k + 1] = off[4][k] + newton_update_blocks(h->nmdf);
@@ -1714,8 +1822,8 @@ static cudaError_t run_round(RoundRunner& R, const PatchJob* d_jobs, const AsmJo
       e = launch_batch_resid(h->pp.motion, d_ajobs, d_items + g0, d_off(0, g0), g1 - g0, off[0][g1] - off[0][g0],
                              h->pp.nq, st);
       if (e == cudaSuccess)
-        e = launch_batch_tan(h->pp.motion, d_ajobs, d_items + g0, d_off(1, g0), g1 - g0, off[1][g1] - off[1][g0],
-                             h->pp.nq, st);
+        e = launch_batch_tan(h->pp.motion, epb[g0], d_ajobs, d_items + g0, d_off(1, g0), g1 - g0,
+                             off[1][g1] - off[1][g0], h->pp.nq, st);
     }
     if (e == cudaSuccess) {
       launch_batch_gather(d_ajobs, d_items, d_off(2, 0), m, off[2][m], st);
@@ -1747,6 +1855,7 @@ static cudaError_t run_round(RoundRunner& R, const PatchJob* d_jobs, const AsmJo
     key.push_back((int64_t)items[k].job * 4 + items[k].start);
     key.push_back(((int64_t)h->numel << 32) | (uint32_t)h->numnp);
     key.push_back((h->nmdf << 24) | ((int64_t)h->n_dir << 8) | (h->pp.motion << 4) | (h->ndf & 15));
+    key.push_back(epb[k]);
   }
   for (int k = 0; k < m; ++k) key.push_back(R.h_order[k]);
   auto found = R.graphs.find(key);
@@ -2001,6 +2110,8 @@ struct mafem_server {
   PatchJob* h_jobs = nullptr;  // pinned staging of the job tables
   AsmJob* d_ajobs = nullptr;
   AsmJob* h_ajobs = nullptr;
+  unsigned char* d_tune = nullptr;  // the tangent autotuner's one-item round
+  unsigned char* h_tune = nullptr;  // pinned
   cudaStream_t admin = nullptr;  // job-table uploads
   RoundRunner lanes[kLanes];
   std::vector<ServerReq*> lane_reqs[kLanes];  // the requests of each lane's round in flight
@@ -2022,6 +2133,8 @@ struct mafem_server {
     if (h_jobs) cudaFreeHost(h_jobs);
     if (d_ajobs) cudaFree(d_ajobs);
     if (h_ajobs) cudaFreeHost(h_ajobs);
+    if (d_tune) cudaFree(d_tune);
+    if (h_tune) cudaFreeHost(h_tune);
     if (admin) cudaStreamDestroy(admin);
   }
 };
@@ -2042,6 +2155,8 @@ extern "C" int mafem_server_create(int64_t hbm_budget_bytes, int32_t max_active,
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_jobs, m * sizeof(PatchJob));
   if (e == cudaSuccess) e = cudaMalloc(&s->d_ajobs, m * sizeof(AsmJob));
   if (e == cudaSuccess) e = cudaMallocHost(&s->h_ajobs, m * sizeof(AsmJob));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_tune, round_layout(1).bytes);
+  if (e == cudaSuccess) e = cudaMallocHost(&s->h_tune, round_layout(1).bytes);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->admin, cudaStreamNonBlocking);
   for (RoundRunner& l : s->lanes)
     if (e == cudaSuccess) e = l.init(s->max_active);
@@ -2157,6 +2272,8 @@ extern "C" int mafem_server_round(mafem_server* s, int32_t* n_active, int32_t* n
       cudaMemcpyAsync(s->d_jobs + q->slot, s->h_jobs + q->slot, sizeof(PatchJob), cudaMemcpyHostToDevice, s->admin);
       cudaMemcpyAsync(s->d_ajobs + q->slot, s->h_ajobs + q->slot, sizeof(AsmJob), cudaMemcpyHostToDevice, s->admin);
       cudaStreamSynchronize(s->admin);
+      // the tangent kernel's tile for a kind of patch not seen yet (optional: the default on failure)
+      if (tan_tune(h, s->d_ajobs, q->slot, s->d_tune, s->h_tune, s->admin) != MAFEM_OK) cudaGetLastError();
     }
     s->active.push_back(q);
   }

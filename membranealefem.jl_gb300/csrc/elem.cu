@@ -736,7 +736,8 @@ __global__ void __launch_bounds__(kResEPB * 9) elem_resid_kernel(DevPatch Pt, Ph
 // ---- batched element kernels of the FP32 form: every patch of a round in one launch per motion ----
 // The CTA reads its patch's tables and parameters into shared memory, then runs
 // the single-patch kernel's body on its CTA number within the patch.
-constexpr int kTanEPB = 4;  // elements per CTA of the FP32 tangent kernel
+// elements per CTA of the FP32 tangent kernel: 2 or 4, chosen per motion by
+// the batch's autotuner (fewer elements per CTA, more CTAs per SM)
 template <int MOTION>
 __global__ void __launch_bounds__(kResEPB * 9) batch_resid_kernel(const AsmJob* __restrict__ jobs,
                                                                  const AsmItem* __restrict__ items,
@@ -753,7 +754,7 @@ __global__ void __launch_bounds__(kResEPB * 9) batch_resid_kernel(const AsmJob* 
   __syncthreads();
   resid_body<MOTION>(sP, spp, it.time, it.dt, J->r_el, off[0] + (int)blockIdx.x - off[k], smem_raw);
 }
-template <int MOTION>
+template <int MOTION, int EPB>
 __global__ void batch_tan_kernel(const AsmJob* __restrict__ jobs, const AsmItem* __restrict__ items,
                                  const int* __restrict__ off, int m) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -766,7 +767,7 @@ __global__ void batch_tan_kernel(const AsmJob* __restrict__ jobs, const AsmItem*
   batch_copy(&sP, &J->P, (int)sizeof(DevPatch));
   batch_copy(&spp, &J->pp, (int)sizeof(PhysParams));
   __syncthreads();
-  elem_body<float, float, false, MOTION, kTanEPB>(sP, spp, it.time, it.dt, nullptr, J->K_el, nullptr, 0, 0,
+  elem_body<float, float, false, MOTION, EPB>(sP, spp, it.time, it.dt, nullptr, J->K_el, nullptr, 0, 0,
                                                   off[0] + (int)blockIdx.x - off[k], smem_raw);
 }
 
@@ -852,15 +853,18 @@ cudaError_t launch_elem<float>(const DevPatch& Pt, const PhysParams& pp, double 
 }
 
 int batch_resid_ctas(int numel) { return (numel + kResEPB - 1) / kResEPB; }
-int batch_tan_ctas(int numel) { return (numel + kTanEPB - 1) / kTanEPB; }
+int batch_tan_ctas(int numel, int epb) { return (numel + epb - 1) / epb; }
 
 template <int MOTION>
 static cudaError_t batch_setup_t() {
   cudaError_t e = cudaFuncSetAttribute(batch_resid_kernel<MOTION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)resid_smem(72));
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(batch_tan_kernel<MOTION>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)elem_smem<float, float>(72, kTanEPB));
+    e = cudaFuncSetAttribute(batch_tan_kernel<MOTION, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)elem_smem<float, float>(72, 2));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(batch_tan_kernel<MOTION, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)elem_smem<float, float>(72, 4));
   return e;
 }
 cudaError_t batch_asm_setup() {
@@ -885,19 +889,26 @@ cudaError_t launch_batch_resid(int motion, const AsmJob* jobs, const AsmItem* it
   }
   return cudaGetLastError();
 }
-cudaError_t launch_batch_tan(int motion, const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
-                             int nq, cudaStream_t st) {
-  if (ctas <= 0) return cudaSuccess;
-  const size_t sm = elem_smem<float, float>(nq, kTanEPB);
-  const int thr = kTanEPB * nq;
+template <int EPB>
+static cudaError_t launch_batch_tan_t(int motion, const AsmJob* jobs, const AsmItem* items, const int* off, int m,
+                                      int ctas, int nq, cudaStream_t st) {
+  const size_t sm = elem_smem<float, float>(nq, EPB);
+  const int thr = EPB * nq;
   switch (motion) {
-    case MAFEM_STATIC: batch_tan_kernel<STATIC_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
-    case MAFEM_EUL: batch_tan_kernel<EUL_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
-    case MAFEM_LAG: batch_tan_kernel<LAG_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
-    case MAFEM_ALEV: batch_tan_kernel<ALEV_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
-    default: batch_tan_kernel<ALEVB_><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_STATIC: batch_tan_kernel<STATIC_, EPB><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_EUL: batch_tan_kernel<EUL_, EPB><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_LAG: batch_tan_kernel<LAG_, EPB><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    case MAFEM_ALEV: batch_tan_kernel<ALEV_, EPB><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
+    default: batch_tan_kernel<ALEVB_, EPB><<<ctas, thr, sm, st>>>(jobs, items, off, m); break;
   }
   return cudaGetLastError();
+}
+cudaError_t launch_batch_tan(int motion, int epb, const AsmJob* jobs, const AsmItem* items, const int* off, int m,
+                             int ctas, int nq, cudaStream_t st) {
+  if (ctas <= 0) return cudaSuccess;
+  if (epb == 2) return launch_batch_tan_t<2>(motion, jobs, items, off, m, ctas, nq, st);
+  if (epb == 4) return launch_batch_tan_t<4>(motion, jobs, items, off, m, ctas, nq, st);
+  return cudaErrorInvalidValue;
 }
 
 template size_t elem_smem_bytes<double>(int, int);

@@ -286,7 +286,7 @@ struct AsmOut {  // one patch's results of a round, read by the host
 constexpr int kGatherCols = 4;  // band columns per CTA of the batched gather
 // CTAs per patch of each batched kernel
 int batch_resid_ctas(int numel);
-int batch_tan_ctas(int numel);
+int batch_tan_ctas(int numel, int epb);  // epb: elements per CTA of the tangent kernel, 2 or 4
 inline int batch_gather_ctas(int64_t n) { return (int)((n + kGatherCols - 1) / kGatherCols); }
 inline int batch_rgather_ctas(int64_t nmdf) { return (int)((nmdf + 255) / 256); }
 inline int batch_pred_ctas(int numnp) { return (3 * numnp + 255) / 256; }
@@ -297,8 +297,8 @@ cudaError_t batch_asm_setup();
 // off[0 .. m]); each launch covers CTAs off[0] .. off[m] - 1.
 cudaError_t launch_batch_resid(int motion, const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
                                int nq, cudaStream_t st);
-cudaError_t launch_batch_tan(int motion, const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas,
-                             int nq, cudaStream_t st);
+cudaError_t launch_batch_tan(int motion, int epb, const AsmJob* jobs, const AsmItem* items, const int* off, int m,
+                             int ctas, int nq, cudaStream_t st);
 // Both bands and the residual; the residual gather also zeroes each patch's info words.
 void launch_batch_gather(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas, cudaStream_t st);
 void launch_batch_rgather(const AsmJob* jobs, const AsmItem* items, const int* off, int m, int ctas, cudaStream_t st);

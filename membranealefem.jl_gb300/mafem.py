@@ -201,6 +201,7 @@ def lib():
         L.mafem_batch_destroy.argtypes = [vp]
         L.mafem_batch_set_patch_solve.argtypes = [vp, C.c_int32]
         L.mafem_batch_set_rounds.argtypes = [vp, C.c_int32, C.c_int32]
+        L.mafem_tangent_tile.argtypes = [vp, C.POINTER(C.c_int32), _PD, _PD]
         L.mafem_batch_get_stats.argtypes = [vp, C.POINTER(BatchStats)]
         L.mafem_server_create.argtypes = [C.c_int64, C.c_int32, C.POINTER(vp)]
         L.mafem_server_destroy.argtypes = [vp]
@@ -539,6 +540,18 @@ class Solver:
         of this patch on 1, 2 and 4 CTAs for the round-by-round autotuner; call
         between steps with the GPU otherwise idle."""
         _raise(lib().mafem_autotune_patch(self.h), self.h)
+
+    def tangent_tile(self):
+        """The batched rounds' FP32 tangent kernel for this kind of patch:
+        (elements per CTA chosen, ms with 2, ms with 4), or None before a batch
+        or server has measured it."""
+        e = C.c_int32()
+        m2, m4 = C.c_double(), C.c_double()
+        rc = lib().mafem_tangent_tile(self.h, C.byref(e), C.byref(m2), C.byref(m4))
+        if rc == ERR_UNSUPPORTED:
+            return None
+        _raise(rc, self.h)
+        return int(e.value), float(m2.value), float(m4.value)
 
     def profile_factor(self, time: float, dt: float) -> dict:
         """Per-kernel device time of one assembly + factorisation of the resident state."""

@@ -297,3 +297,25 @@ def test_batched_round_launches_do_not_grow_with_the_patch_count():
     large = ROUND_CASES[:4] + [(m, n1 + 1, n2) for m, n1, n2 in ROUND_CASES[:4]]
     assert per_round(large, True) <= per_round(small, True) + 3
     assert per_round(large, False) > 1.5 * per_round(small, False)
+
+
+def test_tangent_tile_autotuned_per_motion():
+    """mafem_batch_create times the batched FP32 tangent kernel with 2 and 4
+    elements per CTA for each kind of patch and keeps the faster; the choice
+    and both times are reported per kind."""
+    solvers = []
+    try:
+        for motion, n in ((M.LAG, 10), (M.ALEVB, 12)):
+            p, _, mesh, xms, cps = _round_setup(motion, n, n)
+            s = M.Solver(mesh, p, M.FP32_REFINE)
+            s.upload(xms, cps)
+            solvers.append(s)
+        with M.Batch(solvers) as b:
+            assert b.set_patch_solve(True)
+            for s in solvers:
+                epb, ms2, ms4 = s.tangent_tile()
+                assert epb in (2, 4) and ms2 > 0 and ms4 > 0
+                assert (ms2 if epb == 2 else ms4) == min(ms2, ms4)
+    finally:
+        for s in solvers:
+            s.close()
