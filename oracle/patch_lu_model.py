@@ -201,3 +201,38 @@ def double_float_residual(ab0: np.ndarray, kl: int, b: np.ndarray, x: np.ndarray
         sl[i] = (sl[i] + (corr + e).astype(f32)).astype(f32)
         sh[i] = t
     return b - (sh.astype(np.float64) + sl.astype(np.float64))
+
+
+def coupled_runs(unk_node: np.ndarray, node_first: np.ndarray, num1np: int, num2np: int, rb: int, n: int,
+                 kl: int) -> list[tuple[int, int]]:
+    """The column runs [j0, j1) that the batched refinement residual walks for
+    the 32 rows rb .. rb + 31 (patch_residual in band_lu_patch.cu), in
+    increasing order: grid row g couples to points [s1a - 2, W) through the
+    rows' points on grid row s2a, to [0, s1b + 2] through those on grid row
+    s2b, and to the whole grid row through any grid row between them; each
+    run clipped to the band window [rb - kl, rb + 32 + kl)."""
+    W, H = num1np, num2np
+    jlo, jhi = max(rb - kl, 0), min(n, rb + 32 + kl)
+    na, nb = int(unk_node[rb]), int(unk_node[min(rb + 31, n - 1)])
+    s1a, s2a, s1b, s2b = na % W, na // W, nb % W, nb // W
+    runs = []
+    for g in range(max(s2a - 2, 0), min(s2b + 2, H - 1) + 1):
+        c0, c1, d0, d1 = 0, -1, 0, -1
+        fa, fb = abs(g - s2a) <= 2, abs(g - s2b) <= 2
+        fm = s2b - s2a >= 2 and s2a - 1 <= g <= s2b + 1
+        if s2a == s2b:
+            c0, c1 = max(s1a - 2, 0), min(s1b + 2, W - 1)
+        elif fm or (fa and fb and s1b + 3 >= s1a - 2):
+            c1 = W - 1
+        else:
+            if fb:
+                c1 = min(s1b + 2, W - 1)
+            if fa:
+                d0, d1 = max(s1a - 2, 0), W - 1
+        for e0, e1 in ((c0, c1), (d0, d1)):
+            if e1 < e0:
+                continue
+            j0, j1 = max(int(node_first[g * W + e0]), jlo), min(int(node_first[g * W + e1 + 1]), jhi)
+            if j0 < j1:
+                runs.append((j0, j1))
+    return runs

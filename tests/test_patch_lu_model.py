@@ -90,3 +90,45 @@ def test_predicted_correction_stop_keeps_the_error_bound(motion, n, tol):
     assert info == 0
     x64, _ = lapack.dgbtrs(f, kl, kl, -r, piv)
     assert np.linalg.norm(x_pred - x64) <= 2 * tol * np.linalg.norm(x64)
+
+
+@pytest.mark.parametrize("motion,n1,n2", [(M.ALEVB, 12, 12), (M.LAG, 9, 9), (M.ALEVB, 16, 10), (M.LAG, 5, 7),
+                                          (M.ALEV, 7, 7), (M.EUL, 6, 8)])
+def test_refinement_residual_runs_cover_the_tangent(motion, n1, n2):
+    """The batched refinement residual walks only the columns a warp's 32 rows
+    couple to (patch_residual): on the oracle's assembled tangent every
+    nonzero of those rows lies in one of the runs, and the runs are increasing,
+    disjoint and inside the band window -- so the double-float sums equal the
+    walk of the whole window, whose other entries are stored zeros."""
+    p, q = params_pair(motion, M.F_PULL, n1, n2, pull_speed=0.3, pull_centre=1)
+    mesh, om = M.Mesh(p), O.Mesh(q)
+    xms, cps = state(p, mesh, seed=1, amp=1e-3)
+    r, ab = om.calc_r_K(xms, cps, 0.01, 0.01, nthreads=2)
+    kl = om.half_bw
+    K = PM.dense_from_band(ab, kl, dtype=np.float64)
+    n = K.shape[0]
+    ID = np.asarray(mesh.ID)
+    if ID.shape[0] != mesh.numnp:
+        ID = ID.T
+    unk_node = np.zeros(n, dtype=int)
+    for nd in range(mesh.numnp):
+        for d in range(mesh.ndf):
+            if ID[nd, d] > 0:
+                unk_node[ID[nd, d] - 1] = nd
+    assert np.all(np.diff(unk_node) >= 0)  # the kernel's precondition (checked again at mafem_create)
+    node_first = np.concatenate([[0], np.cumsum(np.bincount(unk_node, minlength=mesh.numnp))])
+    walked = full = 0
+    for rb in range(0, n, 32):
+        runs = PM.coupled_runs(unk_node, node_first, mesh.num1np, mesh.num2np, rb, n, kl)
+        jlo, jhi = max(rb - kl, 0), min(n, rb + 32 + kl)
+        cover = np.zeros(n, dtype=bool)
+        last = jlo
+        for j0, j1 in runs:
+            assert last <= j0 < j1 <= jhi
+            last = j1
+            cover[j0:j1] = True
+            walked += j1 - j0
+        full += jhi - jlo
+        nz = np.nonzero(np.any(K[rb:min(rb + 32, n)] != 0, axis=0))[0]
+        assert np.all(cover[nz])
+    assert walked < full
