@@ -1485,6 +1485,9 @@ struct RoundRunner {
   std::vector<int> items_of;  // the last round's result rows: index of each row's handle
   bool busy = false;
 
+  RoundRunner() = default;
+  RoundRunner(const RoundRunner&) = delete;  // owns its streams, events, buffers and graphs
+  RoundRunner& operator=(const RoundRunner&) = delete;
   cudaError_t init(int max_patches) {
     cap = max_patches;
     const size_t rb = round_layout(cap).bytes + (size_t)(cap + 1) * sizeof(int) + 16;
